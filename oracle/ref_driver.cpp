@@ -1,0 +1,132 @@
+// Test infrastructure only: a small driver linked against the reference's own
+// sources (compiled by oracle/Makefile from the read-only reference tree).  It
+// runs the reference's RSVD operators exactly as src/Halko.cpp:271-345 does,
+// but writes U, S, V, F and the column permutation at full double precision
+// (the reference's text writers keep 6 significant digits, src/Data.cpp:215).
+//
+// usage: ref_driver OUTDIR <PCAone command-line options, e.g. -b prefix -k 10 -d 2>
+//
+// Outputs (numpy .npy, float64 column-major / int64):
+//   F.npy         allele frequencies after the AF pass (src/FilePlink.cpp:33-62)
+//   U.npy S.npy V.npy   final operator state (src/Halko.cpp:46-97)
+//   perm.npy      the in-core column permutation (src/RSVD.hpp:61-78), if any
+//   Omg0.npy      the initial random test matrix (src/Halko.cpp:15-23)
+//   G0.npy        optional (--dump-g0 as first option): the decoded, centred
+//                 matrix before standardisation (N x M), small inputs only
+#define _DECLARE_TOOLBOX_HERE
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "FilePlink.hpp"
+#include "Halko.hpp"
+#include "Utils.hpp"
+
+namespace {
+
+void write_npy(const std::string& path, const char* descr, const void* data, size_t elem,
+               std::vector<long long> shape, bool fortran) {
+  std::string hdr = std::string("{'descr': '") + descr + "', 'fortran_order': " +
+                    (fortran ? "True" : "False") + ", 'shape': (";
+  for (size_t i = 0; i < shape.size(); ++i) hdr += std::to_string(shape[i]) + ", ";
+  hdr += "), }";
+  size_t total = 10 + hdr.size() + 1;
+  size_t pad = (64 - total % 64) % 64;
+  hdr.append(pad, ' ');
+  hdr += '\n';
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) throw std::runtime_error("cannot write " + path);
+  const char magic[] = "\x93NUMPY\x01\x00";
+  std::fwrite(magic, 1, 8, f);
+  uint16_t hl = (uint16_t)hdr.size();
+  std::fwrite(&hl, 2, 1, f);
+  std::fwrite(hdr.data(), 1, hdr.size(), f);
+  size_t n = 1;
+  for (auto s : shape) n *= (size_t)s;
+  std::fwrite(data, elem, n, f);
+  std::fclose(f);
+}
+
+void dump(const std::string& dir, const char* name, const Mat2D& m) {
+  write_npy(dir + "/" + name + ".npy", "<f8", m.data(), 8, {(long long)m.rows(), (long long)m.cols()}, true);
+}
+void dump1(const std::string& dir, const char* name, const Mat1D& v) {
+  write_npy(dir + "/" + name + ".npy", "<f8", v.data(), 8, {(long long)v.size()}, false);
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 3) {
+    std::fprintf(stderr, "usage: %s OUTDIR [--dump-g0] <PCAone options>\n", argv[0]);
+    return 2;
+  }
+  std::string outdir = argv[1];
+  bool dump_g0 = false;
+  std::vector<char*> args;
+  args.push_back(argv[0]);
+  for (int i = 2; i < argc; ++i) {
+    if (std::strcmp(argv[i], "--dump-g0") == 0) {
+      dump_g0 = true;
+      continue;
+    }
+    args.push_back(argv[i]);
+  }
+  Param params((int)args.size(), args.data());
+  cao.cao.open(outdir + "/ref.log");
+  cao.is_screen = false;
+  if (params.file_t != FileType::PLINK) {
+    std::fprintf(stderr, "only PLINK input is driven here\n");
+    return 2;
+  }
+  Data* data = new FileBed(params);
+  data->prepare();
+  dump1(outdir, "F", data->F);
+  if (dump_g0) dump(outdir, "G0", data->G);
+
+  // operator selection and call sequence of run_pca_with_halko (src/Halko.cpp:271-320)
+  RsvdOpData* rsvd;
+  if (params.svd_t == SvdType::PCAoneAlg2)
+    rsvd = new FancyRsvdOpData(data, params.k, params.oversamples);
+  else
+    rsvd = new NormalRsvdOpData(data, params.k, params.oversamples);
+  dump(outdir, "Omg0", rsvd->Omg);
+  int em_iters = 0;
+  if (!params.missme) {
+    rsvd->setFlags(false, params.ld ? false : true);
+    rsvd->computeUSV(params.maxp, params.tol);
+  } else {
+    rsvd->setFlags(false, false);
+    rsvd->computeUSV(params.maxp, params.tol);
+    flip_UV(rsvd->U, rsvd->V, false);
+    for (uint i = 0; i < params.maxiter; ++i) {
+      rsvd->setFlags(true, false);
+      Mat2D Vpre = rsvd->V;
+      rsvd->computeUSV(params.maxp, params.tol);
+      flip_UV(rsvd->U, rsvd->V, false);
+      double diff = params.mev ? 1.0 - mev(rsvd->V, Vpre) : minSSE(rsvd->V, Vpre).sum() / Vpre.cols();
+      em_iters = (int)i + 1;
+      if (diff < params.tolem) break;
+    }
+    if (params.emu) {
+      rsvd->setFlags(true, true);
+      rsvd->computeUSV(params.maxp, params.tol);
+      flip_UV(rsvd->U, rsvd->V, false);
+    }
+  }
+  dump(outdir, "U", rsvd->U);
+  dump1(outdir, "S", rsvd->S);
+  dump(outdir, "V", rsvd->V);
+  if (data->perm.indices().size() > 0) {
+    std::vector<long long> p(data->perm.indices().size());
+    for (size_t i = 0; i < p.size(); ++i) p[i] = data->perm.indices()[i];
+    write_npy(outdir + "/perm.npy", "<i8", p.data(), 8, {(long long)p.size()}, false);
+  }
+  std::vector<long long> meta = {(long long)data->nsamples, (long long)data->nsnps, em_iters};
+  write_npy(outdir + "/meta.npy", "<i8", meta.data(), 8, {3}, false);
+  delete rsvd;
+  delete data;
+  return 0;
+}

@@ -1,0 +1,92 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Run in a container that has the reference tree (the fixtures are committed;
+tests never run this):
+
+    make -C oracle ref            # builds oracle/_ref/ref_driver from the reference sources
+    python tests/golden/make_golden.py
+
+Each case draws a seeded synthetic PLINK fileset (pcaone_gb300.synthetic),
+runs the reference's RSVD operators through oracle/_ref/ref_driver with the
+listed PCAone options, and stores the packed genotypes, the options and the
+reference's full-precision outputs (F, U, S, V, the column permutation, the
+initial random matrix, the EM iteration count and a SHA-256 of the decoded
+centred matrix) in <case>.npz.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from pcaone_gb300 import synthetic  # noqa: E402
+
+DRIVER = os.path.join(REPO, "oracle", "_ref", "ref_driver")
+
+# name -> (population model kwargs, PCAone options)
+CASES = {
+    # odd N (padding lanes carry garbage bits), winSVD with 16 windows
+    "wsvd_n301": (dict(nsamples=301, nsnps=2400, npop=3, fst=0.1, seed=11, mcar=0.01, pad_garbage=True),
+                  ["-d", "2", "-k", "4", "--maxp", "6", "-w", "16"]),
+    # winSVD with the default 64 windows and k=10 (the CLI keeps p=10)
+    "wsvd_n500_k10": (dict(nsamples=500, nsnps=4000, npop=3, fst=0.05, seed=12, mcar=0.01),
+                      ["-d", "2", "-k", "10", "--maxp", "6"]),
+    # winSVD without the column shuffle, uniform random test matrix, 5 PCs
+    "wsvd_noshuffle_uniform": (dict(nsamples=256, nsnps=2048, npop=4, fst=0.08, seed=13, mcar=0.02),
+                               ["-d", "2", "-S", "-k", "5", "--maxp", "8", "-w", "8", "--rand", "0"]),
+    # single-pass RSVD with power iterations
+    "ssvd_n203": (dict(nsamples=203, nsnps=1500, npop=3, fst=0.1, seed=5, mcar=0.05, pad_garbage=True),
+                  ["-d", "1", "-k", "3", "--maxp", "4"]),
+    # EMU on the window method without shuffle (the in-core shuffled EMU path
+    # scales permuted columns with unpermuted frequencies, src/Data.cpp:328,355)
+    "em_wsvd_noshuffle": (dict(nsamples=203, nsnps=1500, npop=3, fst=0.1, seed=5, mcar=0.05, pad_garbage=True),
+                          ["-d", "2", "-S", "--emu", "--maxiter", "8", "--maxp", "6", "-k", "3", "-w", "16"]),
+    # EMU on the single-pass method
+    "em_ssvd": (dict(nsamples=160, nsnps=1200, npop=3, fst=0.1, seed=7, mcar=0.08),
+                ["-d", "1", "--emu", "--maxiter", "5", "--maxp", "3", "-k", "2"]),
+}
+
+
+def run_case(name: str, model_kw: dict, opts: list) -> dict:
+    kw = dict(model_kw)
+    pad_garbage = kw.pop("pad_garbage", False)
+    model = synthetic.draw_population_model(**kw)
+    packed = synthetic.sample_packed_bed(model, pad_garbage=pad_garbage)
+    with tempfile.TemporaryDirectory() as td:
+        prefix = os.path.join(td, name)
+        synthetic.write_plink(prefix, packed, model.nsamples)
+        out = os.path.join(td, "out")
+        os.makedirs(out)
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        subprocess.check_call([DRIVER, out, "--dump-g0", "-b", prefix] + opts, env=env)
+        res = {k: np.load(os.path.join(out, k + ".npy")) for k in ("F", "U", "S", "V", "Omg0", "meta")}
+        g0 = np.load(os.path.join(out, "G0.npy"))
+        res["G0_sha256"] = np.frombuffer(hashlib.sha256(np.asfortranarray(g0).tobytes(order="F")).digest(),
+                                         dtype=np.uint8)
+        if os.path.exists(os.path.join(out, "perm.npy")):
+            res["perm"] = np.load(os.path.join(out, "perm.npy"))
+    res["packed"] = packed
+    res["options"] = np.array(json.dumps(opts))
+    return res
+
+
+def main() -> None:
+    if not os.path.exists(DRIVER):
+        sys.exit("build the reference driver first: make -C oracle ref")
+    for name, (mkw, opts) in CASES.items():
+        res = run_case(name, mkw, opts)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+        print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"])
+
+
+if __name__ == "__main__":
+    main()
