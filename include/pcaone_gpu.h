@@ -1,0 +1,151 @@
+/*
+ * pcaone_gpu.h -- C-ABI of the GB300 randomized-SVD hot path.
+ *
+ * The library replaces, for the in-core PLINK path, the reference's
+ * RSVD operator interface (class RsvdOpData, src/Halko.hpp:6-42) and the data
+ * it reads (class Data / FileBed, src/Data.hpp:9-59, src/FilePlink.hpp:7-47).
+ * Every entry point takes plain pointers and sizes, returns 0 on success or a
+ * negative PCAONE_E* code, and keeps the message of the last failure for
+ * pcaone_gpu_last_error().  Matrices crossing the boundary are column-major
+ * doubles, the layout of the reference's Eigen Mat2D.
+ *
+ * One context drives one GPU from one host thread; contexts are not
+ * thread-safe.  All device memory belongs to the context.
+ */
+#ifndef PCAONE_GPU_H_
+#define PCAONE_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PCAONE_GPU_ABI_VERSION 1
+
+/* status codes */
+#define PCAONE_OK 0
+#define PCAONE_E_ARG -1       /* invalid argument or call order */
+#define PCAONE_E_CUDA -2      /* CUDA runtime error */
+#define PCAONE_E_NOMEM -3     /* device allocation failed */
+#define PCAONE_E_FORMAT -4    /* malformed input (e.g. bad .bed magic) */
+#define PCAONE_E_NUMERIC -5   /* numerical breakdown (non-SPD Gram, NaN) */
+#define PCAONE_E_LIMIT -6     /* size beyond a documented limit */
+
+/* precision of the block products G = X*Omega and H = X^T*G */
+#define PCAONE_PREC_FP32 0    /* FP32 SIMT products, FP64 window sums */
+#define PCAONE_PREC_BF16 1    /* tcgen05 tensor-core products, BF16 operands */
+#define PCAONE_PREC_FP8 2     /* tcgen05 tensor-core products, FP8 e4m3 operands */
+
+/* SVD method (Param::svd_t, src/Cmd.hpp:14) */
+#define PCAONE_SVD_SINGLE 1   /* NormalRsvdOpData: single-pass RSVD, -d 1 */
+#define PCAONE_SVD_WINDOW 2   /* FancyRsvdOpData: window-based winSVD, -d 2 */
+
+/* Largest supported sketch width k + oversamples. */
+#define PCAONE_MAX_L 112
+
+typedef struct pcaone_gpu_ctx pcaone_gpu_ctx;
+
+typedef struct {
+  int device;   /* CUDA device ordinal */
+  int verbose;  /* 0 silent, 1 per-epoch lines on stderr like the reference's log */
+} pcaone_gpu_desc;
+
+/* The subset of Param (src/Cmd.hpp:16-98) the RSVD path reads.  Callers apply
+ * the CLI's derived settings themselves, as Param::Param does
+ * (src/Cmd.cpp:216 oversamples >= k, :228-232 maxiter, :238 perm). */
+typedef struct {
+  int svd;          /* PCAONE_SVD_SINGLE or PCAONE_SVD_WINDOW */
+  int k;            /* number of PCs */
+  int oversamples;  /* p; sketch width L = k + p <= PCAONE_MAX_L */
+  int maxp;         /* maximum power iterations (epochs - 1) */
+  int bands;        /* winSVD windows, power of two >= 4 (-w) */
+  int seed;         /* random-matrix seed (--seed) */
+  int rand;         /* 1 Gaussian, 0 uniform(-1,1) test matrix (--rand) */
+  int perm;         /* shuffle SNP columns before winSVD (true for -d 2 without -S) */
+  int emu;          /* EM imputation of missing genotypes (--emu) */
+  int maxiter;      /* EM iterations (--maxiter) */
+  double tol;       /* RSVD tolerance (--tol-rsvd) */
+  double tolem;     /* EM tolerance (--tol-em) */
+  int ploidy;       /* 2 for diploid (standardisation sqrt(ploidy)/sd) */
+  int standardize;  /* 1: per-SNP genetic standardisation (scale == -9) */
+  int precision;    /* PCAONE_PREC_* */
+} pcaone_gpu_params;
+
+/* Fills p with the reference's defaults (src/Cmd.hpp:29-95). */
+void pcaone_gpu_default_params(pcaone_gpu_params* p);
+
+/* ---- context ------------------------------------------------------------ */
+int pcaone_gpu_open(const pcaone_gpu_desc* desc, pcaone_gpu_ctx** out);
+int pcaone_gpu_close(pcaone_gpu_ctx* ctx);
+const char* pcaone_gpu_last_error(const pcaone_gpu_ctx* ctx);
+int pcaone_gpu_abi_version(void);
+/* wall-clock split of the last run_halko/compute_usv call, seconds:
+ * t[0] total, t[1] block products, t[2] QR/SVD, t[3] EM fill */
+int pcaone_gpu_timings(const pcaone_gpu_ctx* ctx, double t[4]);
+
+/* ---- data: replaces FileBed::read_all (src/FilePlink.cpp:26-120) --------- */
+/* packed: the .bed body after the 3 magic bytes, nsnps rows of (nsamples+3)/4
+ * bytes in SNP-major order (host memory; copied to HBM). */
+int pcaone_gpu_load_bed(pcaone_gpu_ctx* ctx, const uint8_t* packed, uint64_t nsnps, uint32_t nsamples);
+/* Same, from a whole .bed file image including its 3 magic bytes; checks the
+ * magic like src/FilePlink.hpp:24-27 and the size like FilePlink.cpp:125-126. */
+int pcaone_gpu_load_bed_file_image(pcaone_gpu_ctx* ctx, const uint8_t* image, uint64_t image_bytes,
+                                   uint64_t nsnps, uint32_t nsamples);
+/* Same, from device memory already holding the packed rows (row pitch
+ * src_pitch bytes). */
+int pcaone_gpu_load_bed_device(pcaone_gpu_ctx* ctx, const void* dev_packed, uint64_t src_pitch,
+                               uint64_t nsnps, uint32_t nsamples);
+/* Per-SNP genotype counts (nsnps x 4 int32, row-major: n00 two A1 copies,
+ * n01 missing, n10 heterozygous, n11 no A1 copy) and allele frequency F
+ * (FilePlink.cpp:37-55, bit-exact).  Either pointer may be NULL. */
+int pcaone_gpu_counts(pcaone_gpu_ctx* ctx, int32_t* counts, double* F);
+
+/* Test and benchmark utility with no counterpart in the reference: fills the
+ * context's genotype matrix on the device from the seeded Balding-Nichols
+ * model of pcaone_gb300/synthetic.py (host arrays: freq nsnps x npop and
+ * weights nsamples x npop row-major, miss_sample nsamples, miss_snp nsnps),
+ * then counts like the load functions.  Bytes equal the numpy generator's. */
+int pcaone_gpu_load_synthetic(pcaone_gpu_ctx* ctx, uint64_t nsnps, uint32_t nsamples, int npop,
+                              const double* freq, const double* weights, const double* miss_sample,
+                              const double* miss_snp, uint64_t seed);
+/* Copies the resident packed genotypes back (nsnps rows of (nsamples+3)/4
+ * bytes, the .bed body). */
+int pcaone_gpu_get_bed(pcaone_gpu_ctx* ctx, uint8_t* packed);
+
+/* ---- operator: replaces RsvdOpData and subclasses (src/Halko.hpp) ------- */
+/* Constructor of Normal/FancyRsvdOpData: draws Omega (initOmg, Halko.cpp:15-23). */
+int pcaone_gpu_op_init(pcaone_gpu_ctx* ctx, const pcaone_gpu_params* params);
+/* Replace the initial random matrix (N x L column-major) by the caller's own
+ * draw; this and every later op_init / initOmg use it until the data is
+ * reloaded or omega is NULL (which restores the library's draw).  May be
+ * called before or after pcaone_gpu_op_init. */
+int pcaone_gpu_set_omega(pcaone_gpu_ctx* ctx, const double* omega, uint32_t rows, uint32_t cols);
+/* RsvdOpData::setFlags (Halko.hpp:32-35). */
+int pcaone_gpu_set_flags(pcaone_gpu_ctx* ctx, int update, int standardize);
+/* computeGandH (Halko.cpp:99-269, in-core branches): one epoch pi.  G (M x L)
+ * and H (N x L) are copied out when non-NULL. */
+int pcaone_gpu_compute_g_and_h(pcaone_gpu_ctx* ctx, int pi, double* G, double* H);
+/* RsvdOpData::computeUSV (Halko.cpp:46-97): epochs until convergence.
+ * U (N x k), S (k), V (M x k, rows in the working SNP order) when non-NULL. */
+int pcaone_gpu_compute_usv(pcaone_gpu_ctx* ctx, int p, double tol, double* U, double* S, double* V,
+                           int* epochs);
+/* run_pca_with_halko (Halko.cpp:271-320, non-LD PLINK path) including the EM
+ * loop; outputs like compute_usv, em_iters may be NULL. */
+int pcaone_gpu_run_halko(pcaone_gpu_ctx* ctx, const pcaone_gpu_params* params, double* U, double* S,
+                         double* V, int* em_iters);
+/* The working SNP order: perm[i] = original SNP of column i (Data::perm,
+ * src/Data.hpp:49); identity when no shuffle was applied. */
+int pcaone_gpu_get_perm(pcaone_gpu_ctx* ctx, int32_t* perm);
+
+/* ---- Arnoldi matvec: replaces ArnoldiOpData::perform_op (Arnoldi.cpp:18-46) */
+/* y = X X^T x over the loaded genotypes (X samples x SNPs, centred, scaled
+ * when standardize != 0), x and y of length N. */
+int pcaone_gpu_matvec(pcaone_gpu_ctx* ctx, const double* x, double* y, int standardize);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PCAONE_GPU_H_ */

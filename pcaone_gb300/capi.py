@@ -1,0 +1,236 @@
+"""ctypes binding of the C-ABI in include/pcaone_gpu.h.
+
+The library is the in-tree build pcaone_gb300/lib/libpcaone_gb300.so (see
+pcaone_gb300/build.py).  There is no fallback: if the library is missing or a
+call fails, an exception is raised.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_uint32, c_uint64, c_void_p
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "lib", "libpcaone_gb300.so")
+
+PCAONE_OK = 0
+ERRORS = {-1: "PCAONE_E_ARG", -2: "PCAONE_E_CUDA", -3: "PCAONE_E_NOMEM", -4: "PCAONE_E_FORMAT",
+          -5: "PCAONE_E_NUMERIC", -6: "PCAONE_E_LIMIT"}
+PREC_FP32, PREC_BF16, PREC_FP8 = 0, 1, 2
+SVD_SINGLE, SVD_WINDOW = 1, 2
+MAX_L = 112
+
+# every symbol include/pcaone_gpu.h declares
+EXPORTS = [
+    "pcaone_gpu_default_params", "pcaone_gpu_open", "pcaone_gpu_close", "pcaone_gpu_last_error",
+    "pcaone_gpu_abi_version", "pcaone_gpu_timings", "pcaone_gpu_load_bed", "pcaone_gpu_load_bed_file_image",
+    "pcaone_gpu_load_bed_device", "pcaone_gpu_counts", "pcaone_gpu_op_init", "pcaone_gpu_set_omega",
+    "pcaone_gpu_set_flags", "pcaone_gpu_compute_g_and_h", "pcaone_gpu_compute_usv", "pcaone_gpu_run_halko",
+    "pcaone_gpu_get_perm", "pcaone_gpu_matvec", "pcaone_gpu_load_synthetic", "pcaone_gpu_get_bed",
+]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("svd", c_int), ("k", c_int), ("oversamples", c_int), ("maxp", c_int), ("bands", c_int),
+                ("seed", c_int), ("rand", c_int), ("perm", c_int), ("emu", c_int), ("maxiter", c_int),
+                ("tol", c_double), ("tolem", c_double), ("ploidy", c_int), ("standardize", c_int),
+                ("precision", c_int)]
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [("device", c_int), ("verbose", c_int)]
+
+
+class PcaoneError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str = LIBPATH) -> ctypes.CDLL:
+    """Load the library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA library not built: {path} (run pcaone_gb300/build.py)")
+    lib = ctypes.CDLL(path)
+    P = POINTER
+    lib.pcaone_gpu_default_params.argtypes = [P(Params)]
+    lib.pcaone_gpu_default_params.restype = None
+    lib.pcaone_gpu_open.argtypes = [P(Desc), P(c_void_p)]
+    lib.pcaone_gpu_close.argtypes = [c_void_p]
+    lib.pcaone_gpu_last_error.argtypes = [c_void_p]
+    lib.pcaone_gpu_last_error.restype = c_char_p
+    lib.pcaone_gpu_abi_version.argtypes = []
+    lib.pcaone_gpu_timings.argtypes = [c_void_p, c_void_p]
+    lib.pcaone_gpu_load_bed.argtypes = [c_void_p, c_void_p, c_uint64, c_uint32]
+    lib.pcaone_gpu_load_bed_file_image.argtypes = [c_void_p, c_void_p, c_uint64, c_uint64, c_uint32]
+    lib.pcaone_gpu_load_bed_device.argtypes = [c_void_p, c_void_p, c_uint64, c_uint64, c_uint32]
+    lib.pcaone_gpu_counts.argtypes = [c_void_p, c_void_p, c_void_p]
+    lib.pcaone_gpu_op_init.argtypes = [c_void_p, P(Params)]
+    lib.pcaone_gpu_set_omega.argtypes = [c_void_p, c_void_p, c_uint32, c_uint32]
+    lib.pcaone_gpu_set_flags.argtypes = [c_void_p, c_int, c_int]
+    lib.pcaone_gpu_compute_g_and_h.argtypes = [c_void_p, c_int, c_void_p, c_void_p]
+    lib.pcaone_gpu_compute_usv.argtypes = [c_void_p, c_int, c_double, c_void_p, c_void_p, c_void_p, P(c_int)]
+    lib.pcaone_gpu_run_halko.argtypes = [c_void_p, P(Params), c_void_p, c_void_p, c_void_p, P(c_int)]
+    lib.pcaone_gpu_get_perm.argtypes = [c_void_p, c_void_p]
+    lib.pcaone_gpu_matvec.argtypes = [c_void_p, c_void_p, c_void_p, c_int]
+    lib.pcaone_gpu_load_synthetic.argtypes = [c_void_p, c_uint64, c_uint32, c_int, c_void_p, c_void_p, c_void_p,
+                                              c_void_p, c_uint64]
+    lib.pcaone_gpu_get_bed.argtypes = [c_void_p, c_void_p]
+    for name in EXPORTS:
+        if name not in ("pcaone_gpu_default_params", "pcaone_gpu_last_error"):
+            getattr(lib, name).restype = c_int
+    _lib = lib
+    return lib
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    load().pcaone_gpu_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class Context:
+    """One GPU context (pcaone_gpu_open / pcaone_gpu_close)."""
+
+    def __init__(self, device: int = 0, verbose: int = 0):
+        self.lib = load()
+        self.h = c_void_p()
+        d = Desc(device, verbose)
+        rc = self.lib.pcaone_gpu_open(ctypes.byref(d), ctypes.byref(self.h))
+        if rc != PCAONE_OK:
+            raise PcaoneError(rc, "pcaone_gpu_open failed (no usable CUDA device?)")
+        self.nsamples = 0
+        self.nsnps = 0
+        self.L = 0
+        self.k = 0
+
+    def close(self):
+        if self.h:
+            self.lib.pcaone_gpu_close(self.h)
+            self.h = c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != PCAONE_OK:
+            msg = self.lib.pcaone_gpu_last_error(self.h)
+            raise PcaoneError(rc, msg.decode() if msg else "")
+
+    # ---- data ----
+    def load_bed(self, packed: np.ndarray, nsamples: int):
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        self._check(self.lib.pcaone_gpu_load_bed(self.h, _ptr(packed), packed.shape[0], nsamples))
+        self.nsamples, self.nsnps = int(nsamples), int(packed.shape[0])
+
+    def load_bed_file_image(self, image: bytes, nsnps: int, nsamples: int):
+        buf = np.frombuffer(image, dtype=np.uint8)
+        self._check(self.lib.pcaone_gpu_load_bed_file_image(self.h, _ptr(buf), buf.size, nsnps, nsamples))
+        self.nsamples, self.nsnps = int(nsamples), int(nsnps)
+
+    def load_bed_device(self, dev_ptr: int, pitch: int, nsnps: int, nsamples: int):
+        self._check(self.lib.pcaone_gpu_load_bed_device(self.h, c_void_p(dev_ptr), pitch, nsnps, nsamples))
+        self.nsamples, self.nsnps = int(nsamples), int(nsnps)
+
+    def load_synthetic(self, model):
+        """Generate ``model`` (synthetic.PopulationModel) on the device."""
+        fr = np.ascontiguousarray(model.freq, dtype=np.float64)
+        w = np.ascontiguousarray(model.weights, dtype=np.float64)
+        ms = np.ascontiguousarray(model.miss_sample, dtype=np.float64)
+        mj = np.ascontiguousarray(model.miss_snp, dtype=np.float64)
+        self._check(self.lib.pcaone_gpu_load_synthetic(self.h, model.nsnps, model.nsamples, model.npop, _ptr(fr),
+                                                       _ptr(w), _ptr(ms), _ptr(mj), model.seed))
+        self.nsamples, self.nsnps = int(model.nsamples), int(model.nsnps)
+
+    def get_bed(self):
+        out = np.empty((self.nsnps, (self.nsamples + 3) // 4), dtype=np.uint8)
+        self._check(self.lib.pcaone_gpu_get_bed(self.h, _ptr(out)))
+        return out
+
+    def counts(self):
+        cnt = np.empty((self.nsnps, 4), dtype=np.int32)
+        F = np.empty(self.nsnps, dtype=np.float64)
+        self._check(self.lib.pcaone_gpu_counts(self.h, _ptr(cnt), _ptr(F)))
+        return cnt, F
+
+    # ---- operator ----
+    def op_init(self, params: Params):
+        self._check(self.lib.pcaone_gpu_op_init(self.h, ctypes.byref(params)))
+        self.k, self.L = params.k, params.k + params.oversamples
+
+    def set_omega(self, omega):
+        if omega is None:
+            self._check(self.lib.pcaone_gpu_set_omega(self.h, None, 0, 0))
+            return
+        om = np.asfortranarray(omega, dtype=np.float64)
+        self._check(self.lib.pcaone_gpu_set_omega(self.h, _ptr(om), om.shape[0], om.shape[1]))
+
+    def set_flags(self, update: bool, standardize: bool):
+        self._check(self.lib.pcaone_gpu_set_flags(self.h, int(update), int(standardize)))
+
+    def compute_g_and_h(self, pi: int):
+        G = np.empty((self.nsnps, self.L), dtype=np.float64, order="F")
+        H = np.empty((self.nsamples, self.L), dtype=np.float64, order="F")
+        self._check(self.lib.pcaone_gpu_compute_g_and_h(self.h, pi, _ptr(G), _ptr(H)))
+        return G, H
+
+    def _outs(self):
+        U = np.empty((self.nsamples, self.k), dtype=np.float64, order="F")
+        S = np.empty(self.k, dtype=np.float64)
+        V = np.empty((self.nsnps, self.k), dtype=np.float64, order="F")
+        return U, S, V
+
+    def compute_usv(self, p: int, tol: float):
+        U, S, V = self._outs()
+        ep = c_int(0)
+        self._check(self.lib.pcaone_gpu_compute_usv(self.h, p, tol, _ptr(U), _ptr(S), _ptr(V), ctypes.byref(ep)))
+        return U, S, V, ep.value
+
+    def run_halko(self, params: Params, want_v: bool = True):
+        self.k, self.L = params.k, params.k + params.oversamples
+        U, S, V = self._outs()
+        it = c_int(0)
+        self._check(self.lib.pcaone_gpu_run_halko(self.h, ctypes.byref(params), _ptr(U), _ptr(S),
+                                                  _ptr(V) if want_v else None, ctypes.byref(it)))
+        return U, S, (V if want_v else None), it.value
+
+    def perm(self):
+        out = np.empty(self.nsnps, dtype=np.int32)
+        self._check(self.lib.pcaone_gpu_get_perm(self.h, _ptr(out)))
+        return out
+
+    def matvec(self, x: np.ndarray, standardize: bool = True):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty_like(x)
+        self._check(self.lib.pcaone_gpu_matvec(self.h, _ptr(x), _ptr(y), int(standardize)))
+        return y
+
+    def timings(self):
+        t = np.zeros(4, dtype=np.float64)
+        self._check(self.lib.pcaone_gpu_timings(self.h, _ptr(t)))
+        return dict(total=t[0], products=t[1], qr_svd=t[2], em_fill=t[3])

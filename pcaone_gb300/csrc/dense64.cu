@@ -1,0 +1,680 @@
+// FP64 dense kernels of the RSVD driver: tall-skinny Gram / cross products,
+// Cholesky and triangular inverse of (k+p)^2 matrices, tall x small products,
+// the Householder sign rule, flipOmg, the Jacobi eigensolver for the small
+// SVD of B, mev, the EM fill and the Arnoldi matvec.
+//
+// Tall matrices (N x L, M x L) are row-major with leading dimension LP (the
+// sketch width padded to a multiple of 8; padding columns are zero).  Small
+// matrices are LP x LP row-major.
+#include <algorithm>
+
+#include "internal.cuh"
+
+namespace pcaone {
+
+namespace {
+
+constexpr int kRowsTile = 32;
+
+// part[b] = A[rows of block b]^T B[rows of block b] (na x nb entries, row-major
+// na x nb).  sym: A == B and only the upper triangle is formed (mirrored by the
+// reduction).  FP64 products and sums.
+__global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict__ A, int lda, int na,
+                                                       const double* __restrict__ B, int ldb, int nb, int64_t rows,
+                                                       int64_t rows_per_block, int sym, double* __restrict__ part) {
+  extern __shared__ double sm[];
+  double* As = sm;                       // kRowsTile x na
+  double* Bs = sm + kRowsTile * na;      // kRowsTile x nb
+  uint16_t* pi = reinterpret_cast<uint16_t*>(Bs + kRowsTile * nb);
+  uint16_t* pj = pi + na * nb;
+  const int tid = threadIdx.x;
+  int nent = 0;
+  if (sym) {
+    nent = na * (na + 1) / 2;
+    for (int e = tid; e < nent; e += blockDim.x) {
+      // row i of the upper triangle starts at i*na - i*(i-1)/2
+      int i = 0, base = 0;
+      while (base + (na - i) <= e) { base += na - i; ++i; }
+      pi[e] = (uint16_t)i;
+      pj[e] = (uint16_t)(i + (e - base));
+    }
+  } else {
+    nent = na * nb;
+    for (int e = tid; e < nent; e += blockDim.x) {
+      pi[e] = (uint16_t)(e / nb);
+      pj[e] = (uint16_t)(e % nb);
+    }
+  }
+  const int64_t r0 = blockIdx.x * rows_per_block;
+  const int64_t r1 = min(r0 + rows_per_block, rows);
+  double acc[64];
+#pragma unroll
+  for (int q = 0; q < 64; ++q) acc[q] = 0.0;
+  __syncthreads();
+  for (int64_t rt = r0; rt < r1; rt += kRowsTile) {
+    const int nr = (int)min((int64_t)kRowsTile, r1 - rt);
+    for (int e = tid; e < kRowsTile * na; e += blockDim.x) {
+      const int r = e / na, c = e % na;
+      As[e] = r < nr ? A[(rt + r) * lda + c] : 0.0;
+    }
+    if (!sym)
+      for (int e = tid; e < kRowsTile * nb; e += blockDim.x) {
+        const int r = e / nb, c = e % nb;
+        Bs[e] = r < nr ? B[(rt + r) * ldb + c] : 0.0;
+      }
+    __syncthreads();
+    const double* Bt = sym ? As : Bs;
+    const int ldt = sym ? na : nb;
+#pragma unroll
+    for (int q = 0; q < 64; ++q) {
+      const int e = tid + q * 256;
+      if (e < nent) {
+        const int i = pi[e], j = pj[e];
+        double s = acc[q];
+        for (int r = 0; r < kRowsTile; ++r) s = fma(As[r * na + i], Bt[r * ldt + j], s);
+        acc[q] = s;
+      }
+    }
+    __syncthreads();
+  }
+  double* out = part + (size_t)blockIdx.x * na * nb;
+#pragma unroll
+  for (int q = 0; q < 64; ++q) {
+    const int e = tid + q * 256;
+    if (e < nent) out[pi[e] * nb + pj[e]] = acc[q];
+  }
+}
+
+// W (ldw columns) = sum over blocks of part; sym mirrors the upper triangle.
+__global__ void k_cross_reduce(const double* __restrict__ part, int nblocks, int na, int nb, int sym,
+                               double* __restrict__ W, int ldw) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= na * nb) return;
+  const int i = e / nb, j = e % nb;
+  if (sym && j < i) return;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; ++b) s += part[(size_t)b * na * nb + e];
+  W[i * ldw + j] = s;
+  if (sym) W[j * ldw + i] = s;
+}
+
+__global__ void k_zero(double* p, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0.0;
+}
+
+// Cholesky W = R^T R of the leading L x L block (right-looking, in shared
+// memory) and R^{-1} by back substitution; the padding block of R and Rinv is
+// the identity.  status: 0 ok, 1 non-positive or non-finite pivot.
+__global__ void k_chol_inv(const double* __restrict__ W, int L, int LP, double shift, double* __restrict__ R,
+                           double* __restrict__ Rinv, int* __restrict__ status) {
+  extern __shared__ double a[];  // L x L
+  __shared__ int fail;
+  const int tid = threadIdx.x;
+  if (tid == 0) fail = 0;
+  for (int e = tid; e < L * L; e += blockDim.x) {
+    const int i = e / L, j = e % L;
+    a[e] = W[i * LP + j] + (i == j ? shift : 0.0);
+  }
+  __syncthreads();
+  for (int k = 0; k < L; ++k) {
+    if (tid == 0) {
+      const double d = a[k * L + k];
+      if (!(d > 0.0) || !isfinite(d)) fail = 1;
+      a[k * L + k] = d > 0.0 ? sqrt(d) : 1.0;
+    }
+    __syncthreads();
+    const double dk = a[k * L + k];
+    for (int j = k + 1 + tid; j < L; j += blockDim.x) a[k * L + j] /= dk;
+    __syncthreads();
+    const int m = L - k - 1;
+    for (int e = tid; e < m * m; e += blockDim.x) {
+      const int i = k + 1 + e / m, j = k + 1 + e % m;
+      if (j >= i) a[i * L + j] -= a[k * L + i] * a[k * L + j];
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < LP * LP; e += blockDim.x) {
+    const int i = e / LP, j = e % LP;
+    double v;
+    if (i < L && j < L)
+      v = j >= i ? a[i * L + j] : 0.0;
+    else
+      v = i == j ? 1.0 : 0.0;
+    R[e] = v;
+  }
+  __syncthreads();
+  // Rinv column c: X[c][c] = 1/R[c][c]; X[i][c] = -(sum_{t=i+1..c} R[i][t] X[t][c]) / R[i][i]
+  for (int c = tid; c < LP; c += blockDim.x) {
+    for (int i = LP - 1; i >= 0; --i) {
+      double v;
+      if (i > c) {
+        v = 0.0;
+      } else if (i >= L) {
+        v = i == c ? 1.0 : 0.0;
+      } else if (i == c) {
+        v = 1.0 / a[i * L + i];
+      } else {
+        double s = 0.0;
+        for (int t = i + 1; t <= c && t < L; ++t) s += a[i * L + t] * Rinv[t * LP + c];
+        v = -s / a[i * L + i];
+      }
+      Rinv[i * LP + c] = v;
+    }
+  }
+  if (tid == 0) *status = fail;
+}
+
+// C[rows x n] = A[rows x LP] * B[LP x n]; B and a 32-row tile of A in shared
+// memory; thread (row r, column group cg) forms columns cg, cg+8, ...
+// C may alias A (ldc == LP, n <= LP): each CTA reads a row tile into shared
+// memory before it writes the same rows.
+__global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows, int LP,
+                                                   const double* __restrict__ B, int ldb, int n, double* C,
+                                                   int ldc) {
+  extern __shared__ double sm[];
+  double* Bs = sm;              // LP x n
+  double* As = sm + LP * n;     // 32 x LP
+  const int tid = threadIdx.x;
+  for (int e = tid; e < LP * n; e += blockDim.x) Bs[e] = B[(e / n) * ldb + (e % n)];
+  const int r = tid >> 3, cg = tid & 7;
+  for (int64_t rt = (int64_t)blockIdx.x * kRowsTile; rt < rows; rt += (int64_t)gridDim.x * kRowsTile) {
+    __syncthreads();
+    for (int e = tid; e < kRowsTile * LP; e += blockDim.x) {
+      const int64_t row = rt + e / LP;
+      As[e] = row < rows ? A[row * LP + (e % LP)] : 0.0;
+    }
+    __syncthreads();
+    const int64_t row = rt + r;
+    if (row < rows) {
+      for (int c = cg; c < n; c += 8) {
+        double s = 0.0;
+        for (int t = 0; t < LP; ++t) s = fma(As[r * LP + t], Bs[t * n + c], s);
+        C[row * ldc + c] = s;
+      }
+    }
+  }
+}
+
+// Signs d_i an Eigen/LAPACK Householder QR gives its Q relative to the
+// positive-diagonal factor: the modified LU of the top L x L block of the
+// orthonormal Q (Ballard et al., "Reconstructing Householder vectors from
+// tall-skinny QR", 2015): s_i = -sign(a_ii) with sign(0) = +1, a_ii -= s_i,
+// then eliminate below the pivot.  Mirrors beta = -sign(c0)*norm of the
+// reflector (Eigen makeHouseholder; LAPACK dlarfg).
+__global__ void k_house_signs(const double* __restrict__ Q, int L, int LP, double* __restrict__ sgn) {
+  extern __shared__ double a[];  // L x L
+  const int tid = threadIdx.x;
+  for (int e = tid; e < L * L; e += blockDim.x) a[e] = Q[(e / L) * LP + (e % L)];
+  __syncthreads();
+  for (int i = 0; i < L; ++i) {
+    if (tid == 0) {
+      const double s = a[i * L + i] >= 0.0 ? -1.0 : 1.0;
+      sgn[i] = s;
+      a[i * L + i] -= s;
+    }
+    __syncthreads();
+    const int m = L - i - 1;
+    const double piv = a[i * L + i];
+    for (int e = tid; e < m * m; e += blockDim.x) {
+      const int r = i + 1 + e / m, c = i + 1 + e % m;
+      a[r * L + c] -= a[r * L + i] / piv * a[i * L + c];
+    }
+    __syncthreads();
+  }
+  for (int c = L + tid; c < LP; c += blockDim.x) sgn[c] = 1.0;
+}
+
+__global__ void k_scale_cols(double* __restrict__ Q, int64_t rows, int LP, const double* __restrict__ sgn) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= rows * LP) return;
+  Q[idx] *= sgn[idx % LP];
+}
+
+// column sums of |o2 - o| and |o2 + o| over a slab of rows
+__global__ void k_flip_partial(const double* __restrict__ o2, const double* __restrict__ o, int64_t rows, int LP,
+                               int64_t rows_per_block, double* __restrict__ part) {
+  const int c = threadIdx.x;
+  if (c >= LP) return;
+  const int64_t r0 = blockIdx.x * rows_per_block, r1 = min(r0 + rows_per_block, rows);
+  double dm = 0.0, dp = 0.0;
+  for (int64_t r = r0; r < r1; ++r) {
+    const double a = o2[r * LP + c], b = o[r * LP + c];
+    dm += fabs(a - b);
+    dp += fabs(a + b);
+  }
+  part[((size_t)blockIdx.x * 2 + 0) * LP + c] = dm;
+  part[((size_t)blockIdx.x * 2 + 1) * LP + c] = dp;
+}
+
+__global__ void k_flip_flags(const double* __restrict__ part, int nblocks, int L, int LP, double* __restrict__ sgn) {
+  const int c = threadIdx.x;
+  if (c >= LP) return;
+  double dm = 0.0, dp = 0.0;
+  for (int b = 0; b < nblocks; ++b) {
+    dm += part[((size_t)b * 2 + 0) * LP + c];
+    dp += part[((size_t)b * 2 + 1) * LP + c];
+  }
+  sgn[c] = (c < L && dm > 2.0 * dp) ? -1.0 : 1.0;
+}
+
+__global__ void k_flip_apply(double* __restrict__ o2, double* __restrict__ o, int64_t n, int LP,
+                             const double* __restrict__ sgn) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const double v = o[idx] * sgn[idx % LP];
+  o[idx] = v;
+  o2[idx] = v;
+}
+
+__global__ void k_add(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ c, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) c[i] = a[i] + b[i];
+}
+
+__global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
+// C = A * B for LP x LP row-major (single CTA)
+__global__ void k_mult_small(const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C,
+                             int LP) {
+  for (int e = threadIdx.x; e < LP * LP; e += blockDim.x) {
+    const int i = e / LP, j = e % LP;
+    double s = 0.0;
+    for (int t = 0; t < LP; ++t) s = fma(A[i * LP + t], B[t * LP + j], s);
+    C[e] = s;
+  }
+}
+
+// Rayleigh-Ritz / small SVD of B = R^{-T} H^T through C = B B^T =
+// Rinv^T (H^T H) Rinv, eigen-decomposed by the cyclic Jacobi method with
+// round-robin parallel ordering (Golub & Van Loan, Matrix Computations,
+// sections 8.5.2 and 8.5.5).  Outputs: UB (LP x LP, eigenvectors by column,
+// sorted by decreasing eigenvalue), sigma (L) = sqrt(eigenvalues) and
+// T = Rinv * UB[:, :k] * diag(1/sigma_k) (LP x k) so that the right singular
+// vectors of B are H*T.  Single CTA; C and the eigenvectors in shared memory.
+__global__ void __launch_bounds__(1024) k_usv_small(const double* __restrict__ Rinv, const double* __restrict__ Wh,
+                                                    int L, int LP, int k, double* __restrict__ UB,
+                                                    double* __restrict__ sigma, double* __restrict__ T,
+                                                    double* __restrict__ tmp, int* __restrict__ status) {
+  extern __shared__ double sm[];
+  double* C = sm;              // L x L
+  double* V = sm + L * L;      // L x L, V[m*L + p] = component m of vector p
+  __shared__ int order[128];
+  __shared__ double cs[64], sn[64];
+  __shared__ int pp[64], qq[64];
+  __shared__ double offn, dn;
+  __shared__ int perm_sorted[128];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // tmp = Wh * Rinv (L x L), then C = Rinv^T * tmp
+  for (int e = tid; e < L * L; e += nt) {
+    const int i = e / L, j = e % L;
+    double s = 0.0;
+    for (int t = 0; t <= j; ++t) s = fma(Wh[i * LP + t], Rinv[t * LP + j], s);
+    tmp[e] = s;
+  }
+  __syncthreads();
+  for (int e = tid; e < L * L; e += nt) {
+    const int i = e / L, j = e % L;
+    double s = 0.0;
+    for (int t = 0; t <= i; ++t) s = fma(Rinv[t * LP + i], tmp[t * L + j], s);
+    C[e] = s;
+    V[e] = (i == j) ? 1.0 : 0.0;
+  }
+  const int n = (L + 1) & ~1;  // even player count; index L (if L odd) is a bye
+  for (int i = tid; i < n; i += nt) order[i] = i;
+  __syncthreads();
+  // symmetrise
+  for (int e = tid; e < L * L; e += nt) {
+    const int i = e / L, j = e % L;
+    if (j > i) {
+      const double m = 0.5 * (C[i * L + j] + C[j * L + i]);
+      C[i * L + j] = m;
+      C[j * L + i] = m;
+    }
+  }
+  __syncthreads();
+  int sweep = 0;
+  for (; sweep < 60; ++sweep) {
+    if (tid == 0) {
+      offn = 0.0;
+      dn = 0.0;
+    }
+    __syncthreads();
+    // convergence test on the Frobenius norms
+    double lo = 0.0, ld = 0.0;
+    for (int e = tid; e < L * L; e += nt) {
+      const int i = e / L, j = e % L;
+      const double v = C[e] * C[e];
+      if (i == j) ld += v; else lo += v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      lo += __shfl_xor_sync(0xffffffffu, lo, o);
+      ld += __shfl_xor_sync(0xffffffffu, ld, o);
+    }
+    if ((tid & 31) == 0) {
+      atomicAdd(&offn, lo);
+      atomicAdd(&dn, ld);
+    }
+    __syncthreads();
+    if (!(offn > 1e-30 * dn) || L < 2) break;
+    for (int round = 0; round < n - 1; ++round) {
+      // rotation parameters for the n/2 disjoint pairs of this round
+      for (int pr = tid; pr < n / 2; pr += nt) {
+        int p = order[pr], q = order[n - 1 - pr];
+        if (p > q) { const int t = p; p = q; q = t; }
+        pp[pr] = p;
+        qq[pr] = q;
+        double c = 1.0, s = 0.0;
+        if (q < L) {
+          const double apq = C[p * L + q];
+          if (fabs(apq) > 1e-300) {
+            const double tau = (C[q * L + q] - C[p * L + p]) / (2.0 * apq);
+            const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + t * t);
+            s = t * c;
+          }
+        }
+        cs[pr] = c;
+        sn[pr] = s;
+      }
+      __syncthreads();
+      // C <- J^T C (rows p, q)
+      for (int e = tid; e < (n / 2) * L; e += nt) {
+        const int pr = e / L, m = e % L;
+        const int p = pp[pr], q = qq[pr];
+        if (q >= L) continue;
+        const double c = cs[pr], s = sn[pr];
+        const double ap = C[p * L + m], aq = C[q * L + m];
+        C[p * L + m] = c * ap - s * aq;
+        C[q * L + m] = s * ap + c * aq;
+      }
+      __syncthreads();
+      // C <- C J (columns p, q) and V <- V J
+      for (int e = tid; e < (n / 2) * L; e += nt) {
+        const int pr = e / L, m = e % L;
+        const int p = pp[pr], q = qq[pr];
+        if (q >= L) continue;
+        const double c = cs[pr], s = sn[pr];
+        const double ap = C[m * L + p], aq = C[m * L + q];
+        C[m * L + p] = c * ap - s * aq;
+        C[m * L + q] = s * ap + c * aq;
+        const double vp = V[m * L + p], vq = V[m * L + q];
+        V[m * L + p] = c * vp - s * vq;
+        V[m * L + q] = s * vp + c * vq;
+      }
+      __syncthreads();
+      if (tid == 0) {  // round-robin: keep order[0], rotate the rest
+        const int last = order[n - 1];
+        for (int i = n - 1; i > 1; --i) order[i] = order[i - 1];
+        order[1] = last;
+      }
+      __syncthreads();
+    }
+  }
+  // sort by decreasing eigenvalue
+  if (tid == 0) {
+    for (int i = 0; i < L; ++i) perm_sorted[i] = i;
+    for (int i = 0; i < L; ++i) {
+      int best = i;
+      for (int j = i + 1; j < L; ++j)
+        if (C[perm_sorted[j] * L + perm_sorted[j]] > C[perm_sorted[best] * L + perm_sorted[best]]) best = j;
+      const int t = perm_sorted[i];
+      perm_sorted[i] = perm_sorted[best];
+      perm_sorted[best] = t;
+    }
+    *status = sweep >= 60 ? 2 : 0;
+  }
+  __syncthreads();
+  for (int e = tid; e < LP * LP; e += nt) {
+    const int i = e / LP, j = e % LP;
+    UB[e] = (i < L && j < L) ? V[i * L + perm_sorted[j]] : (i == j ? 1.0 : 0.0);
+  }
+  for (int j = tid; j < L; j += nt) {
+    const double lam = C[perm_sorted[j] * L + perm_sorted[j]];
+    sigma[j] = sqrt(lam > 0.0 ? lam : 0.0);
+  }
+  __syncthreads();
+  // T = Rinv * UB[:, :k] * diag(1/sigma)
+  for (int e = tid; e < LP * k; e += nt) {
+    const int i = e / k, j = e % k;
+    double s = 0.0;
+    if (i < L)
+      for (int t = i; t < L; ++t) s = fma(Rinv[i * LP + t], V[t * L + perm_sorted[j]], s);
+    const double sg = sqrt(fmax(C[perm_sorted[j] * L + perm_sorted[j]], 0.0));
+    T[e] = sg > 0.0 ? s / sg : 0.0;
+  }
+}
+
+// mev(X, Y) = (1/k) sum_i || X^T y_i ||  from M = X^T Y (k x k)
+__global__ void k_mev_finish(const double* __restrict__ Mxy, int k, double* __restrict__ out) {
+  __shared__ double acc;
+  if (threadIdx.x == 0) acc = 0.0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < k; ++j) s += Mxy[j * k + i] * Mxy[j * k + i];
+    atomicAdd(&acc, sqrt(s));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *out = acc / k;
+}
+
+// EM fill (Data::fit_with_pi EMU branches, src/Data.cpp:318-348): missing entry
+// (position p, sample i) <- clamp(sum_k U[i][k] S[k] V[p][k], -F_j, 1 - F_j),
+// F of the SNP at position p.
+__global__ void k_em_fill(const int32_t* __restrict__ epos, const int32_t* __restrict__ sample,
+                          double* __restrict__ value, int64_t nnz, const int32_t* __restrict__ perm,
+                          const double* __restrict__ F, const double* __restrict__ U, const double* __restrict__ S,
+                          const double* __restrict__ V, int k) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= nnz) return;
+  const int64_t p = epos[e];
+  const int64_t i = sample[e];
+  const int64_t snp = perm ? (int64_t)perm[p] : p;
+  double t = 0.0;
+  for (int q = 0; q < k; ++q) t += U[i * k + q] * S[q] * V[p * k + q];
+  const double f = F[snp];
+  value[e] = fmin(fmax(t, -f), 1.0 - f);
+}
+
+// Arnoldi matvec, first half: t[j] = sum_i x(i,j) * xin[i] (one warp per SNP)
+__global__ void k_matvec_t(BedView v, const double* __restrict__ F, const double* __restrict__ scale,
+                           const double* __restrict__ xin, double* __restrict__ t) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= v.nsnps) return;
+  const double f = F[warp], s = scale[warp];
+  const double tab[4] = {(1.0 - f) * s, 0.0, (0.5 - f) * s, (0.0 - f) * s};
+  const uint8_t* row = v.bed + warp * v.stride;
+  double acc = 0.0;
+  const int nbytes = (v.nsamples + 3) >> 2;
+  for (int b = lane; b < nbytes; b += 32) {
+    const uint32_t w = row[b];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = b * 4 + q;
+      if (i < v.nsamples) {
+        const uint32_t c = (w >> (2 * q)) & 3u;
+        const double x = c == 0 ? tab[0] : (c == 1 ? 0.0 : (c == 2 ? tab[2] : tab[3]));
+        acc = fma(x, xin[i], acc);
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) t[warp] = acc;
+}
+
+// second half: ypart[split][i] = sum_{j in split} x(i,j) * t[j]
+__global__ void k_matvec_y(BedView v, const double* __restrict__ F, const double* __restrict__ scale,
+                           const double* __restrict__ t, int64_t per_split, double* __restrict__ ypart) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= v.nsamples) return;
+  const int64_t j0 = blockIdx.y * per_split, j1 = min(j0 + per_split, v.nsnps);
+  double acc = 0.0;
+  const int64_t byte = i >> 2;
+  const int sh = 2 * (int)(i & 3);
+  for (int64_t j = j0; j < j1; ++j) {
+    const uint32_t c = (v.bed[j * v.stride + byte] >> sh) & 3u;
+    if (c == 1u) continue;
+    const double g = c == 0 ? 1.0 : (c == 2 ? 0.5 : 0.0);
+    acc = fma((g - F[j]) * scale[j], t[j], acc);
+  }
+  ypart[(size_t)blockIdx.y * v.nsamples + i] = acc;
+}
+
+__global__ void k_matvec_reduce(const double* __restrict__ ypart, int nsplit, int n, double* __restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int b = 0; b < nsplit; ++b) s += ypart[(size_t)b * n + i];
+  y[i] = s;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+
+int cross_blocks(int64_t rows) { return (int)std::max<int64_t>(1, std::min<int64_t>(304, (rows + 63) / 64)); }
+
+size_t cross_smem(int na, int nb, int sym) {
+  (void)sym;
+  return sizeof(double) * kRowsTile * (na + nb) + 2 * sizeof(uint16_t) * na * nb + 64;
+}
+
+void launch_cross(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int sym,
+                  double* W, int ldw, double* part, int nblocks, cudaStream_t s) {
+  if (na * nb > 64 * 256 || na > 0xffff) throw Error(-6, "cross product wider than 128 x 128");
+  if (rows == 0) {
+    k_zero<<<ceil_div((int64_t)na * ldw, 256), 256, 0, s>>>(W, (int64_t)na * ldw);
+    PCAONE_LAUNCH_CHECK();
+    return;
+  }
+  const int64_t per = round_up64((rows + nblocks - 1) / nblocks, kRowsTile);
+  nblocks = (int)((rows + per - 1) / per);
+  const size_t smem = cross_smem(na, nb, sym);
+  static bool attr_set = false;
+  if (!attr_set) {
+    PCAONE_CUDA(cudaFuncSetAttribute(k_cross_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set = true;
+  }
+  k_cross_partial<<<nblocks, 256, smem, s>>>(A, lda, na, sym ? A : B, sym ? lda : ldb, nb, rows, per, sym, part);
+  PCAONE_LAUNCH_CHECK();
+  k_cross_reduce<<<ceil_div((int64_t)na * nb, 256), 256, 0, s>>>(part, nblocks, na, nb, sym, W, ldw);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_chol_inv_shift(const double* W, int L, int LP, double shift, double* R, double* Rinv, int* status,
+                           cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    PCAONE_CUDA(cudaFuncSetAttribute(k_chol_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set = true;
+  }
+  k_chol_inv<<<1, 256, sizeof(double) * L * L, s>>>(W, L, LP, shift, R, Rinv, status);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_gemm_tall(const double* A, int64_t rows, int LP, const double* B, int ldb, int n, double* C, int ldc,
+                      cudaStream_t s) {
+  if (rows == 0) return;
+  static bool attr_set = false;
+  if (!attr_set) {
+    PCAONE_CUDA(cudaFuncSetAttribute(k_gemm_tall, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set = true;
+  }
+  const size_t smem = sizeof(double) * ((size_t)LP * n + (size_t)kRowsTile * LP);
+  const int grid = (int)std::min<int64_t>((rows + kRowsTile - 1) / kRowsTile, 152 * 8);
+  k_gemm_tall<<<grid, 256, smem, s>>>(A, rows, LP, B, ldb, n, C, ldc);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_house_signs(double* Q, int64_t rows, int L, int LP, double* sgn, cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    PCAONE_CUDA(cudaFuncSetAttribute(k_house_signs, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set = true;
+  }
+  k_house_signs<<<1, 256, sizeof(double) * L * L, s>>>(Q, L, LP, sgn);
+  PCAONE_LAUNCH_CHECK();
+  k_scale_cols<<<ceil_div(rows * LP, 256), 256, 0, s>>>(Q, rows, LP, sgn);
+  PCAONE_LAUNCH_CHECK();
+}
+
+int flip_blocks(int64_t rows) { return (int)std::max<int64_t>(1, std::min<int64_t>(304, (rows + 255) / 256)); }
+
+void launch_flip_omg(double* omg2, double* omg, int64_t rows, int L, int LP, double* part, double* sgn,
+                     cudaStream_t s) {
+  int nb = flip_blocks(rows);
+  const int64_t per = (rows + nb - 1) / nb;
+  nb = (int)((rows + per - 1) / per);
+  k_flip_partial<<<nb, 128, 0, s>>>(omg2, omg, rows, LP, per, part);
+  PCAONE_LAUNCH_CHECK();
+  k_flip_flags<<<1, 128, 0, s>>>(part, nb, L, LP, sgn);
+  PCAONE_LAUNCH_CHECK();
+  k_flip_apply<<<ceil_div(rows * LP, 256), 256, 0, s>>>(omg2, omg, rows * LP, LP, sgn);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_add(const double* a, const double* b, double* c, int64_t n, cudaStream_t s) {
+  if (n == 0) return;
+  k_add<<<ceil_div(n, 256), 256, 0, s>>>(a, b, c, n);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_to_f32(const double* a, float* b, int64_t n, cudaStream_t s) {
+  if (n == 0) return;
+  k_to_f32<<<ceil_div(n, 256), 256, 0, s>>>(a, b, n);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_mult_small(const double* A, const double* B, double* C, int LP, cudaStream_t s) {
+  k_mult_small<<<1, 256, 0, s>>>(A, B, C, LP);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_usv_small(const double* Rinv, const double* Wh, int L, int LP, int k, double* UB, double* sigma,
+                      double* T, double* tmp, int* status, cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    PCAONE_CUDA(cudaFuncSetAttribute(k_usv_small, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
+    attr_set = true;
+  }
+  k_usv_small<<<1, 1024, sizeof(double) * 2 * L * L, s>>>(Rinv, Wh, L, LP, k, UB, sigma, T, tmp, status);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_mev(const double* X, const double* Y, int64_t rows, int k, double* out, double* W, double* part,
+                int nblocks, cudaStream_t s) {
+  launch_cross(X, k, k, Y, k, k, rows, 0, W, k, part, nblocks, s);
+  k_mev_finish<<<1, 128, 0, s>>>(W, k, out);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_em_fill(const int32_t* epos, const int32_t* sample, double* value, int64_t nnz, const int32_t* perm,
+                    const double* F, const double* U, const double* S, const double* V, int k, cudaStream_t s) {
+  if (nnz == 0) return;
+  k_em_fill<<<ceil_div(nnz, 256), 256, 0, s>>>(epos, sample, value, nnz, perm, F, U, S, V, k);
+  PCAONE_LAUNCH_CHECK();
+}
+
+int matvec_splits(int64_t nsnps, int nsamples) {
+  const int xt = ceil_div(nsamples, 256);
+  int sp = std::max(1, 1216 / std::max(1, xt));
+  return (int)std::min<int64_t>(sp, std::max<int64_t>(1, nsnps));
+}
+
+void launch_matvec(const BedView& v, const double* F, const double* scale, const double* x, double* t,
+                   double* y, double* ypart, int nsplit, cudaStream_t s) {
+  k_matvec_t<<<ceil_div(v.nsnps * 32, 256), 256, 0, s>>>(v, F, scale, x, t);
+  PCAONE_LAUNCH_CHECK();
+  const int64_t per = (v.nsnps + nsplit - 1) / nsplit;
+  dim3 grid(ceil_div(v.nsamples, 256), nsplit);
+  k_matvec_y<<<grid, 256, 0, s>>>(v, F, scale, t, per, ypart);
+  PCAONE_LAUNCH_CHECK();
+  k_matvec_reduce<<<ceil_div(v.nsamples, 256), 256, 0, s>>>(ypart, nsplit, v.nsamples, y);
+  PCAONE_LAUNCH_CHECK();
+}
+
+}  // namespace pcaone

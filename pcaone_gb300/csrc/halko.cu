@@ -1,0 +1,842 @@
+// Host side of the RSVD operator: the GPU counterparts of RsvdOpData,
+// NormalRsvdOpData and FancyRsvdOpData (reference src/Halko.hpp, src/Halko.cpp)
+// and of the Data/FileBed state they read, plus the C-ABI of include/pcaone_gpu.h.
+//
+// Layout in HBM (one context):
+//   bed      nsnps x stride bytes, stride = npad/4 (npad = N rounded up to 128)
+//   F        nsnps doubles, counts nsnps x 4 int32
+//   Omega    npad x LP doubles (+ FP32 copy), rows >= N and columns >= L zero
+//   H, H1, H2  npad x LP doubles;  G  nsnps x LP doubles (rows in working order)
+//   U        npad x k, V nsnps x k (row-major), S k
+// where L = k + oversamples and LP = L rounded up to 8.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/pcaone_gpu.h"
+#include "internal.cuh"
+
+namespace pcaone {
+
+void host_random_omega(int seed, int gaussian, int64_t rows, int64_t cols, double* out_colmajor);
+void host_shuffle_columns(int64_t n, int32_t* out);
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  // (re)allocates when the size changes; contents are zeroed when `zero`
+  void ensure(size_t count, cudaStream_t s, bool zero = true) {
+    if (count == 0) count = 1;
+    if (count != n) {
+      release();
+      PCAONE_CUDA(cudaMalloc(&p, count * sizeof(T)));
+      n = count;
+    }
+    if (zero) PCAONE_CUDA(cudaMemsetAsync(p, 0, count * sizeof(T), s));
+  }
+};
+
+using clk = std::chrono::steady_clock;
+static double secs(clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); }
+
+struct Context {
+  int device = 0;
+  int verbose = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  double t_total = 0, t_prod = 0, t_qr = 0, t_em = 0;
+
+  // ---- data (Data / FileBed) ----
+  int N = 0;
+  int npad = 0;
+  int64_t M = 0;
+  int64_t stride = 0;
+  bool have_data = false;
+  DBuf<uint8_t> bed;
+  DBuf<int32_t> counts;
+  DBuf<double> F;
+  std::vector<int32_t> counts_host;  // filled lazily
+
+  // missing entries in working order (EM)
+  int64_t nnz = -1;
+  DBuf<int64_t> miss_rowptr;
+  DBuf<int32_t> miss_pos, miss_sample;
+  DBuf<double> miss_value;
+  bool miss_valid = false;
+
+  // ---- operator (RsvdOpData) ----
+  bool have_op = false;
+  pcaone_gpu_params P{};
+  int L = 0, LP = 0, k = 0;
+  bool update = false, standardize = false, scaled = false, fitted = false;
+  std::vector<double> omega0;  // N x L column-major (host)
+  std::vector<double> omega_user;  // caller-supplied initial matrix (pcaone_gpu_set_omega)
+  int omega_user_rows = 0, omega_user_cols = 0;
+  DBuf<double> Omg0, Omg, Omg2;
+  DBuf<float> Omg32;
+  DBuf<double> H, H1, H2, G;
+  DBuf<float4> lut32;
+  DBuf<double> scale;
+  DBuf<int32_t> perm;
+  bool permuted = false;
+  std::vector<int32_t> perm_host;
+  int bandsize = 1;
+  int64_t blocksize = 0;
+  // window scratch
+  DBuf<float> part, hpart, g32;
+  // small matrices and reductions
+  DBuf<double> W, R1, R1i, R2, R2i, R3, R3i, Rt, Rti, UB, sigma, T, tmp, sgn, red, mevv;
+  DBuf<int> status, flag;
+  DBuf<double> U, Upre, V, Vpre;
+  bool have_usv = false;
+  DBuf<double> outbuf;
+  DBuf<double> mv_t, mv_ypart, mv_x, mv_y, mv_scale;
+
+  BedView view() const { return BedView{bed.p, stride, M, N}; }
+};
+
+// ------------------------------------------------------------------------
+// data
+// ------------------------------------------------------------------------
+static void load_common(Context& c, uint64_t nsnps, uint32_t nsamples) {
+  if (nsamples == 0 || nsnps == 0) throw Error(PCAONE_E_ARG, "empty genotype matrix");
+  if (nsnps > 0x7fffffffull) throw Error(PCAONE_E_LIMIT, "more than 2^31-1 SNPs");
+  if (nsamples > 0x7fffff00u) throw Error(PCAONE_E_LIMIT, "too many samples");
+  c.N = (int)nsamples;
+  c.M = (int64_t)nsnps;
+  c.npad = round_up(c.N, 128);
+  c.stride = c.npad / 4;
+  c.bed.ensure((size_t)c.M * c.stride, c.stream, true);
+  c.counts.ensure((size_t)c.M * 4, c.stream, false);
+  c.F.ensure((size_t)c.M, c.stream, false);
+  c.have_data = false;
+  c.have_op = false;
+  c.omega_user.clear();
+  c.miss_valid = false;
+  c.nnz = -1;
+  c.counts_host.clear();
+}
+
+static void finish_load(Context& c) {
+  launch_sanitize_padding(c.bed.p, c.stride, c.M, c.N, c.stream);
+  launch_counts(c.view(), c.counts.p, c.F.p, c.stream);
+  c.have_data = true;
+}
+
+static void load_bed_host(Context& c, const uint8_t* packed, uint64_t nsnps, uint32_t nsamples) {
+  load_common(c, nsnps, nsamples);
+  const size_t bps = ((size_t)nsamples + 3) / 4;
+  PCAONE_CUDA(cudaMemcpy2DAsync(c.bed.p, c.stride, packed, bps, bps, nsnps, cudaMemcpyHostToDevice, c.stream));
+  finish_load(c);
+}
+
+static void load_bed_device(Context& c, const void* src, uint64_t pitch, uint64_t nsnps, uint32_t nsamples) {
+  load_common(c, nsnps, nsamples);
+  const size_t bps = ((size_t)nsamples + 3) / 4;
+  PCAONE_CUDA(cudaMemcpy2DAsync(c.bed.p, c.stride, src, pitch, bps, nsnps, cudaMemcpyDeviceToDevice, c.stream));
+  finish_load(c);
+}
+
+static void load_synthetic(Context& c, uint64_t nsnps, uint32_t nsamples, int npop, const double* freq,
+                           const double* weights, const double* miss_sample, const double* miss_snp,
+                           uint64_t seed) {
+  if (npop <= 0 || !freq || !weights || !miss_sample || !miss_snp) throw Error(PCAONE_E_ARG, "bad model arrays");
+  load_common(c, nsnps, nsamples);
+  DBuf<double> dw, dms, dfreq, dmsnp;
+  dw.ensure((size_t)nsamples * npop, c.stream, false);
+  dms.ensure(nsamples, c.stream, false);
+  PCAONE_CUDA(cudaMemcpyAsync(dw.p, weights, (size_t)nsamples * npop * 8, cudaMemcpyHostToDevice, c.stream));
+  PCAONE_CUDA(cudaMemcpyAsync(dms.p, miss_sample, (size_t)nsamples * 8, cudaMemcpyHostToDevice, c.stream));
+  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>((int64_t)nsnps, (1 << 26) / npop));
+  dfreq.ensure((size_t)chunk * npop, c.stream, false);
+  dmsnp.ensure((size_t)chunk, c.stream, false);
+  for (int64_t j0 = 0; j0 < (int64_t)nsnps; j0 += chunk) {
+    const int64_t n = std::min<int64_t>(chunk, (int64_t)nsnps - j0);
+    PCAONE_CUDA(cudaMemcpyAsync(dfreq.p, freq + j0 * npop, (size_t)n * npop * 8, cudaMemcpyHostToDevice, c.stream));
+    PCAONE_CUDA(cudaMemcpyAsync(dmsnp.p, miss_snp + j0, (size_t)n * 8, cudaMemcpyHostToDevice, c.stream));
+    launch_synth(c.bed.p + j0 * c.stride, c.stride, j0, n, (int)nsamples, npop, dfreq.p, dw.p, dms.p, dmsnp.p,
+                 seed, c.stream);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  }
+  finish_load(c);
+}
+
+static void need_data(const Context& c) {
+  if (!c.have_data) throw Error(PCAONE_E_ARG, "no genotype data loaded");
+}
+static void need_op(const Context& c) {
+  need_data(c);
+  if (!c.have_op) throw Error(PCAONE_E_ARG, "operator not initialised (pcaone_gpu_op_init)");
+}
+
+// ------------------------------------------------------------------------
+// operator set-up (RsvdOpData ctor + initOmg, Halko.cpp:15-23)
+// ------------------------------------------------------------------------
+static void upload_omega0(Context& c) {
+  std::vector<double> rowmajor((size_t)c.npad * c.LP, 0.0);
+  for (int j = 0; j < c.L; ++j)
+    for (int i = 0; i < c.N; ++i) rowmajor[(size_t)i * c.LP + j] = c.omega0[(size_t)j * c.N + i];
+  PCAONE_CUDA(cudaMemcpyAsync(c.Omg0.p, rowmajor.data(), rowmajor.size() * sizeof(double), cudaMemcpyHostToDevice,
+                              c.stream));
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+static void op_init(Context& c, const pcaone_gpu_params& p) {
+  need_data(c);
+  if (p.k <= 0 || p.oversamples < 0) throw Error(PCAONE_E_ARG, "k must be positive and oversamples >= 0");
+  const int L = p.k + p.oversamples;
+  if (L > kMaxL) throw Error(PCAONE_E_LIMIT, "k + oversamples exceeds " + std::to_string(kMaxL));
+  if (L > c.N) throw Error(PCAONE_E_ARG, "k + oversamples exceeds the number of samples");
+  if (p.svd != PCAONE_SVD_SINGLE && p.svd != PCAONE_SVD_WINDOW) throw Error(PCAONE_E_ARG, "svd must be 1 or 2");
+  if (p.svd == PCAONE_SVD_WINDOW && (p.bands < 4 || (p.bands & (p.bands - 1)) != 0))
+    throw Error(PCAONE_E_ARG, "the -w/--batches must be a power of 2 and the minimun is 4.");
+  if (p.precision != PCAONE_PREC_FP32)
+    throw Error(PCAONE_E_ARG, "precision form not available in this build of the operator");
+  c.P = p;
+  c.k = p.k;
+  c.L = L;
+  c.LP = round_up(L, 8);
+  c.update = c.standardize = c.scaled = c.fitted = false;
+  c.have_usv = false;
+  c.permuted = false;
+  c.perm_host.clear();
+  if (!c.omega_user.empty()) {
+    if (c.omega_user_rows != c.N || c.omega_user_cols != L)
+      throw Error(PCAONE_E_ARG, "the supplied omega is not N x (k + oversamples)");
+    c.omega0 = c.omega_user;
+  } else {
+    c.omega0.assign((size_t)c.N * L, 0.0);
+    host_random_omega(p.seed, p.rand ? 1 : 0, c.N, L, c.omega0.data());
+  }
+  const size_t nl = (size_t)c.npad * c.LP;
+  c.Omg0.ensure(nl, c.stream);
+  c.Omg.ensure(nl, c.stream);
+  c.Omg2.ensure(nl, c.stream);
+  c.Omg32.ensure(nl, c.stream);
+  c.H.ensure(nl, c.stream);
+  c.H1.ensure(nl, c.stream);
+  c.H2.ensure(nl, c.stream);
+  c.G.ensure((size_t)c.M * c.LP, c.stream);
+  c.lut32.ensure((size_t)c.M, c.stream, false);
+  c.scale.ensure((size_t)c.M, c.stream, false);
+  c.perm.ensure((size_t)c.M, c.stream, false);
+  const size_t ll = (size_t)c.LP * c.LP;
+  for (DBuf<double>* b : {&c.W, &c.R1, &c.R1i, &c.R2, &c.R2i, &c.R3, &c.R3i, &c.Rt, &c.Rti, &c.UB, &c.tmp})
+    b->ensure(ll, c.stream);
+  c.sigma.ensure(c.LP, c.stream);
+  c.sgn.ensure(c.LP, c.stream);
+  c.T.ensure((size_t)c.LP * c.k, c.stream);
+  c.mevv.ensure(4, c.stream);
+  c.status.ensure(4, c.stream);
+  c.flag.ensure(c.LP, c.stream);
+  const int cb = std::max(cross_blocks(std::max<int64_t>(c.M, c.npad)), flip_blocks(c.npad));
+  c.red.ensure((size_t)cb * std::max(c.LP * c.LP, 2 * c.LP), c.stream, false);
+  c.U.ensure((size_t)c.npad * c.k, c.stream);
+  c.Upre.ensure((size_t)c.npad * c.k, c.stream);
+  c.V.ensure((size_t)c.M * c.k, c.stream);
+  c.Vpre.ensure((size_t)c.M * c.k, c.stream);
+  // window scratch: the largest window of the schedule
+  const int64_t win = p.svd == PCAONE_SVD_WINDOW ? (c.M + p.bands - 1) / p.bands
+                                                   : std::min<int64_t>(c.M, 16384);
+  WindowArgs a{c.view(), nullptr, nullptr, 0, (int)std::max<int64_t>(1, win), c.LP, c.npad};
+  const int nch = window_g_chunks(a), nsp = window_h_splits(a);
+  c.part.ensure((size_t)nch * a.nsnp * c.LP, c.stream, false);
+  c.hpart.ensure((size_t)nsp * c.npad * c.LP, c.stream, false);
+  c.g32.ensure((size_t)a.nsnp * c.LP, c.stream, false);
+  upload_omega0(c);
+  c.have_op = true;
+}
+
+// a caller-supplied initial matrix replaces the library's draw in this and
+// every later op_init (NULL clears it)
+static void set_omega(Context& c, const double* omega, uint32_t rows, uint32_t cols) {
+  need_data(c);
+  if (!omega) {
+    c.omega_user.clear();
+    c.omega_user_rows = c.omega_user_cols = 0;
+    return;
+  }
+  if ((int)rows != c.N || cols == 0 || cols > (uint32_t)kMaxL) throw Error(PCAONE_E_ARG, "omega must be N x L");
+  c.omega_user.assign(omega, omega + (size_t)rows * cols);
+  c.omega_user_rows = (int)rows;
+  c.omega_user_cols = (int)cols;
+  if (c.have_op) {
+    if ((int)cols != c.L) throw Error(PCAONE_E_ARG, "omega must be N x (k + oversamples)");
+    c.omega0 = c.omega_user;
+    upload_omega0(c);
+  }
+}
+
+// initOmg: Omega = Omega2 = the initial draw
+static void init_omg(Context& c) {
+  const size_t nl = (size_t)c.npad * c.LP;
+  PCAONE_CUDA(cudaMemcpyAsync(c.Omg.p, c.Omg0.p, nl * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+  PCAONE_CUDA(cudaMemcpyAsync(c.Omg2.p, c.Omg0.p, nl * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+  launch_to_f32(c.Omg.p, c.Omg32.p, (int64_t)nl, c.stream);
+}
+
+static int read_status(Context& c) {
+  int st = 0;
+  PCAONE_CUDA(cudaMemcpyAsync(&st, c.status.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  return st;
+}
+
+// Orthonormal factor of A (rows x LP, in place) by CholeskyQR2, or shifted
+// CholeskyQR3 when the first Gram is not numerically positive definite
+// (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa 2020).  On return Rt
+// holds R (upper, A_in = Q R) and Rti its inverse.
+static void cholqr(Context& c, double* A, int64_t rows) {
+  const int L = c.L, LP = c.LP;
+  const int nb = cross_blocks(rows);
+  launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream);
+  launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R1.p, c.R1i.p, c.status.p, c.stream);
+  bool shifted = false;
+  if (read_status(c) != 0) {
+    // shift = 11 (m n + n (n + 1)) u ||A||_F^2
+    std::vector<double> w((size_t)LP * LP);
+    PCAONE_CUDA(cudaMemcpy(w.data(), c.W.p, w.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    double tr = 0;
+    for (int i = 0; i < L; ++i) tr += w[(size_t)i * LP + i];
+    const double shift = 11.0 * ((double)rows * L + (double)L * (L + 1)) * 1.1102230246251565e-16 * tr;
+    launch_chol_inv_shift(c.W.p, L, LP, shift, c.R1.p, c.R1i.p, c.status.p, c.stream);
+    if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: Gram matrix not positive definite");
+    shifted = true;
+  }
+  launch_gemm_tall(A, rows, LP, c.R1i.p, LP, LP, A, LP, c.stream);
+  launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream);
+  launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R2.p, c.R2i.p, c.status.p, c.stream);
+  if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: second Gram not positive definite");
+  launch_gemm_tall(A, rows, LP, c.R2i.p, LP, LP, A, LP, c.stream);
+  launch_mult_small(c.R2.p, c.R1.p, c.Rt.p, LP, c.stream);     // R = R2 R1
+  launch_mult_small(c.R1i.p, c.R2i.p, c.Rti.p, LP, c.stream);  // R^-1 = R1^-1 R2^-1
+  if (shifted) {
+    launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream);
+    launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R3.p, c.R3i.p, c.status.p, c.stream);
+    if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: third Gram not positive definite");
+    launch_gemm_tall(A, rows, LP, c.R3i.p, LP, LP, A, LP, c.stream);
+    launch_mult_small(c.R3.p, c.Rt.p, c.R1.p, LP, c.stream);
+    launch_mult_small(c.Rti.p, c.R3i.p, c.R1i.p, LP, c.stream);
+    PCAONE_CUDA(cudaMemcpyAsync(c.Rt.p, c.R1.p, (size_t)LP * LP * 8, cudaMemcpyDeviceToDevice, c.stream));
+    PCAONE_CUDA(cudaMemcpyAsync(c.Rti.p, c.R1i.p, (size_t)LP * LP * 8, cudaMemcpyDeviceToDevice, c.stream));
+  }
+}
+
+// Omega <- Q of a Householder QR of H (same column signs as Eigen's
+// HouseholderQR::householderQ()), then PCAone::flipOmg(Omg2, Omg).
+static void update_omega_from_h(Context& c) {
+  const size_t nl = (size_t)c.npad * c.LP;
+  PCAONE_CUDA(cudaMemcpyAsync(c.Omg.p, c.H.p, nl * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+  cholqr(c, c.Omg.p, c.N);
+  launch_house_signs(c.Omg.p, c.N, c.L, c.LP, c.sgn.p, c.stream);
+  launch_flip_omg(c.Omg2.p, c.Omg.p, c.N, c.L, c.LP, c.red.p, c.sgn.p, c.stream);
+  launch_to_f32(c.Omg.p, c.Omg32.p, (int64_t)nl, c.stream);
+}
+
+static void zero(DBuf<double>& b, cudaStream_t s) { PCAONE_CUDA(cudaMemsetAsync(b.p, 0, b.n * sizeof(double), s)); }
+
+// missing-genotype list in working order (built once the order is final)
+static void build_missing(Context& c) {
+  if (c.miss_valid) return;
+  if (c.counts_host.empty()) {
+    c.counts_host.resize((size_t)c.M * 4);
+    PCAONE_CUDA(cudaMemcpyAsync(c.counts_host.data(), c.counts.p, c.counts_host.size() * sizeof(int32_t),
+                                cudaMemcpyDeviceToHost, c.stream));
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  }
+  std::vector<int64_t> rowptr((size_t)c.M + 1, 0);
+  for (int64_t p = 0; p < c.M; ++p) {
+    const int64_t snp = c.permuted ? c.perm_host[p] : p;
+    rowptr[p + 1] = rowptr[p] + c.counts_host[(size_t)snp * 4 + 1];
+  }
+  c.nnz = rowptr[c.M];
+  c.miss_rowptr.ensure(rowptr.size(), c.stream, false);
+  PCAONE_CUDA(cudaMemcpyAsync(c.miss_rowptr.p, rowptr.data(), rowptr.size() * sizeof(int64_t),
+                              cudaMemcpyHostToDevice, c.stream));
+  c.miss_pos.ensure((size_t)c.nnz, c.stream, false);
+  c.miss_sample.ensure((size_t)c.nnz, c.stream, false);
+  c.miss_value.ensure((size_t)c.nnz, c.stream, true);
+  launch_missing_list(c.view(), c.permuted ? c.perm.p : nullptr, c.miss_rowptr.p, c.miss_pos.p, c.miss_sample.p,
+                      c.stream);
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  c.miss_valid = true;
+}
+
+// Data::fit_with_pi EMU branch (src/Data.cpp:318-348) on the missing list
+static void fit_with_pi(Context& c) {
+  if (!c.have_usv) throw Error(PCAONE_E_ARG, "EM update requested before a first computeUSV");
+  const auto t0 = clk::now();
+  build_missing(c);
+  launch_em_fill(c.miss_pos.p, c.miss_sample.p, c.miss_value.p, c.nnz, c.permuted ? c.perm.p : nullptr, c.F.p,
+                 c.U.p, c.sigma.p, c.V.p, c.k, c.stream);
+  c.fitted = true;
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  c.t_em += secs(t0, clk::now());
+}
+
+static void refresh_lut(Context& c) {
+  launch_lut(c.F.p, c.M, c.scaled ? 1 : 0, c.P.ploidy, c.lut32.p, nullptr, c.scale.p, c.stream);
+}
+
+// the pi == 0 data preparation shared by both operators
+static void prepare_epoch0(Context& c, bool window) {
+  if (c.update && c.P.emu) fit_with_pi(c);
+  if (c.standardize) c.scaled = true;  // Data::standardize_E scales in place, once
+  refresh_lut(c);
+  if (window) {
+    c.bandsize = 1;
+    c.blocksize = (c.M + c.P.bands - 1) / c.P.bands;
+    if (c.P.perm && !(c.update && c.P.emu) && !c.permuted) {
+      // PCAone::permute_matrix (src/RSVD.hpp:61-70): column i <- column perm[i]
+      c.perm_host.resize((size_t)c.M);
+      host_shuffle_columns(c.M, c.perm_host.data());
+      PCAONE_CUDA(cudaMemcpyAsync(c.perm.p, c.perm_host.data(), c.M * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                  c.stream));
+      PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+      c.permuted = true;
+      c.miss_valid = false;
+    }
+  }
+}
+
+// one window: G[pos0 .. pos0+n) = X_w Omega;  Hx += X_w^T G_w
+static void window_product(Context& c, int64_t pos0, int64_t n, double* Hx) {
+  if (n <= 0) return;
+  WindowArgs a{c.view(), c.permuted ? c.perm.p : nullptr, c.lut32.p, pos0, (int)n, c.LP, c.npad};
+  SparseRows sp{};
+  if (c.fitted && c.P.emu && c.nnz > 0) {
+    sp = SparseRows{c.miss_rowptr.p, c.miss_sample.p, c.miss_value.p, c.scale.p,
+                    c.permuted ? c.perm.p : nullptr, 1};
+  }
+  const int nch = window_g_chunks(a);
+  const int nsp = window_h_splits(a);
+  if ((size_t)nch * n * c.LP > c.part.n || (size_t)nsp * c.npad * c.LP > c.hpart.n || (size_t)n * c.LP > c.g32.n)
+    throw Error(PCAONE_E_ARG, "internal: window scratch too small");
+  launch_window_g(a, c.Omg32.p, c.part.p, nch, c.stream);
+  launch_window_g_finish(a, c.part.p, nch, sp, c.Omg.p, c.G.p, c.g32.p, c.stream);
+  launch_window_h(a, c.g32.p, c.hpart.p, nsp, c.stream);
+  launch_window_h_finish(a, c.hpart.p, nsp, sp, c.G.p, Hx, c.stream);
+}
+
+// NormalRsvdOpData::computeGandH, in-core branch (src/Halko.cpp:99-128)
+static void compute_g_and_h_single(Context& c, int pi) {
+  if (pi == 0) init_omg(c);
+  if (pi == 0) prepare_epoch0(c, false);
+  if (pi > 0) update_omega_from_h(c);
+  zero(c.H, c.stream);
+  const int64_t nwin = (c.M + 16383) / 16384;
+  const int64_t w = (c.M + nwin - 1) / nwin;
+  for (int64_t pos = 0; pos < c.M; pos += w) window_product(c, pos, std::min(w, c.M - pos), c.H.p);
+}
+
+// FancyRsvdOpData::computeGandH, in-core branch (src/Halko.cpp:155-225)
+static void compute_g_and_h_window(Context& c, int pi) {
+  const int bands = c.P.bands;
+  if (pi == 0) init_omg(c);
+  if (std::ldexp(1.0, pi) >= bands) {
+    zero(c.H1, c.stream);
+    zero(c.H2, c.stream);
+  }
+  if (pi == 0) prepare_epoch0(c, true);
+  c.bandsize = std::min(c.bandsize * 2, bands);
+  const int64_t bs = c.blocksize;
+  for (int b = 0, i = 1; b < bands; ++b, ++i) {
+    const int64_t start = (int64_t)b * bs;
+    const int64_t stop = (int64_t)(b + 1) * bs >= c.M ? c.M - 1 : (int64_t)(b + 1) * bs - 1;
+    const int64_t n = stop - start + 1;  // <= 0 for windows past the last SNP (M < bands * blocksize)
+    window_product(c, start, n, i <= c.bandsize / 2 ? c.H1.p : c.H2.p);
+    const bool adjacent = pi > 0 && (b + 1) == (int)std::ldexp(1.0, pi - 1) && std::ldexp(1.0, pi) < bands;
+    if ((b + 1) < c.bandsize && !adjacent) continue;
+    if (!((i == c.bandsize) || (i == c.bandsize / 2) || adjacent)) continue;
+    launch_add(c.H1.p, c.H2.p, c.H.p, (int64_t)c.npad * c.LP, c.stream);
+    update_omega_from_h(c);
+    if (i == c.bandsize) {
+      zero(c.H1, c.stream);
+      i = 0;
+    } else {
+      zero(c.H2, c.stream);
+    }
+  }
+}
+
+static void compute_g_and_h(Context& c, int pi) {
+  if (c.P.svd == PCAONE_SVD_WINDOW)
+    compute_g_and_h_window(c, pi);
+  else
+    compute_g_and_h_single(c, pi);
+}
+
+// RsvdOpData::computeUSV (src/Halko.cpp:46-97)
+static int compute_usv(Context& c, int p, double tol) {
+  const int64_t M = c.M;
+  const int N = c.N, L = c.L, LP = c.LP, k = c.k;
+  int epochs = 0;
+  bool done = false, ucur_in_upre = false;
+  for (int pi = 0; pi <= p; ++pi) {
+    auto t0 = clk::now();
+    compute_g_and_h(c, pi);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+    auto t1 = clk::now();
+    c.t_prod += secs(t0, t1);
+    ++epochs;
+    cholqr(c, c.G.p, M);  // G <- Q2, Rt = R2 R1
+    launch_cross(c.H.p, LP, L, c.H.p, LP, L, N, 1, c.W.p, LP, c.red.p, cross_blocks(N), c.stream);
+    launch_usv_small(c.Rti.p, c.W.p, L, LP, k, c.UB.p, c.sigma.p, c.T.p, c.tmp.p, c.status.p + 1, c.stream);
+    // Ucur = H T (right singular vectors of B = R^{-T} H^T)
+    launch_gemm_tall(c.H.p, N, LP, c.T.p, k, k, c.U.p, k, c.stream);
+    // Upre <- Ucur only where the reference assigns it (Halko.cpp:84-94); the
+    // winSVD minimum-epoch branch keeps the older Upre.
+    bool set_upre = pi == 0;
+    if (pi > 0) {
+      launch_mev(c.U.p, c.Upre.p, N, k, c.mevv.p, c.tmp.p, c.red.p, cross_blocks(N), c.stream);
+      double mv = 0;
+      PCAONE_CUDA(cudaMemcpyAsync(&mv, c.mevv.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+      PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+      const double diff = 1.0 - mv;
+      if (c.verbose && !c.P.emu) std::fprintf(stderr, "running of epoch = %d, diff = %g\n", pi, diff);
+      if (diff < tol || pi == p) {
+        if (c.P.svd == PCAONE_SVD_WINDOW && std::ldexp(1.0, pi) < c.P.bands) {
+          p = (int)std::log2((double)c.P.bands);
+        } else {
+          launch_gemm_tall(c.G.p, M, LP, c.UB.p, LP, k, c.V.p, k, c.stream);  // V = Q2 U_B[:, :k]
+          done = true;
+        }
+      } else {
+        set_upre = true;
+      }
+    }
+    ucur_in_upre = false;
+    if (set_upre) {
+      std::swap(c.U.p, c.Upre.p);
+      ucur_in_upre = true;
+    }
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+    c.t_qr += secs(t1, clk::now());
+    if (done) break;
+  }
+  if (ucur_in_upre) std::swap(c.U.p, c.Upre.p);  // U = Ucur after the loop (Halko.cpp:96)
+  c.have_usv = true;
+  return epochs;
+}
+
+static void copy_out(Context& c, const double* dev, int64_t rows, int ld, int cols, double* host) {
+  if (!host) return;
+  c.outbuf.ensure((size_t)rows * cols, c.stream, false);
+  launch_transpose_out(dev, rows, ld, cols, c.outbuf.p, c.stream);
+  PCAONE_CUDA(cudaMemcpyAsync(host, c.outbuf.p, (size_t)rows * cols * sizeof(double), cudaMemcpyDeviceToHost,
+                              c.stream));
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+static void outputs(Context& c, double* U, double* S, double* V) {
+  copy_out(c, c.U.p, c.N, c.k, c.k, U);
+  copy_out(c, c.V.p, c.M, c.k, c.k, V);
+  if (S) {
+    PCAONE_CUDA(cudaMemcpyAsync(S, c.sigma.p, c.k * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  }
+}
+
+static void flip_uv(Context& c) { launch_flip_uv(c.U.p, c.N, c.V.p, c.M, c.k, c.flag.p, c.stream); }
+
+// run_pca_with_halko (src/Halko.cpp:271-320), PLINK input, no LD output
+static int run_halko(Context& c, const pcaone_gpu_params& p) {
+  op_init(c, p);
+  int em_iters = 0;
+  if (!p.emu) {
+    c.update = false;
+    c.standardize = p.standardize != 0;
+    compute_usv(c, p.maxp, p.tol);
+    return 0;
+  }
+  c.update = false;
+  c.standardize = false;
+  compute_usv(c, p.maxp, p.tol);
+  flip_uv(c);
+  for (int it = 0; it < p.maxiter; ++it) {
+    c.update = true;
+    c.standardize = false;
+    PCAONE_CUDA(cudaMemcpyAsync(c.Vpre.p, c.V.p, (size_t)c.M * c.k * sizeof(double), cudaMemcpyDeviceToDevice,
+                                c.stream));
+    compute_usv(c, p.maxp, p.tol);
+    flip_uv(c);
+    launch_mev(c.V.p, c.Vpre.p, c.M, c.k, c.mevv.p, c.tmp.p, c.red.p, cross_blocks(c.M), c.stream);
+    double mv = 0;
+    PCAONE_CUDA(cudaMemcpyAsync(&mv, c.mevv.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+    const double diff = 1.0 - mv;
+    em_iters = it + 1;
+    if (c.verbose) std::fprintf(stderr, "individual allele frequencies estimated iter = %d, diff = %g\n", it + 1, diff);
+    if (diff < p.tolem) break;
+  }
+  c.update = true;
+  c.standardize = true;
+  compute_usv(c, p.maxp, p.tol);
+  flip_uv(c);
+  return em_iters;
+}
+
+static void matvec(Context& c, const double* x, double* y, int standardize) {
+  need_data(c);
+  const int N = c.N;
+  c.mv_x.ensure(N, c.stream, false);
+  c.mv_y.ensure(N, c.stream, false);
+  c.mv_t.ensure((size_t)c.M, c.stream, false);
+  c.mv_scale.ensure((size_t)c.M, c.stream, false);
+  const int nsplit = matvec_splits(c.M, N);
+  c.mv_ypart.ensure((size_t)nsplit * N, c.stream, false);
+  PCAONE_CUDA(cudaMemcpyAsync(c.mv_x.p, x, N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  launch_lut(c.F.p, c.M, standardize, 2, nullptr, nullptr, c.mv_scale.p, c.stream);
+  launch_matvec(c.view(), c.F.p, c.mv_scale.p, c.mv_x.p, c.mv_t.p, c.mv_y.p, c.mv_ypart.p, nsplit, c.stream);
+  PCAONE_CUDA(cudaMemcpyAsync(y, c.mv_y.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+}  // namespace pcaone
+
+// ==========================================================================
+// C-ABI
+// ==========================================================================
+using pcaone::Context;
+using pcaone::Error;
+
+struct pcaone_gpu_ctx {
+  Context c;
+};
+
+template <class F>
+static int guarded(pcaone_gpu_ctx* ctx, F&& fn) {
+  if (!ctx) return PCAONE_E_ARG;
+  try {
+    PCAONE_CUDA(cudaSetDevice(ctx->c.device));
+    fn(ctx->c);
+    ctx->c.last_error.clear();
+    return PCAONE_OK;
+  } catch (const Error& e) {
+    ctx->c.last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    ctx->c.last_error = "host allocation failed";
+    return PCAONE_E_NOMEM;
+  } catch (const std::exception& e) {
+    ctx->c.last_error = e.what();
+    return PCAONE_E_ARG;
+  }
+}
+
+extern "C" {
+
+void pcaone_gpu_default_params(pcaone_gpu_params* p) {
+  if (!p) return;
+  p->svd = PCAONE_SVD_WINDOW;
+  p->k = 10;
+  p->oversamples = 10;
+  p->maxp = 20;
+  p->bands = 64;
+  p->seed = 112;
+  p->rand = 1;
+  p->perm = 1;
+  p->emu = 0;
+  p->maxiter = 100;
+  p->tol = 1e-4;
+  p->tolem = 1e-5;
+  p->ploidy = 2;
+  p->standardize = 1;
+  p->precision = PCAONE_PREC_FP32;
+}
+
+int pcaone_gpu_abi_version(void) { return PCAONE_GPU_ABI_VERSION; }
+
+int pcaone_gpu_open(const pcaone_gpu_desc* desc, pcaone_gpu_ctx** out) {
+  if (!out) return PCAONE_E_ARG;
+  *out = nullptr;
+  std::unique_ptr<pcaone_gpu_ctx> ctx(new (std::nothrow) pcaone_gpu_ctx());
+  if (!ctx) return PCAONE_E_NOMEM;
+  ctx->c.device = desc ? desc->device : 0;
+  ctx->c.verbose = desc ? desc->verbose : 0;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PCAONE_E_CUDA;
+  if (ctx->c.device < 0 || ctx->c.device >= ndev) return PCAONE_E_ARG;
+  if (cudaSetDevice(ctx->c.device) != cudaSuccess) return PCAONE_E_CUDA;
+  if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) return PCAONE_E_CUDA;
+  *out = ctx.release();
+  return PCAONE_OK;
+}
+
+int pcaone_gpu_close(pcaone_gpu_ctx* ctx) {
+  if (!ctx) return PCAONE_OK;
+  cudaSetDevice(ctx->c.device);
+  cudaStreamSynchronize(ctx->c.stream);
+  cudaStream_t s = ctx->c.stream;
+  delete ctx;  // frees device buffers
+  cudaStreamDestroy(s);
+  return PCAONE_OK;
+}
+
+const char* pcaone_gpu_last_error(const pcaone_gpu_ctx* ctx) {
+  return ctx ? ctx->c.last_error.c_str() : "null context";
+}
+
+int pcaone_gpu_timings(const pcaone_gpu_ctx* ctx, double t[4]) {
+  if (!ctx || !t) return PCAONE_E_ARG;
+  t[0] = ctx->c.t_total;
+  t[1] = ctx->c.t_prod;
+  t[2] = ctx->c.t_qr;
+  t[3] = ctx->c.t_em;
+  return PCAONE_OK;
+}
+
+int pcaone_gpu_load_bed(pcaone_gpu_ctx* ctx, const uint8_t* packed, uint64_t nsnps, uint32_t nsamples) {
+  return guarded(ctx, [&](Context& c) {
+    if (!packed) throw Error(PCAONE_E_ARG, "null genotype buffer");
+    pcaone::load_bed_host(c, packed, nsnps, nsamples);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_load_bed_file_image(pcaone_gpu_ctx* ctx, const uint8_t* image, uint64_t image_bytes,
+                                   uint64_t nsnps, uint32_t nsamples) {
+  return guarded(ctx, [&](Context& c) {
+    if (!image || image_bytes < 3) throw Error(PCAONE_E_FORMAT, "truncated .bed image");
+    if (image[0] != 0x6c || image[1] != 0x1b || image[2] != 0x01)
+      throw Error(PCAONE_E_FORMAT, "Incorrect magic number in plink bed file.");
+    const uint64_t need = 3 + nsnps * (((uint64_t)nsamples + 3) / 4);
+    if (image_bytes < need)
+      throw Error(PCAONE_E_FORMAT, "truncated .bed: " + std::to_string(image_bytes) + " bytes, expected " +
+                                       std::to_string(need));
+    pcaone::load_bed_host(c, image + 3, nsnps, nsamples);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_load_bed_device(pcaone_gpu_ctx* ctx, const void* dev_packed, uint64_t src_pitch, uint64_t nsnps,
+                               uint32_t nsamples) {
+  return guarded(ctx, [&](Context& c) {
+    if (!dev_packed) throw Error(PCAONE_E_ARG, "null genotype buffer");
+    if (src_pitch < ((uint64_t)nsamples + 3) / 4) throw Error(PCAONE_E_ARG, "row pitch below (N+3)/4");
+    pcaone::load_bed_device(c, dev_packed, src_pitch, nsnps, nsamples);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_load_synthetic(pcaone_gpu_ctx* ctx, uint64_t nsnps, uint32_t nsamples, int npop, const double* freq,
+                              const double* weights, const double* miss_sample, const double* miss_snp,
+                              uint64_t seed) {
+  return guarded(ctx, [&](Context& c) {
+    pcaone::load_synthetic(c, nsnps, nsamples, npop, freq, weights, miss_sample, miss_snp, seed);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_get_bed(pcaone_gpu_ctx* ctx, uint8_t* packed) {
+  return guarded(ctx, [&](Context& c) {
+    pcaone::need_data(c);
+    if (!packed) throw Error(PCAONE_E_ARG, "null buffer");
+    const size_t bps = ((size_t)c.N + 3) / 4;
+    PCAONE_CUDA(cudaMemcpy2DAsync(packed, bps, c.bed.p, c.stride, bps, c.M, cudaMemcpyDeviceToHost, c.stream));
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_counts(pcaone_gpu_ctx* ctx, int32_t* counts, double* F) {
+  return guarded(ctx, [&](Context& c) {
+    pcaone::need_data(c);
+    if (counts)
+      PCAONE_CUDA(cudaMemcpyAsync(counts, c.counts.p, (size_t)c.M * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                  c.stream));
+    if (F) PCAONE_CUDA(cudaMemcpyAsync(F, c.F.p, (size_t)c.M * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_op_init(pcaone_gpu_ctx* ctx, const pcaone_gpu_params* params) {
+  return guarded(ctx, [&](Context& c) {
+    if (!params) throw Error(PCAONE_E_ARG, "null params");
+    pcaone::op_init(c, *params);
+  });
+}
+
+int pcaone_gpu_set_omega(pcaone_gpu_ctx* ctx, const double* omega, uint32_t rows, uint32_t cols) {
+  return guarded(ctx, [&](Context& c) {
+    pcaone::set_omega(c, omega, rows, cols);
+  });
+}
+
+int pcaone_gpu_set_flags(pcaone_gpu_ctx* ctx, int update, int standardize) {
+  return guarded(ctx, [&](Context& c) {
+    pcaone::need_op(c);
+    c.update = update != 0;
+    c.standardize = standardize != 0;
+  });
+}
+
+int pcaone_gpu_compute_g_and_h(pcaone_gpu_ctx* ctx, int pi, double* G, double* H) {
+  return guarded(ctx, [&](Context& c) {
+    pcaone::need_op(c);
+    if (pi < 0) throw Error(PCAONE_E_ARG, "negative epoch");
+    pcaone::compute_g_and_h(c, pi);
+    pcaone::copy_out(c, c.G.p, c.M, c.LP, c.L, G);
+    pcaone::copy_out(c, c.H.p, c.N, c.LP, c.L, H);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_compute_usv(pcaone_gpu_ctx* ctx, int p, double tol, double* U, double* S, double* V, int* epochs) {
+  return guarded(ctx, [&](Context& c) {
+    pcaone::need_op(c);
+    const auto t0 = pcaone::clk::now();
+    c.t_prod = c.t_qr = c.t_em = 0;
+    const int e = pcaone::compute_usv(c, p, tol);
+    if (epochs) *epochs = e;
+    pcaone::outputs(c, U, S, V);
+    c.t_total = pcaone::secs(t0, pcaone::clk::now());
+  });
+}
+
+int pcaone_gpu_run_halko(pcaone_gpu_ctx* ctx, const pcaone_gpu_params* params, double* U, double* S, double* V,
+                         int* em_iters) {
+  return guarded(ctx, [&](Context& c) {
+    if (!params) throw Error(PCAONE_E_ARG, "null params");
+    const auto t0 = pcaone::clk::now();
+    c.t_prod = c.t_qr = c.t_em = 0;
+    const int it = pcaone::run_halko(c, *params);
+    if (em_iters) *em_iters = it;
+    pcaone::outputs(c, U, S, V);
+    c.t_total = pcaone::secs(t0, pcaone::clk::now());
+  });
+}
+
+int pcaone_gpu_get_perm(pcaone_gpu_ctx* ctx, int32_t* perm) {
+  return guarded(ctx, [&](Context& c) {
+    pcaone::need_data(c);
+    if (!perm) throw Error(PCAONE_E_ARG, "null perm");
+    if (c.permuted)
+      std::memcpy(perm, c.perm_host.data(), (size_t)c.M * sizeof(int32_t));
+    else
+      for (int64_t i = 0; i < c.M; ++i) perm[i] = (int32_t)i;
+  });
+}
+
+int pcaone_gpu_matvec(pcaone_gpu_ctx* ctx, const double* x, double* y, int standardize) {
+  return guarded(ctx, [&](Context& c) {
+    if (!x || !y) throw Error(PCAONE_E_ARG, "null vector");
+    pcaone::matvec(c, x, y, standardize);
+  });
+}
+
+}  // extern "C"

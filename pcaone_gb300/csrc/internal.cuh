@@ -1,0 +1,128 @@
+// Internal declarations shared by the CUDA translation units of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+namespace pcaone {
+
+// Error carried from any layer to the C-ABI, which turns it into a status code.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define PCAONE_CUDA(call)                                                                   \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      throw ::pcaone::Error(e_ == cudaErrorMemoryAllocation ? -3 : -2,                      \
+                            std::string(#call) + ": " + cudaGetErrorString(e_));            \
+  } while (0)
+
+#define PCAONE_LAUNCH_CHECK() PCAONE_CUDA(cudaGetLastError())
+
+constexpr int kMaxL = 112;  // sketch width limit (Jacobi state in shared memory)
+
+inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+inline int64_t round_up64(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// ---------------------------------------------------------------------------
+// Genotype data resident in HBM
+//   bed     : nsnps rows of `stride` bytes (row j = SNP j of the .bed, 2-bit
+//             lanes, sample i at bits 2*(i%4) of byte i/4).  stride is a
+//             multiple of 16; lanes at and beyond nsamples hold code 00.
+//   counts  : nsnps x 4 int32 (n00, n01, n10, n11)
+//   F       : nsnps doubles (allele frequency of A1)
+// ---------------------------------------------------------------------------
+struct BedView {
+  const uint8_t* bed;
+  int64_t stride;
+  int64_t nsnps;
+  int nsamples;
+};
+
+// bed.cu
+void launch_sanitize_padding(uint8_t* bed, int64_t stride, int64_t nsnps, int nsamples, cudaStream_t s);
+void launch_counts(const BedView& v, int32_t* counts, double* F, cudaStream_t s);
+// per-SNP decode table: lut[j] = {x(00), x(01), x(10), x(11)} with x(c) =
+// scale_j * (BED2GENO[c] - F_j), x(01) = 0; lut64 likewise in double.
+void launch_lut(const double* F, int64_t nsnps, int standardize, int ploidy, float4* lut32, double* lut64,
+                double* scale, cudaStream_t s);
+// synthetic genotypes (counter-based hash); see synthetic.py for the model
+void launch_synth(uint8_t* bed, int64_t stride, int64_t snp0, int64_t nsnps, int nsamples, int npop,
+                  const double* freq, const double* weights, const double* miss_sample,
+                  const double* miss_snp, uint64_t seed, cudaStream_t s);
+
+// window products, FP32 SIMT form (prod_simt.cu)
+struct WindowArgs {
+  BedView v;
+  const int32_t* perm;   // position -> SNP (nullptr: identity)
+  const float4* lut;     // per SNP
+  int64_t pos0;          // first position of the window
+  int nsnp;              // SNPs in the window
+  int LP;                // padded sketch width (multiple of 8, <= 112)
+  int npad;              // padded samples (multiple of 128)
+};
+// part[c][j][l] = sum over samples of chunk c of x(sample, pos0+j) * omg32[sample][l]
+int window_g_chunks(const WindowArgs& a);
+void launch_window_g(const WindowArgs& a, const float* omg32, float* part, int nchunks, cudaStream_t s);
+// G[pos0+j][l] = sum_c part[c][j][l] (+ sparse missing-value term), g32 = float(G rows)
+struct SparseRows {    // missing entries of the window in CSR by position
+  const int64_t* rowptr;  // nsnps+1 (global positions)
+  const int32_t* sample;  // entry -> sample
+  const double* value;    // entry -> value in the centred scale (EM fill)
+  const double* scale;    // per SNP scale (1 when not standardised)
+  const int32_t* perm;    // position -> SNP
+  int active;
+};
+void launch_window_g_finish(const WindowArgs& a, const float* part, int nchunks, const SparseRows& sp,
+                            const double* omg, double* G, float* g32, cudaStream_t s);
+// hpart[c][i][l] = sum over SNPs of split c of x(i, pos0+j) * g32[j][l]
+int window_h_splits(const WindowArgs& a);
+void launch_window_h(const WindowArgs& a, const float* g32, float* hpart, int nsplit, cudaStream_t s);
+// Hx[i][l] += sum_c hpart[c][i][l] (+ sparse term), rows < nsamples
+void launch_window_h_finish(const WindowArgs& a, const float* hpart, int nsplit, const SparseRows& sp,
+                            const double* G, double* Hx, cudaStream_t s);
+
+// dense FP64 helpers (dense64.cu); tall matrices are row-major with ld = LP
+int cross_blocks(int64_t rows);
+size_t cross_smem(int na, int nb, int sym);
+// W[i][j] (ld ldw) = sum_r A[r][i] * B[r][j], i < na, j < nb; sym: B = A
+void launch_cross(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int sym,
+                  double* W, int ldw, double* part, int nblocks, cudaStream_t s);
+// Cholesky of W + shift*I (leading L block) -> R (upper), Rinv; padding = identity
+void launch_chol_inv_shift(const double* W, int L, int LP, double shift, double* R, double* Rinv, int* status,
+                           cudaStream_t s);
+// C (rows x n, ld ldc) = A (rows x LP) * B (LP x n, ld ldb); C may alias A
+void launch_gemm_tall(const double* A, int64_t rows, int LP, const double* B, int ldb, int n, double* C, int ldc,
+                      cudaStream_t s);
+// Q columns times the signs an Eigen / LAPACK Householder QR gives
+void launch_house_signs(double* Q, int64_t rows, int L, int LP, double* sgn, cudaStream_t s);
+int flip_blocks(int64_t rows);
+void launch_flip_omg(double* omg2, double* omg, int64_t rows, int L, int LP, double* part, double* sgn,
+                     cudaStream_t s);
+void launch_add(const double* a, const double* b, double* c, int64_t n, cudaStream_t s);
+void launch_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
+void launch_mult_small(const double* A, const double* B, double* C, int LP, cudaStream_t s);
+void launch_usv_small(const double* Rinv, const double* Wh, int L, int LP, int k, double* UB, double* sigma,
+                      double* T, double* tmp, int* status, cudaStream_t s);
+void launch_mev(const double* X, const double* Y, int64_t rows, int k, double* out, double* W, double* part,
+                int nblocks, cudaStream_t s);
+void launch_em_fill(const int32_t* epos, const int32_t* sample, double* value, int64_t nnz, const int32_t* perm,
+                    const double* F, const double* U, const double* S, const double* V, int k, cudaStream_t s);
+int matvec_splits(int64_t nsnps, int nsamples);
+void launch_matvec(const BedView& v, const double* F, const double* scale, const double* x, double* t, double* y,
+                   double* ypart, int nsplit, cudaStream_t s);
+
+// misc (util.cu)
+void launch_missing_list(const BedView& v, const int32_t* perm, const int64_t* rowptr, int32_t* epos,
+                         int32_t* sample, cudaStream_t s);
+void launch_flip_uv(double* U, int64_t nrows_u, double* V, int64_t nrows_v, int k, int* flag, cudaStream_t s);
+void launch_transpose_out(const double* A, int64_t rows, int lda, int cols, double* out, cudaStream_t s);
+
+}  // namespace pcaone

@@ -1,0 +1,155 @@
+"""Host-side mirror of the reference's RSVD operator interface over the C-ABI.
+
+Names and call order follow src/Halko.hpp / src/Halko.cpp so that code (and
+tests) written against the reference read the same:
+
+    data = FileBed("prefix")                 # FileBed ctor + Data::prepare (in-core)
+    op = FancyRsvdOpData(data, k, os)        # or NormalRsvdOpData
+    op.setFlags(False, True)
+    op.computeUSV(maxp, tol)                 # -> op.U, op.S, op.V
+
+Everything runs on the GPU through libpcaone_gb300.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import os
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import capi
+from .synthetic import read_bed
+
+
+class FileBed:
+    """PLINK fileset resident on the GPU (src/FilePlink.hpp:7-47, FilePlink.cpp:26-120)."""
+
+    def __init__(self, prefix: Optional[str] = None, *, packed: Optional[np.ndarray] = None,
+                 nsamples: Optional[int] = None, device: int = 0, verbose: int = 0):
+        self.ctx = capi.Context(device, verbose)
+        if prefix is not None:
+            fam = prefix + ".fam"
+            bim = prefix + ".bim"
+            with open(fam) as f:
+                n = sum(1 for _ in f)
+            with open(bim) as f:
+                m = sum(1 for _ in f)
+            with open(prefix + ".bed", "rb") as f:
+                image = f.read()
+            self.ctx.load_bed_file_image(image, m, n)
+        elif packed is not None and nsamples is not None:
+            self.ctx.load_bed(packed, nsamples)
+        else:
+            raise ValueError("give a PLINK prefix or packed genotypes with nsamples")
+        self.nsamples = self.ctx.nsamples
+        self.nsnps = self.ctx.nsnps
+        self._counts = None
+
+    @property
+    def F(self) -> np.ndarray:
+        return self.counts()[1]
+
+    def counts(self):
+        if self._counts is None:
+            self._counts = self.ctx.counts()
+        return self._counts
+
+    def perform_op(self, x: np.ndarray, standardize: bool = True) -> np.ndarray:
+        """ArnoldiOpData::perform_op (src/Arnoldi.cpp:18-46): y = X X^T x."""
+        return self.ctx.matvec(x, standardize)
+
+    def close(self):
+        self.ctx.close()
+
+
+@dataclass
+class Param:
+    """The Param fields the RSVD path reads (src/Cmd.hpp:16-98) with the CLI's
+    derived settings applied by ``finalize`` (src/Cmd.cpp:216, 228-232, 238)."""
+    svd: int = 2
+    k: int = 10
+    oversamples: int = 10
+    maxp: int = 20
+    bands: int = 64
+    seed: int = 112
+    rand: int = 1
+    emu: bool = False
+    maxiter: int = 100
+    tol: float = 1e-4
+    tolem: float = 1e-5
+    noshuffle: bool = False
+    ploidy: int = 2
+    precision: int = capi.PREC_FP32
+
+    def finalize(self) -> "Param":
+        self.oversamples = max(self.oversamples, self.k)
+        if not self.emu:
+            self.maxiter = 0
+        return self
+
+    def to_c(self, standardize: bool = True) -> capi.Params:
+        return capi.default_params(svd=self.svd, k=self.k, oversamples=self.oversamples, maxp=self.maxp,
+                                   bands=self.bands, seed=self.seed, rand=self.rand,
+                                   perm=int(self.svd == 2 and not self.noshuffle), emu=int(self.emu),
+                                   maxiter=self.maxiter, tol=self.tol, tolem=self.tolem, ploidy=self.ploidy,
+                                   standardize=int(standardize), precision=self.precision)
+
+
+class RsvdOpData:
+    """RsvdOpData (src/Halko.hpp:6-42) backed by the GPU context of ``data``."""
+    svd = 2
+
+    def __init__(self, data: FileBed, k: int, os_: int = 10, *, params: Optional[Param] = None,
+                 omega: Optional[np.ndarray] = None):
+        self.data = data
+        self.params = params or Param(svd=self.svd, k=k, oversamples=os_)
+        self.params.svd = self.svd
+        self.params.k, self.params.oversamples = k, os_
+        if omega is not None:
+            data.ctx.set_omega(omega)
+        data.ctx.op_init(self.params.to_c())
+        self.U = self.S = self.V = None
+
+    def rows(self):
+        return self.data.nsnps
+
+    def cols(self):
+        return self.data.nsamples
+
+    def ranks(self):
+        return self.params.k
+
+    def oversamples(self):
+        return self.params.oversamples
+
+    def size(self):
+        return self.ranks() + self.oversamples()
+
+    def setFlags(self, update: bool, standardize: bool):  # noqa: N802 - reference name
+        self.data.ctx.set_flags(update, standardize)
+
+    def computeGandH(self, pi: int):  # noqa: N802
+        return self.data.ctx.compute_g_and_h(pi)
+
+    def computeUSV(self, p: int, tol: float):  # noqa: N802
+        self.U, self.S, self.V, self.epochs = self.data.ctx.compute_usv(p, tol)
+        return self
+
+
+class NormalRsvdOpData(RsvdOpData):
+    """Single-pass RSVD, -d 1 (src/Halko.hpp:44-66)."""
+    svd = 1
+
+
+class FancyRsvdOpData(RsvdOpData):
+    """Window-based winSVD, -d 2 (src/Halko.hpp:68-93)."""
+    svd = 2
+
+
+def run_pca_with_halko(data: FileBed, params: Param, omega: Optional[np.ndarray] = None):
+    """run_pca_with_halko (src/Halko.cpp:271-320): returns (U, S, V, em_iters);
+    V rows are in the working SNP order, ``data.ctx.perm()`` maps them back."""
+    if omega is not None:
+        data.ctx.set_omega(omega)
+    return data.ctx.run_halko(params.to_c())
