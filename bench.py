@@ -1,0 +1,336 @@
+"""Benchmark: seconds to the top-k PCs of a PLINK genotype matrix on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload c2] [--precision fp32]
+
+One step = the whole hot path on one synthetic workload: packed genotypes ->
+counts and allele frequencies -> window-based RSVD (winSVD, 7 epochs for the
+64-window schedule) -> U, S, V.
+
+* ``value``: steps timed with CUDA events (synchronised on both sides), the
+  packed matrix already resident in HBM (device-to-device load into the
+  operator, then run_halko).  The packed matrix (12.5 GB for c2) is far larger
+  than L2, so no flush is needed between steps.
+* ``e2e``: the same through the C-ABI with host buffers: pinned host .bed body
+  -> pcaone_gpu_load_bed (H2D inside the timed region) -> run_halko -> U, S, V
+  back to the host.
+* ``roofline``: the dominant kernel (the window H product), algorithmic flops
+  2*N*SNPs*L per launch over its CUDA-event time on the library's stream.
+* ``cpu_baseline`` / ``--impl reference``: the oracle (numpy/LAPACK restatement
+  of the reference's Eigen/OpenMP path) on a bounded sample of the same
+  workload, scaled to the full workload by N*M.
+
+Multi-GPU: the path is not sharded (replicas only); under torchrun each rank
+runs its own replica and the slowest rank's time is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+# cpu sample: first N' samples x M' SNPs of the same population model
+CPU_SAMPLE = {"nsamples": 6000, "nsnps": 30000}
+
+
+def load_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        loaded = [x for x in sm if x is not None]
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def workload_params(name: str, precision: str):
+    from pcaone_gb300 import capi, synthetic
+    wl = synthetic.WORKLOADS[name]
+    prec = {"fp32": capi.PREC_FP32, "bf16": capi.PREC_BF16, "fp8": capi.PREC_FP8}[precision]
+    p = capi.default_params(svd=2, k=wl["k"], oversamples=wl["p"], maxp=wl["maxp"], bands=wl["bands"],
+                            perm=1, standardize=1, precision=prec)
+    return wl, p
+
+
+_cpu_sample_cache = {}
+
+
+def cpu_sample_run(name: str):
+    """Time the oracle (numpy restatement of the reference's path) on a bounded
+    sample; returns (seconds for the sample, seconds scaled to the workload,
+    description, cores).  The sample is drawn once per process."""
+    from oracle import halko as H
+    from pcaone_gb300 import synthetic
+    wl = synthetic.WORKLOADS[name]
+    n, m = CPU_SAMPLE["nsamples"], CPU_SAMPLE["nsnps"]
+    if name not in _cpu_sample_cache:
+        model = synthetic.model_for(name, seed=1, nsamples=n, nsnps=m)
+        _cpu_sample_cache[name] = synthetic.sample_packed_bed(model)
+        H.build_rng_lib()
+    packed = _cpu_sample_cache[name]
+    t0 = time.perf_counter()
+    d = H.OracleData(packed, n, perm=True, bands=wl["bands"])
+    H.run_pca_with_halko(d, wl["k"], wl["p"], maxp=wl["maxp"])
+    t = time.perf_counter() - t0
+    scale = (wl["nsamples"] * wl["nsnps"]) / (n * m)
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    desc = (f"numpy/LAPACK restatement of the reference's in-core path (decode, AF, standardise, shuffle, "
+            f"winSVD {wl['maxp'] + 1} epochs, k={wl['k']}, p={wl['p']}, 64 windows) on the first {n} samples x "
+            f"{m} SNPs of the same population model; {t:.2f} s measured, scaled by N*M x{scale:.1f}")
+    return t, t * scale, desc, cores
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, int(os.environ.get("LOCAL_RANK", "0"))
+    import torch.distributed as dist
+    dist.init_process_group("gloo")
+    return dist.get_rank(), ws, int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def reduce_max(x: float, ws: int) -> float:
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args):
+    rank, ws, _ = dist_init()
+    if rank != 0:
+        return
+    wl_name = args.workload
+    from pcaone_gb300 import synthetic
+    wl = synthetic.WORKLOADS[wl_name]
+    times = []
+    desc, cores = "", 1
+    for it in range(args.warmup + args.steps):
+        _, scaled, desc, cores = cpu_sample_run(wl_name)
+        if it >= args.warmup:
+            times.append(scaled)
+    v = statistics.median(times)
+    line = {
+        "impl": "reference", "metric": "sec_to_topk_pcs", "value": v, "unit": "s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{wl_name}: N={wl['nsamples']} x M={wl['nsnps']} PLINK, k={wl['k']}, "
+                               f"p={wl['p']}, winSVD 64 windows, {wl['maxp'] + 1} epochs"},
+        "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": desc},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    rank, ws, local = dist_init()
+    import torch
+    from pcaone_gb300 import capi, synthetic
+    torch.cuda.set_device(local)
+    wl, params = workload_params(args.workload, args.precision)
+    model = synthetic.model_for(args.workload, seed=1)
+    N, M = model.nsamples, model.nsnps
+    bps = (N + 3) // 4
+    L = wl["k"] + wl["p"]
+    peaks, peak_kind = load_peaks()
+
+    ctx = capi.Context(local)
+    # the resident source matrix (value path) and a pinned host copy (e2e path)
+    src = capi.Context(local)
+    src.load_synthetic(model)
+    dev_src = torch.empty((M, bps), dtype=torch.uint8, device=f"cuda:{local}")
+    pinned = torch.empty((M, bps), dtype=torch.uint8, pin_memory=True)
+    src.get_bed(out_ptr=pinned.data_ptr())
+    dev_src.copy_(pinned)
+    src.close()
+    torch.cuda.synchronize()
+
+    def step_device():
+        ctx.load_bed_device(dev_src.data_ptr(), bps, M, N)
+        return ctx.run_halko(params)
+
+    def step_e2e():
+        ctx.load_bed_ptr(pinned.data_ptr(), M, N)
+        return ctx.run_halko(params)
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+
+    # ---- value: resident inputs, CUDA events around each step ----
+    ctx.set_profiling(True)
+    launches0 = ctx.launch_count()
+    times = []
+    with ClockSampler(local) as clocks:
+        barrier(ws)
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            U, S, V, _ = step_device()
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+        barrier(ws)
+    launches = ctx.launch_count() - launches0
+    kstats = ctx.kernel_stats()
+    ctx.set_profiling(False)
+    t_dev = reduce_max(sum(times) / len(times), ws)
+
+    # ---- e2e: host buffers through the C-ABI ----
+    step_e2e()
+    torch.cuda.synchronize()
+    etimes = []
+    for _ in range(args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        step_e2e()
+        e1.record()
+        torch.cuda.synchronize()
+        etimes.append(e0.elapsed_time(e1) / 1e3)
+    t_e2e = reduce_max(sum(etimes) / len(etimes), ws)
+    h2d = M * bps + N * L * 8
+    d2h = (N + M) * wl["k"] * 8 + wl["k"] * 8
+
+    # ---- roofline of the dominant kernel ----
+    dom = max(kstats, key=lambda k: kstats[k]["ms"])
+    ks = kstats[dom]
+    achieved = ks["flops"] / (ks["ms"] / 1e3) / 1e12 if ks["ms"] > 0 else 0.0
+    peak = peaks.get("bf16_tflops", PEAKS_FALLBACK["bf16_tflops"])
+    roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": None, "kernel": f"k_window_{dom[0]}",
+            "note": (f"{args.precision} form; {ks['launches']} launches, {ks['ms']:.1f} ms of "
+                     f"{sum(times) * 1e3:.1f} ms; peak = {peak_kind} bf16 dense")}
+    if args.precision == "fp32":
+        roof["note"] += "; the FP32 form runs on CUDA cores, not the tensor pipe"
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        t_s, t_full, desc, cores = cpu_sample_run(args.workload)
+        cpu = {"value": t_full, "unit": "s", "cores": cores, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": "sec_to_topk_pcs", "value": t_dev, "unit": "s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_dev * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.precision, "data": "synthetic",
+            "config": {"workload": f"{args.workload}: N={N} x M={M} PLINK ({M * bps / 1e9:.1f} GB packed), "
+                                   f"{model.npop} populations, k={wl['k']}, p={wl['p']}, winSVD 64 windows, "
+                                   f"{wl['maxp'] + 1} epochs",
+                       "precision": args.precision, "l2": "inputs larger than L2 (packed matrix resident in HBM)",
+                       "replicas": ws},
+            "clocks": clocks.summary(),
+            "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches / max(1, args.steps)),
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "kernels": kstats,
+            "pcs": {"S_top": [float(x) for x in S[:5]]},
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16", "fp8"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -85,6 +85,17 @@ int pcaone_gpu_abi_version(void);
  * t[0] total, t[1] block products, t[2] QR/SVD, t[3] EM fill */
 int pcaone_gpu_timings(const pcaone_gpu_ctx* ctx, double t[4]);
 
+/* Instrumentation with no counterpart in the reference.  set_profiling(1)
+ * records CUDA events on the context's stream around every launch of the two
+ * window-product kernels (class 0: G = X_w * Omega, class 1: H += X_w^T * G)
+ * and resets the totals; kernel_stats returns per class the summed device
+ * milliseconds, algorithmic flops (2 * N * SNPs * L per launch) and launches.
+ * launch_count is the number of kernels the library has launched so far in
+ * this process. */
+int pcaone_gpu_set_profiling(pcaone_gpu_ctx* ctx, int on);
+int pcaone_gpu_kernel_stats(pcaone_gpu_ctx* ctx, double ms[2], double flops[2], long long launches[2]);
+unsigned long long pcaone_gpu_launch_count(void);
+
 /* ---- data: replaces FileBed::read_all (src/FilePlink.cpp:26-120) --------- */
 /* packed: the .bed body after the 3 magic bytes, nsnps rows of (nsamples+3)/4
  * bytes in SNP-major order (host memory; copied to HBM). */

@@ -29,6 +29,7 @@ EXPORTS = [
     "pcaone_gpu_load_bed_device", "pcaone_gpu_counts", "pcaone_gpu_op_init", "pcaone_gpu_set_omega",
     "pcaone_gpu_set_flags", "pcaone_gpu_compute_g_and_h", "pcaone_gpu_compute_usv", "pcaone_gpu_run_halko",
     "pcaone_gpu_get_perm", "pcaone_gpu_matvec", "pcaone_gpu_load_synthetic", "pcaone_gpu_get_bed",
+    "pcaone_gpu_set_profiling", "pcaone_gpu_kernel_stats", "pcaone_gpu_launch_count",
 ]
 
 
@@ -84,9 +85,13 @@ def load(path: str = LIBPATH) -> ctypes.CDLL:
     lib.pcaone_gpu_load_synthetic.argtypes = [c_void_p, c_uint64, c_uint32, c_int, c_void_p, c_void_p, c_void_p,
                                               c_void_p, c_uint64]
     lib.pcaone_gpu_get_bed.argtypes = [c_void_p, c_void_p]
+    lib.pcaone_gpu_set_profiling.argtypes = [c_void_p, c_int]
+    lib.pcaone_gpu_kernel_stats.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p]
+    lib.pcaone_gpu_launch_count.argtypes = []
     for name in EXPORTS:
         if name not in ("pcaone_gpu_default_params", "pcaone_gpu_last_error"):
             getattr(lib, name).restype = c_int
+    lib.pcaone_gpu_launch_count.restype = ctypes.c_ulonglong
     _lib = lib
     return lib
 
@@ -167,10 +172,20 @@ class Context:
                                                        _ptr(w), _ptr(ms), _ptr(mj), model.seed))
         self.nsamples, self.nsnps = int(model.nsamples), int(model.nsnps)
 
-    def get_bed(self):
+    def get_bed(self, out_ptr: int = 0):
+        """Packed genotypes back to the host: a new array, or into the host
+        buffer at ``out_ptr`` (nsnps * ceil(N/4) bytes, e.g. pinned memory)."""
+        if out_ptr:
+            self._check(self.lib.pcaone_gpu_get_bed(self.h, c_void_p(out_ptr)))
+            return None
         out = np.empty((self.nsnps, (self.nsamples + 3) // 4), dtype=np.uint8)
         self._check(self.lib.pcaone_gpu_get_bed(self.h, _ptr(out)))
         return out
+
+    def load_bed_ptr(self, host_ptr: int, nsnps: int, nsamples: int):
+        """pcaone_gpu_load_bed from a raw host pointer (e.g. pinned memory)."""
+        self._check(self.lib.pcaone_gpu_load_bed(self.h, c_void_p(host_ptr), nsnps, nsamples))
+        self.nsamples, self.nsnps = int(nsamples), int(nsnps)
 
     def counts(self):
         cnt = np.empty((self.nsnps, 4), dtype=np.int32)
@@ -229,6 +244,20 @@ class Context:
         y = np.empty_like(x)
         self._check(self.lib.pcaone_gpu_matvec(self.h, _ptr(x), _ptr(y), int(standardize)))
         return y
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.pcaone_gpu_set_profiling(self.h, int(on)))
+
+    def kernel_stats(self):
+        ms = np.zeros(2)
+        fl = np.zeros(2)
+        n = np.zeros(2, dtype=np.int64)
+        self._check(self.lib.pcaone_gpu_kernel_stats(self.h, _ptr(ms), _ptr(fl), _ptr(n)))
+        return {"g_product": dict(ms=ms[0], flops=fl[0], launches=int(n[0])),
+                "h_product": dict(ms=ms[1], flops=fl[1], launches=int(n[1]))}
+
+    def launch_count(self) -> int:
+        return int(self.lib.pcaone_gpu_launch_count())
 
     def timings(self):
         t = np.zeros(4, dtype=np.float64)

@@ -23,6 +23,8 @@
 
 namespace pcaone {
 
+unsigned long long g_kernel_launches = 0;
+
 void host_random_omega(int seed, int gaussian, int64_t rows, int64_t cols, double* out_colmajor);
 void host_shuffle_columns(int64_t n, int32_t* out);
 
@@ -107,7 +109,42 @@ struct Context {
   DBuf<double> outbuf;
   DBuf<double> mv_t, mv_ypart, mv_x, mv_y, mv_scale;
 
+  // optional per-kernel CUDA-event timing of the window products
+  // (pcaone_gpu_set_profiling): class 0 = G product, 1 = H product
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<int, size_t>> ev_marks;  // (class, index of the start event)
+  std::vector<std::pair<int, double>> ev_work;   // (class, flops of the launch)
+  double prof_ms[2] = {0, 0}, prof_flops[2] = {0, 0};
+  long long prof_launches[2] = {0, 0};
+
   BedView view() const { return BedView{bed.p, stride, M, N}; }
+
+  cudaEvent_t next_event() {
+    if (ev_used == ev_pool.size()) {
+      cudaEvent_t e;
+      PCAONE_CUDA(cudaEventCreate(&e));
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_used++];
+  }
+  // folds recorded event pairs into the per-class totals (stream synchronised)
+  void collect_events() {
+    for (size_t q = 0; q < ev_marks.size(); ++q) {
+      float ms = 0.f;
+      PCAONE_CUDA(cudaEventElapsedTime(&ms, ev_pool[ev_marks[q].second], ev_pool[ev_marks[q].second + 1]));
+      prof_ms[ev_marks[q].first] += ms;
+      prof_flops[ev_work[q].first] += ev_work[q].second;
+      prof_launches[ev_marks[q].first] += 1;
+    }
+    ev_marks.clear();
+    ev_work.clear();
+    ev_used = 0;
+  }
+  ~Context() {
+    for (auto e : ev_pool) cudaEventDestroy(e);
+  }
 };
 
 // ------------------------------------------------------------------------
@@ -427,9 +464,25 @@ static void window_product(Context& c, int64_t pos0, int64_t n, double* Hx) {
   const int nsp = window_h_splits(a);
   if ((size_t)nch * n * c.LP > c.part.n || (size_t)nsp * c.npad * c.LP > c.hpart.n || (size_t)n * c.LP > c.g32.n)
     throw Error(PCAONE_E_ARG, "internal: window scratch too small");
+  const double flops = 2.0 * (double)c.N * (double)n * (double)c.L;
+  auto mark = [&](int cls) {
+    if (!c.profiling) return;
+    const size_t i0 = c.ev_used;
+    PCAONE_CUDA(cudaEventRecord(c.next_event(), c.stream));
+    c.next_event();
+    c.ev_marks.push_back({cls, i0});
+    c.ev_work.push_back({cls, flops});
+  };
+  auto close_mark = [&]() {
+    if (c.profiling) PCAONE_CUDA(cudaEventRecord(c.ev_pool[c.ev_marks.back().second + 1], c.stream));
+  };
+  mark(0);
   launch_window_g(a, c.Omg32.p, c.part.p, nch, c.stream);
+  close_mark();
   launch_window_g_finish(a, c.part.p, nch, sp, c.Omg.p, c.G.p, c.g32.p, c.stream);
+  mark(1);
   launch_window_h(a, c.g32.p, c.hpart.p, nsp, c.stream);
+  close_mark();
   launch_window_h_finish(a, c.hpart.p, nsp, sp, c.G.p, Hx, c.stream);
 }
 
@@ -491,6 +544,7 @@ static int compute_usv(Context& c, int p, double tol) {
     auto t0 = clk::now();
     compute_g_and_h(c, pi);
     PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+    c.collect_events();
     auto t1 = clk::now();
     c.t_prod += secs(t0, t1);
     ++epochs;
@@ -691,6 +745,33 @@ int pcaone_gpu_close(pcaone_gpu_ctx* ctx) {
 const char* pcaone_gpu_last_error(const pcaone_gpu_ctx* ctx) {
   return ctx ? ctx->c.last_error.c_str() : "null context";
 }
+
+int pcaone_gpu_set_profiling(pcaone_gpu_ctx* ctx, int on) {
+  return guarded(ctx, [&](Context& c) {
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+    c.collect_events();
+    c.profiling = on != 0;
+    for (int i = 0; i < 2; ++i) {
+      c.prof_ms[i] = 0;
+      c.prof_flops[i] = 0;
+      c.prof_launches[i] = 0;
+    }
+  });
+}
+
+int pcaone_gpu_kernel_stats(pcaone_gpu_ctx* ctx, double ms[2], double flops[2], long long launches[2]) {
+  return guarded(ctx, [&](Context& c) {
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+    c.collect_events();
+    for (int i = 0; i < 2; ++i) {
+      if (ms) ms[i] = c.prof_ms[i];
+      if (flops) flops[i] = c.prof_flops[i];
+      if (launches) launches[i] = c.prof_launches[i];
+    }
+  });
+}
+
+unsigned long long pcaone_gpu_launch_count(void) { return pcaone::g_kernel_launches; }
 
 int pcaone_gpu_timings(const pcaone_gpu_ctx* ctx, double t[4]) {
   if (!ctx || !t) return PCAONE_E_ARG;

@@ -23,7 +23,14 @@ struct Error : std::runtime_error {
                             std::string(#call) + ": " + cudaGetErrorString(e_));            \
   } while (0)
 
-#define PCAONE_LAUNCH_CHECK() PCAONE_CUDA(cudaGetLastError())
+// every kernel launch of the library is followed by this check, which also
+// counts the launch (pcaone_gpu_launch_count)
+extern unsigned long long g_kernel_launches;
+#define PCAONE_LAUNCH_CHECK()      \
+  do {                             \
+    ++::pcaone::g_kernel_launches; \
+    PCAONE_CUDA(cudaGetLastError()); \
+  } while (0)
 
 constexpr int kMaxL = 112;  // sketch width limit (Jacobi state in shared memory)
 

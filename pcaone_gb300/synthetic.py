@@ -217,6 +217,9 @@ WORKLOADS = {
                anc="uniform", anc_range=(0.01, 0.5), mcar=0.005, k=20, p=20, maxp=6, bands=64),
     "c3": dict(nsamples=200_000, nsnps=1_000_000, npop=8, fst=0.05, anc="beta", anc_range=(0.01, 0.99),
                admixed_frac=0.02, mcar=0.0, k=40, p=10, maxp=6, bands=64),
+    # scaled-down c2 (0.5 GB packed, still larger than L2) for profiling captures
+    "c2s": dict(nsamples=20_000, nsnps=100_000, npop=5, fst=[0.01, 0.02, 0.05, 0.1, 0.2],
+                anc="uniform", anc_range=(0.01, 0.5), mcar=0.005, k=20, p=20, maxp=6, bands=64),
     "c4": dict(nsamples=50_000, nsnps=300_000, npop=4, fst=0.05, anc="uniform", anc_range=(0.05, 0.5),
                miss_sample_beta=(1, 20), miss_snp_beta=(1, 50), k=10, p=10, maxp=6, bands=64),
 }
