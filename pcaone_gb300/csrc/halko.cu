@@ -20,6 +20,7 @@
 
 #include "../../include/pcaone_gpu.h"
 #include "internal.cuh"
+#include "prod_tc.cuh"
 
 namespace pcaone {
 
@@ -73,6 +74,7 @@ struct Context {
   DBuf<int32_t> counts;
   DBuf<double> F;
   std::vector<int32_t> counts_host;  // filled lazily
+  long long counts_total_missing = -1;
 
   // missing entries in working order (EM)
   int64_t nnz = -1;
@@ -108,6 +110,18 @@ struct Context {
   bool have_usv = false;
   DBuf<double> outbuf;
   DBuf<double> mv_t, mv_ypart, mv_x, mv_y, mv_scale;
+
+  // tensor-core form (prod_tc.cu)
+  bool tc = false;
+  DBuf<uint8_t> bedp;                 // packed rows in working order (shuffled window method)
+  const uint8_t* bed_work = nullptr;  // packed rows the tensor-core kernels read
+  DBuf<__nv_bfloat16> wsl, gt;        // W slices (3*LP x npad), Gh/Gm slices (6*LP x ldg)
+  DBuf<double> colsum, cpart, cvec;
+  DBuf<float> part_m;
+  DBuf<int> err;
+  CUtensorMap map_bed_g{}, map_bed_h{}, map_w{}, map_gt{};
+  int ldg = 0, win_max = 0;
+  int nslice_cur = 1, w_slices = 0;
 
   // optional per-kernel CUDA-event timing of the window products
   // (pcaone_gpu_set_profiling): class 0 = G product, 1 = H product
@@ -172,7 +186,19 @@ static void load_common(Context& c, uint64_t nsnps, uint32_t nsamples) {
 static void finish_load(Context& c) {
   launch_sanitize_padding(c.bed.p, c.stride, c.M, c.N, c.stream);
   launch_counts(c.view(), c.counts.p, c.F.p, c.stream);
+  c.counts_total_missing = -1;
   c.have_data = true;
+}
+
+static void ensure_missing_total(Context& c) {
+  if (c.counts_total_missing >= 0) return;
+  c.counts_host.resize((size_t)c.M * 4);
+  PCAONE_CUDA(cudaMemcpyAsync(c.counts_host.data(), c.counts.p, c.counts_host.size() * sizeof(int32_t),
+                              cudaMemcpyDeviceToHost, c.stream));
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  long long t = 0;
+  for (int64_t j = 0; j < c.M; ++j) t += c.counts_host[(size_t)j * 4 + 1];
+  c.counts_total_missing = t;
 }
 
 static void load_bed_host(Context& c, const uint8_t* packed, uint64_t nsnps, uint32_t nsamples) {
@@ -233,6 +259,56 @@ static void upload_omega0(Context& c) {
   PCAONE_CUDA(cudaStreamSynchronize(c.stream));
 }
 
+// tensor-core buffers, launch shapes and TMA descriptors for windows of up to
+// `win` SNPs
+static void tc_make_bed_maps(Context& c) {
+  tc::make_map_2d(&c.map_bed_g, c.bed_work, false, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 16, 128,
+                  false);
+  tc::make_map_2d(&c.map_bed_h, c.bed_work, false, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 32, 64,
+                  false);
+}
+
+static void tc_shapes(int win, int npad, int& chunk, int& nchunks, int& per_split, int& nsplit) {
+  const int xt = ceil_div(win, 128);
+  int nch = std::max(1, ceil_div(304, xt));
+  chunk = round_up(ceil_div(npad, nch), 64);
+  chunk = std::min(chunk, 4096);
+  nchunks = ceil_div(npad, chunk);
+  const int xh = npad / 128;
+  int ns = std::max(1, ceil_div(304, xh));
+  per_split = round_up(ceil_div(win, ns), 64);
+  per_split = std::min(per_split, 4096);
+  nsplit = ceil_div(win, per_split);
+}
+
+static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
+  const int LP = c.LP;
+  c.win_max = win;
+  c.ldg = round_up(win, 64);
+  size_t need_part = 1, need_hpart = 1;
+  for (int64_t n : lens) {
+    if (n <= 0) continue;
+    int ch, nch, per, nsp;
+    tc_shapes((int)n, c.npad, ch, nch, per, nsp);
+    need_part = std::max(need_part, (size_t)nch * n * LP);
+    need_hpart = std::max(need_hpart, (size_t)nsp * c.npad * LP);
+  }
+  c.wsl.ensure((size_t)3 * LP * c.npad, c.stream);
+  c.gt.ensure((size_t)6 * LP * c.ldg, c.stream);
+  c.colsum.ensure(LP, c.stream);
+  c.cvec.ensure(LP, c.stream);
+  c.cpart.ensure((size_t)win * LP, c.stream, false);
+  c.err.ensure(1, c.stream);
+  c.part.ensure(std::max(need_part, c.part.n), c.stream, false);
+  c.part_m.ensure(need_part, c.stream, false);
+  c.hpart.ensure(std::max(need_hpart, c.hpart.n), c.stream, false);
+  c.bed_work = c.bed.p;
+  tc_make_bed_maps(c);
+  tc::make_map_2d(&c.map_w, c.wsl.p, true, (uint64_t)c.npad, (uint64_t)3 * LP, (uint64_t)c.npad * 2, 64, LP, true);
+  tc::make_map_2d(&c.map_gt, c.gt.p, true, (uint64_t)c.ldg, (uint64_t)6 * LP, (uint64_t)c.ldg * 2, 64, LP, true);
+  c.w_slices = 0;
+}
+
 static void op_init(Context& c, const pcaone_gpu_params& p) {
   need_data(c);
   if (p.k <= 0 || p.oversamples < 0) throw Error(PCAONE_E_ARG, "k must be positive and oversamples >= 0");
@@ -242,12 +318,13 @@ static void op_init(Context& c, const pcaone_gpu_params& p) {
   if (p.svd != PCAONE_SVD_SINGLE && p.svd != PCAONE_SVD_WINDOW) throw Error(PCAONE_E_ARG, "svd must be 1 or 2");
   if (p.svd == PCAONE_SVD_WINDOW && (p.bands < 4 || (p.bands & (p.bands - 1)) != 0))
     throw Error(PCAONE_E_ARG, "the -w/--batches must be a power of 2 and the minimun is 4.");
-  if (p.precision != PCAONE_PREC_FP32)
+  if (p.precision != PCAONE_PREC_FP32 && p.precision != PCAONE_PREC_BF16 && p.precision != PCAONE_PREC_BF16X3)
     throw Error(PCAONE_E_ARG, "precision form not available in this build of the operator");
   c.P = p;
   c.k = p.k;
   c.L = L;
-  c.LP = round_up(L, 8);
+  c.tc = p.precision != PCAONE_PREC_FP32;
+  c.LP = c.tc ? round_up(L, 16) : round_up(L, 8);
   c.update = c.standardize = c.scaled = c.fitted = false;
   c.have_usv = false;
   c.permuted = false;
@@ -287,14 +364,24 @@ static void op_init(Context& c, const pcaone_gpu_params& p) {
   c.Upre.ensure((size_t)c.npad * c.k, c.stream);
   c.V.ensure((size_t)c.M * c.k, c.stream);
   c.Vpre.ensure((size_t)c.M * c.k, c.stream);
-  // window scratch: the largest window of the schedule
+  // window scratch: the largest need over the distinct window lengths of the schedule
   const int64_t win = p.svd == PCAONE_SVD_WINDOW ? (c.M + p.bands - 1) / p.bands
-                                                   : std::min<int64_t>(c.M, 16384);
-  WindowArgs a{c.view(), nullptr, nullptr, 0, (int)std::max<int64_t>(1, win), c.LP, c.npad};
-  const int nch = window_g_chunks(a), nsp = window_h_splits(a);
-  c.part.ensure((size_t)nch * a.nsnp * c.LP, c.stream, false);
-  c.hpart.ensure((size_t)nsp * c.npad * c.LP, c.stream, false);
-  c.g32.ensure((size_t)a.nsnp * c.LP, c.stream, false);
+                                                   : (c.M + (c.M + 16383) / 16384 - 1) / ((c.M + 16383) / 16384);
+  std::vector<int64_t> lens = {win, c.M % std::max<int64_t>(1, win)};
+  size_t need_part = 1, need_hpart = 1;
+  for (int64_t n : lens) {
+    if (n <= 0) continue;
+    WindowArgs a{c.view(), nullptr, nullptr, 0, (int)n, c.LP, c.npad};
+    need_part = std::max(need_part, (size_t)window_g_chunks(a) * n * c.LP);
+    need_hpart = std::max(need_hpart, (size_t)window_h_splits(a) * c.npad * c.LP);
+  }
+  c.part.ensure(need_part, c.stream, false);
+  c.hpart.ensure(need_hpart, c.stream, false);
+  c.g32.ensure((size_t)std::max<int64_t>(1, win) * c.LP, c.stream, false);
+  if (c.tc) {
+    tc_setup(c, (int)std::max<int64_t>(1, win), lens);
+    ensure_missing_total(c);
+  }
   upload_omega0(c);
   c.have_op = true;
 }
@@ -325,6 +412,7 @@ static void init_omg(Context& c) {
   PCAONE_CUDA(cudaMemcpyAsync(c.Omg.p, c.Omg0.p, nl * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
   PCAONE_CUDA(cudaMemcpyAsync(c.Omg2.p, c.Omg0.p, nl * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
   launch_to_f32(c.Omg.p, c.Omg32.p, (int64_t)nl, c.stream);
+  c.w_slices = 0;
 }
 
 static int read_status(Context& c) {
@@ -383,6 +471,7 @@ static void update_omega_from_h(Context& c) {
   launch_house_signs(c.Omg.p, c.N, c.L, c.LP, c.sgn.p, c.stream);
   launch_flip_omg(c.Omg2.p, c.Omg.p, c.N, c.L, c.LP, c.red.p, c.sgn.p, c.stream);
   launch_to_f32(c.Omg.p, c.Omg32.p, (int64_t)nl, c.stream);
+  c.w_slices = 0;
 }
 
 static void zero(DBuf<double>& b, cudaStream_t s) { PCAONE_CUDA(cudaMemsetAsync(b.p, 0, b.n * sizeof(double), s)); }
@@ -447,13 +536,117 @@ static void prepare_epoch0(Context& c, bool window) {
       PCAONE_CUDA(cudaStreamSynchronize(c.stream));
       c.permuted = true;
       c.miss_valid = false;
+      if (c.tc) {
+        c.bedp.ensure((size_t)c.M * c.stride, c.stream, false);
+        tc::launch_gather_rows(c.bed.p, c.bedp.p, c.stride, c.perm.p, c.M, c.stream);
+        c.bed_work = c.bedp.p;
+        tc_make_bed_maps(c);
+      }
     }
+  }
+}
+
+// tensor-core form of one window (prod_tc.cu)
+static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
+  const int LP = c.LP, S = c.nslice_cur;
+  if (c.w_slices != S) {
+    tc::launch_omega_slices(c.Omg.p, c.npad, c.N, LP, S, c.wsl.p, c.colsum.p, c.stream);
+    c.w_slices = S;
+  }
+  int chunk, nch, per, nsp;
+  tc_shapes((int)n, c.npad, chunk, nch, per, nsp);
+  if ((size_t)nch * n * LP > c.part.n || (size_t)nsp * c.npad * LP > c.hpart.n || n > c.win_max)
+    throw Error(PCAONE_E_ARG, "internal: tensor-core window scratch too small");
+  const bool mask = true;  // per-CTA skip when its tile holds no missing genotype
+  SparseRows sp{};
+  if (c.fitted && c.P.emu && c.nnz > 0)
+    sp = SparseRows{c.miss_rowptr.p, c.miss_sample.p, c.miss_value.p, c.scale.p, c.permuted ? c.perm.p : nullptr, 1};
+  const bool any_miss = c.counts_total_missing > 0;
+  const double flops = 2.0 * (double)c.N * (double)n * (double)c.L;
+  auto mark = [&](int cls) {
+    if (!c.profiling) return;
+    const size_t i0 = c.ev_used;
+    PCAONE_CUDA(cudaEventRecord(c.next_event(), c.stream));
+    c.next_event();
+    c.ev_marks.push_back({cls, i0});
+    c.ev_work.push_back({cls, flops});
+  };
+  auto close_mark = [&]() {
+    if (c.profiling) PCAONE_CUDA(cudaEventRecord(c.ev_pool[c.ev_marks.back().second + 1], c.stream));
+  };
+  tc::GArgs ga{};
+  ga.pos0 = pos0;
+  ga.nsnp = (int)n;
+  ga.LP = LP;
+  ga.nslice = S;
+  ga.chunk = chunk;
+  ga.npad = c.npad;
+  ga.nchunks = nch;
+  ga.mask = (mask && any_miss) ? 1 : 0;
+  ga.nstages = tc::stages_for(LP, S, 1, ga.mask != 0, 128 * 16);
+  ga.tmem_cols = tc::tmem_cols_for(ga.mask ? 2 * LP : LP);
+  ga.counts = c.counts.p;
+  ga.perm = c.permuted ? c.perm.p : nullptr;
+  ga.part_d = c.part.p;
+  ga.part_m = c.part_m.p;
+  ga.err = c.err.p;
+  mark(0);
+  tc::launch_g(c.map_bed_g, c.map_w, ga, c.stream);
+  close_mark();
+  tc::GFinishArgs fa{};
+  fa.pos0 = pos0;
+  fa.nsnp = (int)n;
+  fa.L = c.L;
+  fa.LP = LP;
+  fa.nslice = S;
+  fa.nchunks = nch;
+  fa.mask = ga.mask;
+  fa.ldg = round_up((int)n, 64);
+  fa.part_d = c.part.p;
+  fa.part_m = ga.mask ? c.part_m.p : nullptr;
+  fa.colsum = c.colsum.p;
+  fa.F = c.F.p;
+  fa.scale = c.scale.p;
+  fa.perm = c.permuted ? c.perm.p : nullptr;
+  fa.omg = c.Omg.p;
+  fa.sp = sp;
+  fa.G = c.G.p;
+  fa.gt = c.gt.p;
+  fa.cpart = c.cpart.p;
+  // the B operand tensor map spans ldg columns; windows shorter than the
+  // longest one leave the tail zeroed by the finish kernel
+  fa.ldg = c.ldg;
+  tc::launch_g_finish(fa, c.cvec.p, c.stream);
+  tc::HArgs ha{};
+  ha.pos0 = pos0;
+  ha.nsnp = (int)n;
+  ha.LP = LP;
+  ha.nslice = S;
+  ha.per_split = per;
+  ha.nsplit = nsp;
+  ha.npad = c.npad;
+  ha.mask = ga.mask;
+  ha.nstages = tc::stages_for(LP, S, ha.mask ? 2 : 1, ha.mask != 0, 64 * 32);
+  ha.tmem_cols = tc::tmem_cols_for(LP);
+  ha.hpart = c.hpart.p;
+  ha.err = c.err.p;
+  mark(1);
+  tc::launch_h(c.map_bed_h, c.map_gt, ha, c.stream);
+  close_mark();
+  tc::launch_h_finish(c.N, c.npad, c.L, LP, c.hpart.p, nsp, c.cvec.p, Hx, c.stream);
+  if (sp.active) {
+    WindowArgs a{c.view(), c.permuted ? c.perm.p : nullptr, c.lut32.p, pos0, (int)n, c.LP, c.npad};
+    launch_window_h_sparse(a, sp, c.G.p, Hx, c.stream);
   }
 }
 
 // one window: G[pos0 .. pos0+n) = X_w Omega;  Hx += X_w^T G_w
 static void window_product(Context& c, int64_t pos0, int64_t n, double* Hx) {
   if (n <= 0) return;
+  if (c.tc) {
+    window_product_tc(c, pos0, n, Hx);
+    return;
+  }
   WindowArgs a{c.view(), c.permuted ? c.perm.p : nullptr, c.lut32.p, pos0, (int)n, c.LP, c.npad};
   SparseRows sp{};
   if (c.fitted && c.P.emu && c.nnz > 0) {
@@ -527,7 +720,25 @@ static void compute_g_and_h_window(Context& c, int pi) {
   }
 }
 
+// BF16 slices of the tensor-core form for epoch pi: PCAONE_PREC_BF16 uses one
+// slice for the winSVD range-finding epochs (2^pi < bands) and three from the
+// minimum-epoch boundary on; PCAONE_PREC_BF16X3 always three.
+static int slices_for_epoch(const Context& c, int pi) {
+  if (c.P.precision == PCAONE_PREC_BF16X3) return 3;
+  if (c.P.svd == PCAONE_SVD_WINDOW && std::ldexp(1.0, pi) < c.P.bands) return 1;
+  return 3;
+}
+
+static void check_tc_err(Context& c) {
+  if (!c.tc) return;
+  int e = 0;
+  PCAONE_CUDA(cudaMemcpyAsync(&e, c.err.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  if (e) throw Error(PCAONE_E_CUDA, "tensor-core pipeline: a bounded wait gave up (kernel aborted its tile)");
+}
+
 static void compute_g_and_h(Context& c, int pi) {
+  c.nslice_cur = c.tc ? slices_for_epoch(c, pi) : 1;
   if (c.P.svd == PCAONE_SVD_WINDOW)
     compute_g_and_h_window(c, pi);
   else
@@ -544,6 +755,7 @@ static int compute_usv(Context& c, int p, double tol) {
     auto t0 = clk::now();
     compute_g_and_h(c, pi);
     PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+    check_tc_err(c);
     c.collect_events();
     auto t1 = clk::now();
     c.t_prod += secs(t0, t1);

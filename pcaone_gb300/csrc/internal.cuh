@@ -96,6 +96,9 @@ void launch_window_h(const WindowArgs& a, const float* g32, float* hpart, int ns
 void launch_window_h_finish(const WindowArgs& a, const float* hpart, int nsplit, const SparseRows& sp,
                             const double* G, double* Hx, cudaStream_t s);
 
+// Hx[sample_e][:] += scale_j * value_e * G[pos][:] over the window's missing entries
+void launch_window_h_sparse(const WindowArgs& a, const SparseRows& sp, const double* G, double* Hx, cudaStream_t s);
+
 // dense FP64 helpers (dense64.cu); tall matrices are row-major with ld = LP
 int cross_blocks(int64_t rows);
 size_t cross_smem(int na, int nb, int sym);

@@ -324,4 +324,10 @@ void launch_window_h_finish(const WindowArgs& a, const float* hpart, int nsplit,
   }
 }
 
+void launch_window_h_sparse(const WindowArgs& a, const SparseRows& sp, const double* G, double* Hx, cudaStream_t s) {
+  if (!sp.active) return;
+  k_window_h_sparse<<<ceil_div((int64_t)a.nsnp * 32, 256), 256, 0, s>>>(a.pos0, a.nsnp, a.LP, sp, G, Hx);
+  PCAONE_LAUNCH_CHECK();
+}
+
 }  // namespace pcaone

@@ -24,6 +24,9 @@ pytestmark = pytest.mark.gpu
 
 ANGLE_TOL = 1e-6
 EIG_TOL = 1e-6
+# products with three BF16 slices of the test matrix carry 24 significand bits,
+# as the FP32 form; the mixed form uses one slice in the range-finding epochs
+PRECISIONS = {"fp32": capi.PREC_FP32, "bf16x3": capi.PREC_BF16X3, "bf16": capi.PREC_BF16}
 
 CASES = golden_cases()
 IDS = [c.name for c in CASES]
@@ -43,14 +46,14 @@ def c_params(opts, precision=capi.PREC_FP32):
                                standardize=1, precision=precision)
 
 
-def compare(U, S, V, Ur, Sr, Vr, label=""):
+def compare(U, S, V, Ur, Sr, Vr, label="", angle_tol=ANGLE_TOL, eig_tol=EIG_TOL):
     n = max(1, H.well_separated(Sr))
     ang_u = H.sin_largest_angle(U[:, :n], Ur[:, :n])
     ang_v = H.sin_largest_angle(V[:, :n], Vr[:, :n])
     eig = float(np.max(H.eig_relerr(S[:n], Sr[:n])))
     print(f"{label} n={n} sin(U)={ang_u:.2e} sin(V)={ang_v:.2e} eig={eig:.2e}")
-    assert ang_u <= ANGLE_TOL and ang_v <= ANGLE_TOL
-    assert eig <= EIG_TOL
+    assert ang_u <= angle_tol and ang_v <= angle_tol
+    assert eig <= eig_tol
     return n, ang_u, ang_v, eig
 
 
@@ -74,23 +77,25 @@ def test_counts_edge_cases():
     assert F[0] == 0.0 and F[1] == 1.0
 
 
+@pytest.mark.parametrize("prec", list(PRECISIONS), ids=list(PRECISIONS))
 @pytest.mark.parametrize("case", CASES, ids=IDS)
-def test_rsvd_vs_reference_outputs(case):
-    """Same Omega as the reference (golden Omg0), FP32 products: U, S, V agree
-    with the reference's FP64 results on the well-separated PCs."""
+def test_rsvd_vs_reference_outputs(case, prec):
+    """Same Omega as the reference (golden Omg0): U, S, V agree with the
+    reference's FP64 results on the well-separated PCs."""
     o = case.opts
     with capi.Context() as c:
         c.load_bed(case.packed, case.nsamples)
         c.set_omega(case.ref["Omg0"])
-        U, S, V, it = c.run_halko(c_params(o))
+        U, S, V, it = c.run_halko(c_params(o, PRECISIONS[prec]))
         if o.perm:
             assert np.array_equal(c.perm(), case.ref["perm"])
     if o.emu:
         assert abs(it - int(case.ref["meta"][2])) <= 1
-    compare(U, S, V, case.ref["U"], case.ref["S"], case.ref["V"], case.name)
+    compare(U, S, V, case.ref["U"], case.ref["S"], case.ref["V"], f"{case.name}[{prec}]")
 
 
-def test_first_epoch_products_vs_oracle():
+@pytest.mark.parametrize("prec", list(PRECISIONS), ids=list(PRECISIONS))
+def test_first_epoch_products_vs_oracle(prec):
     """computeGandH(pi=0) of the window method vs the oracle's FP64 G and H."""
     case = golden_case("wsvd_n301")
     o = case.opts
@@ -101,11 +106,22 @@ def test_first_epoch_products_vs_oracle():
     with capi.Context() as c:
         c.load_bed(case.packed, case.nsamples)
         c.set_omega(case.ref["Omg0"])
-        c.op_init(c_params(o))
+        c.op_init(c_params(o, PRECISIONS[prec]))
         c.set_flags(False, True)
         G, Hg = c.compute_g_and_h(0)
-    assert np.linalg.norm(G - Gr) / np.linalg.norm(Gr) < 1e-5
-    assert np.linalg.norm(Hg - Hr) / np.linalg.norm(Hr) < 1e-5
+    if prec == "bf16":
+        # one BF16 slice (8 significand bits): compare the first window, formed
+        # before any Omega update; later windows see an Omega re-orthonormalised
+        # from a perturbed H, whose trailing columns are ill-conditioned
+        bs = -(-case.nsnps // o.bands)
+        eg = np.linalg.norm(G[:bs] - Gr[:bs]) / np.linalg.norm(Gr[:bs])
+        print(f"epoch-0 first-window G [{prec}]: rel err {eg:.2e}")
+        assert eg < 1e-2
+        return
+    eg = np.linalg.norm(G - Gr) / np.linalg.norm(Gr)
+    eh = np.linalg.norm(Hg - Hr) / np.linalg.norm(Hr)
+    print(f"epoch-0 products [{prec}]: rel err G {eg:.2e} H {eh:.2e}")
+    assert eg < 1e-5 and eh < 1e-5
 
 
 def test_matvec_vs_oracle():
@@ -120,7 +136,8 @@ def test_matvec_vs_oracle():
     assert np.linalg.norm(y - yr) / np.linalg.norm(yr) < 1e-12
 
 
-def test_config1_vs_oracle():
+@pytest.mark.parametrize("prec", list(PRECISIONS), ids=list(PRECISIONS))
+def test_config1_vs_oracle(prec):
     """The 2,000 x 20,000 three-population workload, k=10, 7 epochs."""
     wl = synthetic.WORKLOADS["c1"]
     model = synthetic.model_for("c1", seed=1)
@@ -128,12 +145,13 @@ def test_config1_vs_oracle():
     omega = H.random_omega(112, model.nsamples, wl["k"] + wl["p"])
     d = H.OracleData(packed, model.nsamples, perm=True, bands=wl["bands"], omega0=omega)
     ref = H.run_pca_with_halko(d, wl["k"], wl["p"], maxp=wl["maxp"])
-    p = capi.default_params(k=wl["k"], oversamples=wl["p"], maxp=wl["maxp"], bands=wl["bands"])
+    p = capi.default_params(k=wl["k"], oversamples=wl["p"], maxp=wl["maxp"], bands=wl["bands"],
+                            precision=PRECISIONS[prec])
     with capi.Context() as c:
         c.load_bed(packed, model.nsamples)
         c.set_omega(omega)
         U, S, V, _ = c.run_halko(p)
-    compare(U, S, V, ref.U, ref.S, ref.V, "c1")
+    compare(U, S, V, ref.U, ref.S, ref.V, f"c1[{prec}]")
 
 
 def test_device_generator_matches_numpy():
