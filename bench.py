@@ -118,7 +118,8 @@ class ClockSampler:
 def workload_params(name: str, precision: str):
     from pcaone_gb300 import capi, synthetic
     wl = synthetic.WORKLOADS[name]
-    prec = {"fp32": capi.PREC_FP32, "bf16": capi.PREC_BF16, "fp8": capi.PREC_FP8}[precision]
+    prec = {"fp32": capi.PREC_FP32, "bf16": capi.PREC_BF16, "bf16x3": capi.PREC_BF16X3,
+            "fp8": capi.PREC_FP8}[precision]
     p = capi.default_params(svd=2, k=wl["k"], oversamples=wl["p"], maxp=wl["maxp"], bands=wl["bands"],
                             perm=1, standardize=1, precision=prec)
     return wl, p
@@ -323,7 +324,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2")
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16", "fp8"])
+    ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16", "bf16x3", "fp8"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     if args.impl == "reference":

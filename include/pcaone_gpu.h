@@ -35,12 +35,12 @@ extern "C" {
 
 /* precision of the block products G = X*Omega and H = X^T*G */
 #define PCAONE_PREC_FP32 0    /* FP32 SIMT products, FP64 window sums */
-#define PCAONE_PREC_BF16 1    /* tcgen05 tensor-core products: exact BF16 dosages, the test
-                                 matrix in one BF16 slice for the winSVD range-finding epochs
-                                 and three slices (24 significand bits) from the minimum-epoch
-                                 boundary on; FP32 accumulation, FP64 epilogue */
+#define PCAONE_PREC_BF16 1    /* tcgen05 tensor-core products: exact BF16 dosages and missing
+                                 mask; the test matrix and G split per column into three
+                                 integer BF16 slices (24 bits), exact integer accumulation in
+                                 TMEM, FP32/FP64 epilogue */
 #define PCAONE_PREC_FP8 2     /* reserved: FP8 e4m3 operands (not built yet) */
-#define PCAONE_PREC_BF16X3 3  /* tcgen05 tensor-core products with three BF16 slices in every epoch */
+#define PCAONE_PREC_BF16X3 3  /* same as PCAONE_PREC_BF16 */
 
 /* SVD method (Param::svd_t, src/Cmd.hpp:14) */
 #define PCAONE_SVD_SINGLE 1   /* NormalRsvdOpData: single-pass RSVD, -d 1 */

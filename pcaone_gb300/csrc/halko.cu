@@ -116,7 +116,8 @@ struct Context {
   DBuf<uint8_t> bedp;                 // packed rows in working order (shuffled window method)
   const uint8_t* bed_work = nullptr;  // packed rows the tensor-core kernels read
   DBuf<__nv_bfloat16> wsl, gt;        // W slices (3*LP x npad), Gh/Gm slices (6*LP x ldg)
-  DBuf<double> colsum, cpart, cvec;
+  DBuf<double> colsum, cpart, cvec, wunit, hunit, ghbuf, wrep;
+  DBuf<int> wexp, hexp;
   DBuf<float> part_m;
   DBuf<int> err;
   CUtensorMap map_bed_g{}, map_bed_h{}, map_w{}, map_gt{};
@@ -298,6 +299,12 @@ static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
   c.colsum.ensure(LP, c.stream);
   c.cvec.ensure(LP, c.stream);
   c.cpart.ensure((size_t)win * LP, c.stream, false);
+  c.ghbuf.ensure((size_t)win * LP, c.stream, false);
+  c.wrep.ensure((size_t)c.npad * LP, c.stream, false);
+  c.wunit.ensure((size_t)3 * LP, c.stream);
+  c.hunit.ensure((size_t)6 * LP, c.stream);
+  c.wexp.ensure(LP, c.stream);
+  c.hexp.ensure(LP, c.stream);
   c.err.ensure(1, c.stream);
   c.part.ensure(std::max(need_part, c.part.n), c.stream, false);
   c.part_m.ensure(need_part, c.stream, false);
@@ -379,8 +386,16 @@ static void op_init(Context& c, const pcaone_gpu_params& p) {
   c.hpart.ensure(need_hpart, c.stream, false);
   c.g32.ensure((size_t)std::max<int64_t>(1, win) * c.LP, c.stream, false);
   if (c.tc) {
-    tc_setup(c, (int)std::max<int64_t>(1, win), lens);
     ensure_missing_total(c);
+    // one TMEM accumulator per slice (and per mask part): 3 slices of LP columns
+    // each, doubled when missing genotypes need the mask product, within 512
+    // TMEM per CTA: one accumulator per slice (three slices of LP columns,
+    // doubled for the mask product) plus at least one stage of A operands
+    const bool any_miss = c.counts_total_missing > 0;
+    if ((any_miss ? 2 : 1) * 3 * c.LP + (any_miss ? 64 : 32) > 512)
+      throw Error(PCAONE_E_LIMIT, "tensor-core form: k + oversamples too large for TMEM "
+                                  "(at most 64 with missing genotypes, 144 without)");
+    tc_setup(c, (int)std::max<int64_t>(1, win), lens);
   }
   upload_omega0(c);
   c.have_op = true;
@@ -550,7 +565,8 @@ static void prepare_epoch0(Context& c, bool window) {
 static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   const int LP = c.LP, S = c.nslice_cur;
   if (c.w_slices != S) {
-    tc::launch_omega_slices(c.Omg.p, c.npad, c.N, LP, S, c.wsl.p, c.colsum.p, c.stream);
+    tc::launch_omega_slices(c.Omg.p, c.npad, c.N, LP, S, c.wsl.p, c.wunit.p, c.colsum.p, c.wexp.p, c.wrep.p,
+                            c.stream);
     c.w_slices = S;
   }
   int chunk, nch, per, nsp;
@@ -583,8 +599,9 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ga.npad = c.npad;
   ga.nchunks = nch;
   ga.mask = (mask && any_miss) ? 1 : 0;
-  ga.nstages = tc::stages_for(LP, S, 1, ga.mask != 0, 128 * 16);
-  ga.tmem_cols = tc::tmem_cols_for(ga.mask ? 2 * LP : LP);
+  ga.nstages = tc::stages_for(LP, S, 1, ga.mask ? 2 : 1, ga.mask != 0, 128 * 16);
+  ga.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ga.mask ? 2 : 1, ga.mask != 0, ga.nstages));
+  ga.wscale = c.wunit.p;
   ga.counts = c.counts.p;
   ga.perm = c.permuted ? c.perm.p : nullptr;
   ga.part_d = c.part.p;
@@ -611,12 +628,13 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   fa.omg = c.Omg.p;
   fa.sp = sp;
   fa.G = c.G.p;
+  fa.gh = c.ghbuf.p;
   fa.gt = c.gt.p;
   fa.cpart = c.cpart.p;
   // the B operand tensor map spans ldg columns; windows shorter than the
   // longest one leave the tail zeroed by the finish kernel
   fa.ldg = c.ldg;
-  tc::launch_g_finish(fa, c.cvec.p, c.stream);
+  tc::launch_g_finish(fa, c.hexp.p, c.hunit.p, c.cvec.p, c.stream);
   tc::HArgs ha{};
   ha.pos0 = pos0;
   ha.nsnp = (int)n;
@@ -626,8 +644,9 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ha.nsplit = nsp;
   ha.npad = c.npad;
   ha.mask = ga.mask;
-  ha.nstages = tc::stages_for(LP, S, ha.mask ? 2 : 1, ha.mask != 0, 64 * 32);
-  ha.tmem_cols = tc::tmem_cols_for(LP);
+  ha.nstages = tc::stages_for(LP, S, ha.mask ? 2 : 1, ha.mask ? 2 : 1, ha.mask != 0, 64 * 32);
+  ha.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ha.mask ? 2 : 1, ha.mask != 0, ha.nstages));
+  ha.hscale = c.hunit.p;
   ha.hpart = c.hpart.p;
   ha.err = c.err.p;
   mark(1);
@@ -720,12 +739,12 @@ static void compute_g_and_h_window(Context& c, int pi) {
   }
 }
 
-// BF16 slices of the tensor-core form for epoch pi: PCAONE_PREC_BF16 uses one
-// slice for the winSVD range-finding epochs (2^pi < bands) and three from the
-// minimum-epoch boundary on; PCAONE_PREC_BF16X3 always three.
+// integer slices of the tensor-core form: three (24 bits per column) in every
+// epoch.  Fewer slices in the range-finding epochs were measured to move the
+// converged PCs by up to 3e-4 (principal angle) on a five-population sample.
 static int slices_for_epoch(const Context& c, int pi) {
-  if (c.P.precision == PCAONE_PREC_BF16X3) return 3;
-  if (c.P.svd == PCAONE_SVD_WINDOW && std::ldexp(1.0, pi) < c.P.bands) return 1;
+  (void)c;
+  (void)pi;
   return 3;
 }
 

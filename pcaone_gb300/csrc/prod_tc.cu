@@ -9,21 +9,30 @@
 //   G_j  = s_j * ( 1/2 (D W)_j - f_j * colsum(W) + f_j (M W)_j )
 //   H_i += (D Gh)_i - c + (M Gm)_i,  Gh_j = 1/2 s_j G_j,  Gm_j = 2 f_j Gh_j,
 //                                     c = sum_j 2 f_j Gh_j
-// where W is the test matrix Omega as held in BF16 slices (W = sum of up to
-// three BF16 slices, so that three slices carry 24 significand bits).  The
-// centring terms use the same sliced values as the products, so the operator
-// applied is exactly X times the sliced matrix.
+// where W is the test matrix Omega held as S integer slices (S = 1 or 3):
+// per column l a power-of-two unit u_ls = 2^(E_l - 7 - 8s) with
+// max_i |Omega_il| < 2^E_l, and W_il = sum_s u_ls * w_sil with integers
+// |w_sil| <= 128, exact in BF16 (Ozaki-style error-free splitting; three slices
+// carry 24 significand bits).  Each slice has its own TMEM accumulator: the
+// products d*w and m*w are integers of magnitude <= 256 and every partial sum of
+// a CTA (K <= 4096) stays below 2^24, so the tensor core accumulates exactly and
+// no rounding bias enters; the epilogue combines the slices in FP64 with their
+// units.  Gh and Gm are split the same way (per-column units over the window).
+// The centring terms use the same sliced values as the products, so the
+// operator applied is exactly X times the sliced matrix.
 //
 // Kernels (one CTA = 128 threads = one warpgroup; thread 0 issues TMA and MMA):
 //   k_tc_g : tile of 128 SNPs x one chunk of samples.  TMA brings the packed
-//            tile (128 rows x 16 bytes) and the Omega^T slice tiles (L x 64,
-//            128B swizzle); threads decode the packed bytes into the A tile(s)
-//            (128 x 64 BF16, K-major, 128B swizzle); tcgen05.mma accumulates
-//            D*W and M*W in TMEM; the epilogue (tcgen05.ld) writes FP32
-//            partial sums, combined in FP64 by k_tc_g_finish.
+//            tile (128 rows x 16 bytes) and the W^T slice tiles (S*L rows x 64,
+//            128B swizzle, K-major B operand); decoder warps turn the packed
+//            bytes into the BF16 A operands D and M, written straight into
+//            TMEM (tcgen05.st); tcgen05.mma (A from TMEM, B from shared memory,
+//            the S slices concatenated along N) accumulates D*W and M*W in
+//            TMEM; the epilogue (tcgen05.ld) writes FP32 partial sums,
+//            combined in FP64 by k_tc_g_finish.
 //   k_tc_h : tile of 128 samples x one split of the window's SNPs.  TMA brings
 //            the packed tile (64 SNP rows x 32 bytes) and the Gh^T / Gm^T slice
-//            tiles; threads decode and transpose into D^T / M^T A tiles.
+//            tiles; decoder warps transpose into the D^T / M^T A operands.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -38,7 +47,7 @@ namespace tc {
 
 namespace {
 
-constexpr int kThreads = 128;
+constexpr int kThreads = 384;          // 12 warps: TMA producer, MMA issuer, 8 decode / TMEM-epilogue warps
 constexpr int kStepK = 64;              // K elements per pipeline stage (128 B of BF16 per row)
 constexpr int kMaxStages = 4;
 constexpr long long kTimeoutCycles = 4000000000ll;  // about 2 s at 2 GHz
@@ -86,7 +95,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// Pull a 2-D box into L2 ahead of its TMA load (no shared-memory side effect).
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int c0, int c1) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(reinterpret_cast<uint64_t>(map)),
+               "r"(c0), "r"(c1)
+               : "memory");
+}
+
+constexpr int kPrefetchSteps = 8;  // packed tiles are pulled into L2 this many steps ahead
+
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -101,16 +118,28 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
 }
 
-// D[tmem] (+)= A[smem desc] * B[smem desc]^T, kind::f16 (BF16 in, FP32 accumulate)
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
-                                         uint32_t accumulate) {
+// D[tmem] (+)= A[tmem] * B[smem desc]^T, kind::f16; A rows = TMEM lanes, two
+// BF16 K elements per 32-bit column
+__device__ __forceinline__ void mma_bf16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
+                                            uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
+
+// 32 lanes x 16 consecutive 32-bit columns from registers into TMEM
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* r) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -152,36 +181,84 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-constexpr uint16_t kBf16One = 0x3F80, kBf16Two = 0x4000;
+constexpr uint16_t kBf16One = 0x3F80;
 
-__device__ __forceinline__ uint32_t dosage_bf16(uint32_t code) {
-  // 00 -> 2, 10 -> 1, 01 and 11 -> 0
-  return code == 0u ? kBf16Two : (code == 2u ? kBf16One : 0u);
-}
-__device__ __forceinline__ uint32_t missing_bf16(uint32_t code) { return code == 1u ? kBf16One : 0u; }
 
-__device__ __forceinline__ uint32_t swz(uint32_t row, uint32_t chunk) {
-  // byte offset of 16-byte chunk `chunk` of row `row` in a 128B-swizzled K-major tile
-  return row * 128u + ((chunk ^ (row & 7u)) << 4);
+// SWAR decode of two 2-bit codes held at bits 0-1 and 16-17 of x into two BF16
+// values (low and high half-words): dosage 00 -> 2.0 (0x4000), 10 -> 1.0
+// (0x3F80), 01 and 11 -> 0; missing indicator 01 -> 1.0.
+__device__ __forceinline__ uint32_t dosage_pair(uint32_t x) {
+  const uint32_t lo = x & 0x00010001u, hi = (x >> 1) & 0x00010001u;
+  return (0x40004000u - (hi << 7)) & ~(lo * 0xFFFFu);
 }
+__device__ __forceinline__ uint32_t missing_pair(uint32_t x) {
+  const uint32_t lo = x & 0x00010001u, hi = (x >> 1) & 0x00010001u;
+  return (lo & ~hi) * (uint32_t)kBf16One;
+}
+
 
 struct SmemLayout {
   uint32_t a_d, a_m, b, p, stage_bytes;
 };
 
 __host__ __device__ inline SmemLayout layout_for(int LP, int nslice, int bparts, bool mask, int pbytes) {
+  // the A operands live in TMEM; a stage holds the B slices and the packed tile
   SmemLayout s{};
   uint32_t off = 0;
-  s.a_d = off;
-  off += 128 * 128;
-  s.a_m = off;
-  if (mask) off += 128 * 128;
+  (void)mask;
+  s.a_d = 0;
+  s.a_m = 0;
   s.b = off;
   off += (uint32_t)(bparts * nslice * LP * 128);
   s.p = off;
   off += (uint32_t)pbytes;
   s.stage_bytes = (off + 1023u) & ~1023u;
   return s;
+}
+
+// Issue D[tmem col0 ...] (+)= A * [B rows b_row0 .. b_row0+ncols)^T for one
+// 16-wide K step, the B rows (the slices of one operand, contiguous in shared
+// memory) concatenated along N and cut into MMAs of at most kMaxNTmemA columns
+// (n0 is a multiple of 256 rows, so every B sub-tile starts on a 1024-byte
+// swizzle-atom boundary).
+// MMA shape limit for M = 128: N <= 256 columns.
+constexpr int kMaxNTmemA = 256;
+
+__device__ __forceinline__ void mma_cat(uint32_t tmem_col0, uint32_t a_tmem, uint32_t b_addr, int ncols,
+                                        uint32_t accumulate) {
+  for (int n0 = 0; n0 < ncols; n0 += kMaxNTmemA) {
+    const int n = min(kMaxNTmemA, ncols - n0);
+    mma_bf16_ta(tmem_col0 + n0, a_tmem, desc_sw128(b_addr + n0 * 128), idesc_bf16(128, n), accumulate);
+  }
+}
+
+// Warp roles of both kernels (384 threads): warp 0 lane 0 issues the TMA
+// loads of each pipeline stage, warp 1 lane 0 issues the MMAs, warps 4-11
+// decode the packed tile into the A operand(s) and finally read the
+// accumulators out of TMEM (warp w reads lanes 32*(w%4) .. +31, warps 4-7 the
+// first half of the columns and warps 8-11 the second).  Per stage s: full[s]
+// (TMA bytes landed), dec[s] (256 decoder arrivals), empty[s]
+// (tcgen05.commit of the stage's MMAs).  Every wait is bounded; a role that gives up sets the shared
+// abort flag, which makes every other wait return, so the CTA always reaches
+// its final barrier and frees its TMEM.
+constexpr int kDecodeWarp0 = 4;
+constexpr int kDecoders = 256;
+
+__device__ __forceinline__ bool role_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*abort_flag) return false;
+    if (clock64() - t0 > kTimeoutCycles) {
+      *abort_flag = 1;
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -191,10 +268,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_tc_g(const __grid_constant__ CUtensorMap map_bed, const __grid_constant__ CUtensorMap map_w, GArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  __shared__ uint64_t full_bar[kMaxStages], mma_bar[kMaxStages];
+  __shared__ uint64_t full_bar[kMaxStages], dec_bar[kMaxStages], empty_bar[kMaxStages], acc_bar;
   __shared__ uint32_t tmem_sh;
-  __shared__ int abort_sh, miss_sh;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  __shared__ volatile int abort_sh;
+  __shared__ int miss_sh;
+  __shared__ float unit[3 * 112];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int LP = a.LP, S = a.nslice;
   const SmemLayout lay = layout_for(LP, S, 1, a.mask != 0, 128 * 16);
   const int row0 = blockIdx.x * 128;                  // window-local first SNP of the tile
@@ -202,23 +281,25 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int kend = min(kbeg + a.chunk, a.npad);
   const int nk = (kend - kbeg + kStepK - 1) / kStepK;
   const int nst = a.nstages;
+  const int ncat = S * LP;  // slices concatenated along N
 
   if (tid == 0) {
     abort_sh = 0;
     miss_sh = 0;
     for (int s = 0; s < nst; ++s) {
       mbar_init(&full_bar[s], 1);
-      mbar_init(&mma_bar[s], 1);
+      mbar_init(&dec_bar[s], kDecoders);
+      mbar_init(&empty_bar[s], 1);
     }
+    mbar_init(&acc_bar, 1);
     fence_mbar_init();
   }
+  for (int e = tid; e < S * LP; e += kThreads) unit[e] = (float)a.wscale[e];
   __syncthreads();
-  // does the tile hold a missing genotype? (the mask product is skipped if not)
-  if (a.mask) {
-    const int j = row0 + tid;
+  if (a.mask) {  // does the tile hold a missing genotype? (the mask product is skipped if not)
     int has = 0;
-    if (j < a.nsnp) {
-      const int64_t pos = a.pos0 + j;
+    if (tid < 128 && row0 + tid < a.nsnp) {
+      const int64_t pos = a.pos0 + row0 + tid;
       const int64_t snp = a.perm ? (int64_t)a.perm[pos] : pos;
       has = a.counts[snp * 4 + 1] > 0;
     }
@@ -230,115 +311,114 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc_fence_after();
   const uint32_t tmem = tmem_sh;
   const bool use_m = a.mask && miss_sh;
-  const uint32_t idesc = idesc_bf16(128, LP);
-  const uint32_t tx_bytes = 128 * 16 + (uint32_t)(S * LP * 128);
+  // TMEM columns: accumulators [0, a_col0), then per stage A_D (32 columns =
+  // 64 BF16 K elements) and A_M (32 more when the mask product is formed)
+  const uint32_t a_col0 = (uint32_t)((a.mask ? 2 : 1) * ncat);
+  const uint32_t a_stride = a.mask ? 64u : 32u;
 
-  auto issue = [&](int stage, int kb) {
-    uint8_t* base = smem + stage * lay.stage_bytes;
-    const int k0 = kbeg + kb * kStepK;
-    mbar_expect_tx(&full_bar[stage], tx_bytes);
-    tma_load_2d(base + lay.p, &map_bed, k0 >> 2, (int)(a.pos0 + row0), &full_bar[stage]);
-    for (int s = 0; s < S; ++s) tma_load_2d(base + lay.b + s * LP * 128, &map_w, k0, s * LP, &full_bar[stage]);
-  };
-
-  if (tid == 0)
-    for (int s = 0; s < nst && s < nk; ++s) issue(s, s);
-  int issued_upto = min(nst, nk);  // k-steps whose loads have been issued (thread 0's view)
-
-  for (int kb = 0; kb < nk; ++kb) {
-    const int stage = kb % nst;
-    const uint32_t ph = (uint32_t)(kb / nst) & 1u;
-    if (tid == 0 && kb >= 1 && kb - 1 + nst < nk) {
-      const int ps = (kb - 1) % nst;
-      if (!mbar_wait(&mma_bar[ps], (uint32_t)((kb - 1) / nst) & 1u)) {
-        abort_sh = 1;
-      } else {
-        issue(ps, kb - 1 + nst);
-        issued_upto = kb - 1 + nst + 1;
+  if (warp == 0) {
+    // ---- TMA producer ----
+    if (lane == 0) {
+      const uint32_t tx_bytes = 128 * 16 + (uint32_t)(ncat * 128);
+      int issued = 0;
+      for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
+        tma_prefetch_2d(&map_bed, (kbeg + kb * kStepK) >> 2, (int)(a.pos0 + row0));
+      for (int kb = 0; kb < nk; ++kb) {
+        const int st = kb % nst;
+        if (kb + kPrefetchSteps < nk)
+          tma_prefetch_2d(&map_bed, (kbeg + (kb + kPrefetchSteps) * kStepK) >> 2, (int)(a.pos0 + row0));
+        if (kb >= nst && !role_wait(&empty_bar[st], (uint32_t)(kb / nst - 1) & 1u, &abort_sh)) break;
+        uint8_t* base = smem + st * lay.stage_bytes;
+        const int k0 = kbeg + kb * kStepK;
+        mbar_expect_tx(&full_bar[st], tx_bytes);
+        tma_load_2d(base + lay.p, &map_bed, k0 >> 2, (int)(a.pos0 + row0), &full_bar[st]);
+        for (int s = 0; s < S; ++s) tma_load_2d(base + lay.b + s * LP * 128, &map_w, k0, s * LP, &full_bar[st]);
+        issued = kb + 1;
+      }
+      if (abort_sh) {  // let every issued copy land before the CTA exits
+        for (int kb = 0; kb < issued; ++kb) mbar_wait(&full_bar[kb % nst], (uint32_t)(kb / nst) & 1u);
       }
     }
-    if (!mbar_wait(&full_bar[stage], ph)) abort_sh = 1;
-    uint8_t* base = smem + stage * lay.stage_bytes;
-    // decode: thread = SNP row of the tile, 16 packed bytes = 64 samples
-    {
-      const uint4 pk = *reinterpret_cast<const uint4*>(base + lay.p + tid * 16);
-      const uint32_t w[4] = {pk.x, pk.y, pk.z, pk.w};
+  } else if (warp == 1) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      for (int kb = 0; kb < nk; ++kb) {
+        const int st = kb % nst;
+        if (!role_wait(&dec_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
+        tc_fence_after();
+        uint8_t* base = smem + st * lay.stage_bytes;
+        const uint32_t bb = smem_u32(base + lay.b);
+        const uint32_t ad = tmem + a_col0 + st * a_stride, am = ad + 32;
 #pragma unroll
-      for (int c = 0; c < 8; ++c) {        // 16-byte chunk c = samples 8c .. 8c+7 (two packed bytes)
-        const uint32_t bits = (w[c >> 1] >> ((c & 1) * 16)) & 0xFFFFu;
-        uint32_t q[4], qm[4];
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          const uint32_t c0 = (bits >> (4 * t)) & 3u, c1 = (bits >> (4 * t + 2)) & 3u;
-          q[t] = dosage_bf16(c0) | (dosage_bf16(c1) << 16);
-          qm[t] = missing_bf16(c0) | (missing_bf16(c1) << 16);
+        for (int kk = 0; kk < kStepK / 16; ++kk) {
+          const uint32_t acc = (kb | kk) != 0;
+          mma_cat(tmem, ad + kk * 8, bb + kk * 32, ncat, acc);
+          if (use_m) mma_cat(tmem + ncat, am + kk * 8, bb + kk * 32, ncat, acc);
         }
-        *reinterpret_cast<uint4*>(base + lay.a_d + swz(tid, c)) = make_uint4(q[0], q[1], q[2], q[3]);
-        if (use_m) *reinterpret_cast<uint4*>(base + lay.a_m + swz(tid, c)) = make_uint4(qm[0], qm[1], qm[2], qm[3]);
+        mma_commit(&empty_bar[st]);
       }
+      mma_commit(&acc_bar);  // arrives once every MMA above has completed
     }
-    fence_proxy_async();
-    __syncthreads();
-    if (abort_sh) break;
-    if (tid == 0) {
-      tc_fence_after();
-      const uint32_t ad = smem_u32(base + lay.a_d), am = smem_u32(base + lay.a_m), bb = smem_u32(base + lay.b);
+  } else if (warp >= kDecodeWarp0) {
+    // ---- decoders: TMEM lane quarter q4 = warp % 4 (row r = SNP 32*q4 + lane of
+    // the tile), K half ch: samples 32ch .. 32ch+31 of the step (8 packed bytes)
+    // -> 16 columns of BF16 pairs into the stage's A_D (and A_M) in TMEM ----
+    const int q4 = warp & 3, ch = (warp - kDecodeWarp0) >> 2;
+    const int r = q4 * 32 + lane;
+    const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
+    for (int kb = 0; kb < nk; ++kb) {
+      const int st = kb % nst;
+      if (!role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
+      uint8_t* base = smem + st * lay.stage_bytes;
+      const uint2 pk = *reinterpret_cast<const uint2*>(base + lay.p + r * 16 + ch * 8);
+      uint32_t wd[16], wm[16];
 #pragma unroll
-      for (int kk = 0; kk < kStepK / 16; ++kk) {
-        for (int s = 0; s < S; ++s) {
-          const uint64_t bdesc = desc_sw128(bb + s * LP * 128 + kk * 32);
-          const uint32_t acc = (kb | kk | s) != 0;
-          mma_bf16(tmem, desc_sw128(ad + kk * 32), bdesc, idesc, acc);
-          if (use_m) mma_bf16(tmem + LP, desc_sw128(am + kk * 32), bdesc, idesc, acc);
-        }
+      for (int e = 0; e < 16; ++e) {
+        const uint32_t w32 = e < 8 ? pk.x : pk.y;
+        const int sh = 4 * (e & 7);
+        const uint32_t x = ((w32 >> sh) & 3u) | (((w32 >> (sh + 2)) & 3u) << 16);
+        wd[e] = dosage_pair(x);
+        wm[e] = missing_pair(x);
       }
-      mma_commit(&mma_bar[stage]);
+      const uint32_t acol = tmem + lane_off + a_col0 + st * a_stride + ch * 16;
+      tmem_st16(acol, wd);
+      if (use_m) tmem_st16(acol + 32, wm);
+      tmem_wait_st();
+      tc_fence_before();
+      mbar_arrive(&dec_bar[st]);
     }
-  }
-  // drain: the last committed MMA group, then any loads still in flight
-  if (tid == 0) {
-    if (!abort_sh && nk > 0) {
-      if (!mbar_wait(&mma_bar[(nk - 1) % nst], (uint32_t)((nk - 1) / nst) & 1u)) abort_sh = 1;
-    }
-    if (abort_sh) {
-      *a.err = 1;
-      // wait (bounded) for every issued load so no copy lands after exit
-      for (int kb = 0; kb < issued_upto; ++kb) mbar_wait(&full_bar[kb % nst], (uint32_t)(kb / nst) & 1u);
-    }
-  }
-  __syncthreads();
-  tc_fence_after();
-  if (!abort_sh) {
-    const int j = row0 + tid;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    // ---- epilogue: exact integer slice sums times power-of-two units (FP32 FMAs) ----
+    const bool ok = nk > 0 && role_wait(&acc_bar, 0u, &abort_sh);
+    tc_fence_after();
+    const int quarter = warp & 3, chalf = (warp - kDecodeWarp0) >> 2;
+    const int j = row0 + quarter * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
     float v[8];
-    for (int c0 = 0; c0 < LP; c0 += 8) {
-      if (nk > 0) {
-        tmem_ld8(lane_base + c0, v);
-      } else {
-        for (int t = 0; t < 8; ++t) v[t] = 0.f;
-      }
-      if (j < a.nsnp) {
-        float* dst = a.part_d + ((size_t)blockIdx.y * a.nsnp + j) * LP + c0;
-        *reinterpret_cast<float4*>(dst) = make_float4(v[0], v[1], v[2], v[3]);
-        *reinterpret_cast<float4*>(dst + 4) = make_float4(v[4], v[5], v[6], v[7]);
-      }
-      if (a.mask) {
-        if (use_m && nk > 0) {
-          tmem_ld8(lane_base + LP + c0, v);
-        } else {
-          for (int t = 0; t < 8; ++t) v[t] = 0.f;
-        }
-        if (j < a.nsnp) {
-          float* dst = a.part_m + ((size_t)blockIdx.y * a.nsnp + j) * LP + c0;
-          *reinterpret_cast<float4*>(dst) = make_float4(v[0], v[1], v[2], v[3]);
-          *reinterpret_cast<float4*>(dst + 4) = make_float4(v[4], v[5], v[6], v[7]);
+    if (!abort_sh) {
+      for (int part = 0; part < (a.mask ? 2 : 1); ++part) {
+        const bool live = ok && (part == 0 || use_m);
+        float* out = part == 0 ? a.part_d : a.part_m;
+        for (int c0 = chalf * (LP / 2); c0 < (chalf + 1) * (LP / 2); c0 += 8) {
+          float sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          if (live) {
+            for (int s = S - 1; s >= 0; --s) {
+              tmem_ld8(lane_base + part * ncat + s * LP + c0, v);
+#pragma unroll
+              for (int t = 0; t < 8; ++t) sum[t] = fmaf(unit[s * LP + c0 + t], v[t], sum[t]);
+            }
+          }
+          if (j < a.nsnp) {
+            float* dst = out + ((size_t)blockIdx.y * a.nsnp + j) * LP + c0;
+            *reinterpret_cast<float4*>(dst) = make_float4(sum[0], sum[1], sum[2], sum[3]);
+            *reinterpret_cast<float4*>(dst + 4) = make_float4(sum[4], sum[5], sum[6], sum[7]);
+          }
         }
       }
     }
   }
   tc_fence_before();
   __syncthreads();
+  if (tid == 0 && abort_sh) *a.err = 1;
   if (warp == 0) tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
 }
 
@@ -349,12 +429,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_tc_h(const __grid_constant__ CUtensorMap map_bed, const __grid_constant__ CUtensorMap map_g, HArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  __shared__ uint64_t full_bar[kMaxStages], mma_bar[kMaxStages];
+  __shared__ uint64_t full_bar[kMaxStages], dec_bar[kMaxStages], empty_bar[kMaxStages], acc_bar;
   __shared__ uint32_t tmem_sh;
-  __shared__ int abort_sh;
-  __shared__ uint2 lut[256];   // packed byte -> dosage (BF16) of its 4 samples
-  __shared__ uint2 lutm[256];  // packed byte -> missing indicator (BF16) of its 4 samples
-  const int tid = threadIdx.x, warp = tid >> 5;
+  __shared__ volatile int abort_sh;
+  __shared__ float unit[6 * 112];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int LP = a.LP, S = a.nslice;
   const bool mask = a.mask != 0;
   const SmemLayout lay = layout_for(LP, S, mask ? 2 : 1, mask, 64 * 32);
@@ -363,21 +442,18 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int je = min(jb + a.per_split, a.nsnp);
   const int nk = je > jb ? (je - jb + kStepK - 1) / kStepK : 0;
   const int nst = a.nstages;
+  const int bparts = mask ? 2 : 1;
+  const int ncat = S * LP;
 
-  for (int b = tid; b < 256; b += kThreads) {
-    const uint32_t d0 = dosage_bf16(b & 3), d1 = dosage_bf16((b >> 2) & 3), d2 = dosage_bf16((b >> 4) & 3),
-                   d3 = dosage_bf16((b >> 6) & 3);
-    lut[b] = make_uint2(d0 | (d1 << 16), d2 | (d3 << 16));
-    const uint32_t m0 = missing_bf16(b & 3), m1 = missing_bf16((b >> 2) & 3), m2 = missing_bf16((b >> 4) & 3),
-                   m3 = missing_bf16((b >> 6) & 3);
-    lutm[b] = make_uint2(m0 | (m1 << 16), m2 | (m3 << 16));
-  }
+  for (int e = tid; e < bparts * ncat; e += kThreads) unit[e] = (float)a.hscale[e];
   if (tid == 0) {
     abort_sh = 0;
     for (int s = 0; s < nst; ++s) {
       mbar_init(&full_bar[s], 1);
-      mbar_init(&mma_bar[s], 1);
+      mbar_init(&dec_bar[s], kDecoders);
+      mbar_init(&empty_bar[s], 1);
     }
+    mbar_init(&acc_bar, 1);
     fence_mbar_init();
   }
   if (warp == 0) tmem_alloc(&tmem_sh, (uint32_t)a.tmem_cols);
@@ -385,123 +461,107 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_sh;
-  const uint32_t idesc = idesc_bf16(128, LP);
-  const int bparts = mask ? 2 : 1;
-  const uint32_t tx_bytes = 64 * 32 + (uint32_t)(bparts * S * LP * 128);
+  const uint32_t a_col0 = (uint32_t)(bparts * ncat);
+  const uint32_t a_stride = mask ? 64u : 32u;
 
-  auto issue = [&](int stage, int kb) {
-    uint8_t* base = smem + stage * lay.stage_bytes;
-    const int j0 = jb + kb * kStepK;
-    mbar_expect_tx(&full_bar[stage], tx_bytes);
-    tma_load_2d(base + lay.p, &map_bed, samp0 >> 2, (int)(a.pos0 + j0), &full_bar[stage]);
-    for (int r = 0; r < bparts * S; ++r)
-      tma_load_2d(base + lay.b + r * LP * 128, &map_g, j0, r * LP, &full_bar[stage]);
-  };
-  if (tid == 0)
-    for (int s = 0; s < nst && s < nk; ++s) issue(s, s);
-  int issued_upto = min(nst, nk);
-
-  // decode assignment: byte column q (4 samples), SNP group g (16 SNPs)
-  const int q = tid & 31, g = tid >> 5;
-  for (int kb = 0; kb < nk; ++kb) {
-    const int stage = kb % nst;
-    const uint32_t ph = (uint32_t)(kb / nst) & 1u;
-    if (tid == 0 && kb >= 1 && kb - 1 + nst < nk) {
-      const int ps = (kb - 1) % nst;
-      if (!mbar_wait(&mma_bar[ps], (uint32_t)((kb - 1) / nst) & 1u)) {
-        abort_sh = 1;
-      } else {
-        issue(ps, kb - 1 + nst);
-        issued_upto = kb - 1 + nst + 1;
+  if (warp == 0) {
+    if (lane == 0) {
+      const uint32_t tx_bytes = 64 * 32 + (uint32_t)(bparts * ncat * 128);
+      int issued = 0;
+      for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
+        tma_prefetch_2d(&map_bed, samp0 >> 2, (int)(a.pos0 + jb + kb * kStepK));
+      for (int kb = 0; kb < nk; ++kb) {
+        const int st = kb % nst;
+        if (kb + kPrefetchSteps < nk)
+          tma_prefetch_2d(&map_bed, samp0 >> 2, (int)(a.pos0 + jb + (kb + kPrefetchSteps) * kStepK));
+        if (kb >= nst && !role_wait(&empty_bar[st], (uint32_t)(kb / nst - 1) & 1u, &abort_sh)) break;
+        uint8_t* base = smem + st * lay.stage_bytes;
+        const int j0 = jb + kb * kStepK;
+        mbar_expect_tx(&full_bar[st], tx_bytes);
+        tma_load_2d(base + lay.p, &map_bed, samp0 >> 2, (int)(a.pos0 + j0), &full_bar[st]);
+        for (int r = 0; r < bparts * S; ++r)
+          tma_load_2d(base + lay.b + r * LP * 128, &map_g, j0, r * LP, &full_bar[st]);
+        issued = kb + 1;
+      }
+      if (abort_sh) {
+        for (int kb = 0; kb < issued; ++kb) mbar_wait(&full_bar[kb % nst], (uint32_t)(kb / nst) & 1u);
       }
     }
-    if (!mbar_wait(&full_bar[stage], ph)) abort_sh = 1;
-    uint8_t* base = smem + stage * lay.stage_bytes;
-    {
-      // 16 SNP rows of byte column q -> for each of the 4 samples 4q..4q+3,
-      // 16 consecutive K elements (two 16-byte chunks 2g, 2g+1)
-      uint2 lv[16];
+  } else if (warp == 1) {
+    if (lane == 0) {
+      for (int kb = 0; kb < nk; ++kb) {
+        const int st = kb % nst;
+        if (!role_wait(&dec_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
+        tc_fence_after();
+        uint8_t* base = smem + st * lay.stage_bytes;
+        const uint32_t bb = smem_u32(base + lay.b);
+        const uint32_t ad = tmem + a_col0 + st * a_stride, am = ad + 32;
 #pragma unroll
-      for (int jj = 0; jj < 16; ++jj) lv[jj] = lut[base[lay.p + (g * 16 + jj) * 32 + q]];
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const uint32_t row = (uint32_t)(q * 4 + t);
-        const uint32_t sel = (t & 1) ? 0x7632u : 0x5410u;
-        uint32_t w[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-          const uint32_t lo = (t < 2) ? lv[2 * e].x : lv[2 * e].y;
-          const uint32_t hi = (t < 2) ? lv[2 * e + 1].x : lv[2 * e + 1].y;
-          w[e] = __byte_perm(lo, hi, sel);
+        for (int kk = 0; kk < kStepK / 16; ++kk) {
+          const uint32_t acc = (kb | kk) != 0;
+          mma_cat(tmem, ad + kk * 8, bb + kk * 32, ncat, acc);
+          if (mask) mma_cat(tmem + ncat, am + kk * 8, bb + ncat * 128 + kk * 32, ncat, acc);
         }
-        *reinterpret_cast<uint4*>(base + lay.a_d + swz(row, 2 * g)) = make_uint4(w[0], w[1], w[2], w[3]);
-        *reinterpret_cast<uint4*>(base + lay.a_d + swz(row, 2 * g + 1)) = make_uint4(w[4], w[5], w[6], w[7]);
+        mma_commit(&empty_bar[st]);
       }
-      if (mask) {
+      mma_commit(&acc_bar);
+    }
+  } else if (warp >= kDecodeWarp0) {
+    // ---- decoders: TMEM lane quarter q4 (row r = sample 32*q4 + lane of the
+    // tile), K half ch: SNPs 32ch .. 32ch+31 of the step, one packed byte each
+    // (column r/4 of the SNP row) -> 16 columns of BF16 pairs in TMEM ----
+    const int q4 = warp & 3, ch = (warp - kDecodeWarp0) >> 2;
+    const int r = q4 * 32 + lane;
+    const int sh = 2 * (r & 3);
+    const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
+    for (int kb = 0; kb < nk; ++kb) {
+      const int st = kb % nst;
+      if (!role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
+      const uint8_t* pt = smem + st * lay.stage_bytes + lay.p + (ch * 32) * 32 + (r >> 2);
+      uint32_t wd[16], wm[16];
 #pragma unroll
-        for (int jj = 0; jj < 16; ++jj) lv[jj] = lutm[base[lay.p + (g * 16 + jj) * 32 + q]];
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          const uint32_t row = (uint32_t)(q * 4 + t);
-          const uint32_t sel = (t & 1) ? 0x7632u : 0x5410u;
-          uint32_t w[8];
-#pragma unroll
-          for (int e = 0; e < 8; ++e) {
-            const uint32_t lo = (t < 2) ? lv[2 * e].x : lv[2 * e].y;
-            const uint32_t hi = (t < 2) ? lv[2 * e + 1].x : lv[2 * e + 1].y;
-            w[e] = __byte_perm(lo, hi, sel);
-          }
-          *reinterpret_cast<uint4*>(base + lay.a_m + swz(row, 2 * g)) = make_uint4(w[0], w[1], w[2], w[3]);
-          *reinterpret_cast<uint4*>(base + lay.a_m + swz(row, 2 * g + 1)) = make_uint4(w[4], w[5], w[6], w[7]);
-        }
+      for (int e = 0; e < 16; ++e) {
+        const uint32_t b0 = pt[(2 * e) * 32], b1 = pt[(2 * e + 1) * 32];
+        const uint32_t x = ((b0 >> sh) & 3u) | (((b1 >> sh) & 3u) << 16);
+        wd[e] = dosage_pair(x);
+        wm[e] = missing_pair(x);
       }
+      const uint32_t acol = tmem + lane_off + a_col0 + st * a_stride + ch * 16;
+      tmem_st16(acol, wd);
+      if (mask) tmem_st16(acol + 32, wm);
+      tmem_wait_st();
+      tc_fence_before();
+      mbar_arrive(&dec_bar[st]);
     }
-    fence_proxy_async();
-    __syncthreads();
-    if (abort_sh) break;
-    if (tid == 0) {
-      tc_fence_after();
-      const uint32_t ad = smem_u32(base + lay.a_d), am = smem_u32(base + lay.a_m), bb = smem_u32(base + lay.b);
-#pragma unroll
-      for (int kk = 0; kk < kStepK / 16; ++kk) {
-        for (int s = 0; s < S; ++s) {
-          const uint32_t acc = (kb | kk | s) != 0;
-          mma_bf16(tmem, desc_sw128(ad + kk * 32), desc_sw128(bb + s * LP * 128 + kk * 32), idesc, acc);
-          if (mask)
-            mma_bf16(tmem, desc_sw128(am + kk * 32), desc_sw128(bb + (S + s) * LP * 128 + kk * 32), idesc, 1u);
-        }
-      }
-      mma_commit(&mma_bar[stage]);
-    }
-  }
-  if (tid == 0) {
-    if (!abort_sh && nk > 0) {
-      if (!mbar_wait(&mma_bar[(nk - 1) % nst], (uint32_t)((nk - 1) / nst) & 1u)) abort_sh = 1;
-    }
-    if (abort_sh) {
-      *a.err = 1;
-      for (int kb = 0; kb < issued_upto; ++kb) mbar_wait(&full_bar[kb % nst], (uint32_t)(kb / nst) & 1u);
-    }
-  }
-  __syncthreads();
-  tc_fence_after();
-  if (!abort_sh) {
-    const int i = samp0 + tid;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const bool ok = nk > 0 && role_wait(&acc_bar, 0u, &abort_sh);
+    tc_fence_after();
+    const int quarter = warp & 3, chalf = (warp - kDecodeWarp0) >> 2;
+    const int i = samp0 + quarter * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
     float v[8];
-    for (int c0 = 0; c0 < LP; c0 += 8) {
-      if (nk > 0) {
-        tmem_ld8(lane_base + c0, v);
-      } else {
-        for (int t = 0; t < 8; ++t) v[t] = 0.f;
+    if (!abort_sh) {
+      for (int c0 = chalf * (LP / 2); c0 < (chalf + 1) * (LP / 2); c0 += 8) {
+        // smallest units first, so the FP32 sum rounds as little as possible
+        float sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (ok) {
+          for (int part = bparts - 1; part >= 0; --part) {
+            for (int s = S - 1; s >= 0; --s) {
+              const int r = part * S + s;
+              tmem_ld8(lane_base + r * LP + c0, v);
+#pragma unroll
+              for (int t = 0; t < 8; ++t) sum[t] = fmaf(unit[r * LP + c0 + t], v[t], sum[t]);
+            }
+          }
+        }
+        float* dst = a.hpart + ((size_t)blockIdx.y * a.npad + i) * LP + c0;
+        *reinterpret_cast<float4*>(dst) = make_float4(sum[0], sum[1], sum[2], sum[3]);
+        *reinterpret_cast<float4*>(dst + 4) = make_float4(sum[4], sum[5], sum[6], sum[7]);
       }
-      float* dst = a.hpart + ((size_t)blockIdx.y * a.npad + i) * LP + c0;
-      *reinterpret_cast<float4*>(dst) = make_float4(v[0], v[1], v[2], v[3]);
-      *reinterpret_cast<float4*>(dst + 4) = make_float4(v[4], v[5], v[6], v[7]);
     }
   }
   tc_fence_before();
   __syncthreads();
+  if (tid == 0 && abort_sh) *a.err = 1;
   if (warp == 0) tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
 }
 
@@ -509,52 +569,67 @@ __global__ void __launch_bounds__(kThreads, 1)
 // FP64 epilogues and operand preparation
 // ---------------------------------------------------------------------------
 
-// W slices (BF16, S*LP rows x npad, K-major) of Omega (npad x LP FP64) and the
-// column sums of the sliced matrix over the real samples.  One thread per
-// (sample, column); column sums by a second kernel.
+// Per-column exponent E_l with max_r |A_rl| < 2^E_l over rows [0, rows) of a
+// row-major FP64 matrix (ld LP); one block per column.
+__global__ void k_col_exponent(const double* __restrict__ A, int64_t rows, int LP, int* __restrict__ E) {
+  const int l = blockIdx.x;
+  double m = 0.0;
+  for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) m = fmax(m, fabs(A[r * LP + l]));
+  __shared__ double red[256];
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    int e = 0;
+    if (red[0] > 0.0) frexp(red[0], &e);  // red = m * 2^e, 0.5 <= m < 1, so |A| < 2^e
+    E[l] = e;
+  }
+}
+
+// Error-free split of v into S integer slices with units 2^(E-7-8s):
+// w_s = rint(r / u_s), r -= w_s u_s.  Returns the represented value.
+__device__ __forceinline__ double split_store(double v, int E, int S, __nv_bfloat16* dst, size_t slice_stride) {
+  double r = v, rep = 0.0;
+  for (int s = 0; s < S; ++s) {
+    const double u = ldexp(1.0, E - 7 - 8 * s);
+    const double w = rint(r / u);
+    dst[(size_t)s * slice_stride] = __double2bfloat16(w);  // |w| <= 128: exact
+    r -= w * u;
+    rep += w * u;
+  }
+  return rep;
+}
+
+// W slices of Omega (S*LP rows x npad, K-major), their units, and the column
+// sums of the represented W over the real samples.
 __global__ void k_omega_slices(const double* __restrict__ omg, int npad, int N, int LP, int S,
-                               __nv_bfloat16* __restrict__ w) {
+                               const int* __restrict__ E, __nv_bfloat16* __restrict__ w, double* __restrict__ rep) {
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (idx >= (int64_t)npad * LP) return;
   const int i = (int)(idx / LP), l = (int)(idx % LP);
-  double r = i < N ? omg[idx] : 0.0;
-  for (int s = 0; s < S; ++s) {
-    const __nv_bfloat16 h = __double2bfloat16(r);
-    w[((size_t)s * LP + l) * npad + i] = h;
-    r -= (double)__bfloat162float(h);
-  }
+  const double v = i < N ? omg[idx] : 0.0;
+  rep[idx] = split_store(v, E[l], S, w + (size_t)l * npad + i, (size_t)LP * npad);
 }
 
-__global__ void k_omega_colsum(const __nv_bfloat16* __restrict__ w, int npad, int N, int LP, int S,
-                               double* __restrict__ colsum) {
-  const int l = blockIdx.x;
-  double acc = 0.0;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    double v = 0.0;
-    for (int s = 0; s < S; ++s) v += (double)__bfloat162float(w[((size_t)s * LP + l) * npad + i]);
-    acc += v;
-  }
-  __shared__ double red[256];
-  red[threadIdx.x] = acc;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) colsum[l] = red[0];
+__global__ void k_units(const int* __restrict__ E, int LP, int S, int eoff, double* __restrict__ unit) {
+  const int idx = threadIdx.x + blockIdx.x * blockDim.x;
+  if (idx >= S * LP) return;
+  const int s = idx / LP, l = idx % LP;
+  unit[idx] = ldexp(1.0, E[l] + eoff - 7 - 8 * s);
 }
 
-// G rows: FP64 epilogue of the chunk partials plus the EM sparse term; B
-// operand slices of Gh = 1/2 s G and Gm = 2 f Gh for the H product (columns
-// nsnp .. ld-1 zeroed).
+// G rows: FP64 epilogue of the chunk partials plus the EM sparse term, and
+// Gh = 1/2 s G (FP64) for the H operand.
 __global__ void k_tc_g_finish(GFinishArgs a) {
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t total = (int64_t)a.ldg * a.LP;
-  if (idx >= total) return;
+  if (idx >= (int64_t)a.nsnp * a.LP) return;
   const int j = (int)(idx / a.LP), l = (int)(idx % a.LP);
-  const int S = a.nslice, LP = a.LP;
-  double gm = 0.0;
-  if (j < a.nsnp && l < a.L) {
+  const int LP = a.LP;
+  double gh = 0.0;
+  if (l < a.L) {
     const int64_t pos = a.pos0 + j;
     const int64_t snp = a.perm ? (int64_t)a.perm[pos] : pos;
     const double f = a.F[snp], s = a.scale[snp];
@@ -571,29 +646,34 @@ __global__ void k_tc_g_finish(GFinishArgs a) {
       g += s * sacc;
     }
     a.G[pos * LP + l] = g;
-    // Gh slices; Gm from the sliced Gh so that the centring stays consistent
-    double r = 0.5 * s * g, ghq = 0.0;
-    for (int t = 0; t < S; ++t) {
-      const __nv_bfloat16 h = __double2bfloat16(r);
-      a.gt[((size_t)t * LP + l) * a.ldg + j] = h;
-      const double hv = (double)__bfloat162float(h);
-      ghq += hv;
-      r -= hv;
-    }
-    gm = 2.0 * f * ghq;
-    if (a.mask) {
-      double rm = gm;
-      for (int t = 0; t < S; ++t) {
-        const __nv_bfloat16 h = __double2bfloat16(rm);
-        a.gt[((size_t)(S + t) * LP + l) * a.ldg + j] = h;
-        rm -= (double)__bfloat162float(h);
-      }
-    }
-    a.cpart[(size_t)j * LP + l] = gm;  // c_l = sum_j 2 f_j Gh_j
+    gh = 0.5 * s * g;
+  }
+  a.gh[idx] = gh;
+}
+
+// Gh and Gm = 2 f Gh slices (columns nsnp .. ldg-1 zeroed) with per-column
+// exponents Eh (Gm uses Eh + 1 since |Gm| <= 2 |Gh|), and the terms of
+// c = sum_j Gm_j, all from the represented (sliced) Gh.
+__global__ void k_tc_gh_slices(GFinishArgs a, const int* __restrict__ Eh) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)a.ldg * a.LP) return;
+  const int j = (int)(idx / a.LP), l = (int)(idx % a.LP);
+  const int S = a.nslice, LP = a.LP;
+  const size_t sstride = (size_t)LP * a.ldg;
+  __nv_bfloat16* dh = a.gt + (size_t)l * a.ldg + j;
+  __nv_bfloat16* dm = a.gt + (size_t)S * LP * a.ldg + (size_t)l * a.ldg + j;
+  if (j < a.nsnp && l < a.L) {
+    const int64_t pos = a.pos0 + j;
+    const int64_t snp = a.perm ? (int64_t)a.perm[pos] : pos;
+    const double f = a.F[snp];
+    const double ghq = split_store(a.gh[(size_t)j * LP + l], Eh[l], S, dh, sstride);
+    const double gm = 2.0 * f * ghq;
+    if (a.mask) split_store(gm, Eh[l] + 1, S, dm, sstride);
+    a.cpart[(size_t)j * LP + l] = gm;
   } else {
-    for (int t = 0; t < S; ++t) a.gt[((size_t)t * LP + l) * a.ldg + j] = __float2bfloat16(0.f);
+    for (int s = 0; s < S; ++s) dh[s * sstride] = __float2bfloat16(0.f);
     if (a.mask)
-      for (int t = 0; t < S; ++t) a.gt[((size_t)(S + t) * LP + l) * a.ldg + j] = __float2bfloat16(0.f);
+      for (int s = 0; s < S; ++s) dm[s * sstride] = __float2bfloat16(0.f);
     if (j < a.nsnp) a.cpart[(size_t)j * LP + l] = 0.0;
   }
 }
@@ -663,10 +743,20 @@ void make_map_2d(CUtensorMap* map, const void* base, bool bf16, uint64_t inner, 
   if (r != CUDA_SUCCESS) throw Error(-2, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-int stages_for(int LP, int nslice, int bparts, bool mask, int pbytes) {
+int stages_for(int LP, int nslice, int bparts, int acc_parts, bool mask, int pbytes) {
   const SmemLayout l = layout_for(LP, nslice, bparts, mask, pbytes);
-  const int budget = 200 * 1024;
-  return std::max(1, std::min(kMaxStages, budget / (int)l.stage_bytes));
+  const int budget = 212 * 1024;  // dynamic shared memory (static use is under 12 KB)
+  const int by_smem = budget / (int)l.stage_bytes;
+  // TMEM: accumulators (acc_parts x slices x LP columns) + per-stage A operands
+  // within the 512 columns of an SM
+  const int acc = acc_parts * nslice * LP;
+  const int a_stride = mask ? 64 : 32;
+  const int by_tmem = (512 - acc) / a_stride;
+  return std::max(1, std::min(kMaxStages, std::min(by_smem, by_tmem)));
+}
+
+int tmem_cols_needed(int LP, int nslice, int bparts, bool mask, int nstages) {
+  return bparts * nslice * LP + nstages * (mask ? 64 : 32);
 }
 
 size_t smem_bytes(int LP, int nslice, int bparts, bool mask, int pbytes, int nstages) {
@@ -680,9 +770,11 @@ int tmem_cols_for(int ncols) {
 }
 
 void launch_g(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs& a, cudaStream_t s) {
+  if (a.tmem_cols > 512 || a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.mask ? 2 : 1, a.mask != 0, a.nstages))
+    throw Error(-6, "tensor-core G product: TMEM plan exceeds 512 columns");
   static bool attr = false;
   if (!attr) {
-    PCAONE_CUDA(cudaFuncSetAttribute(k_tc_g, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
+    PCAONE_CUDA(cudaFuncSetAttribute(k_tc_g, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
     attr = true;
   }
   const size_t smem = smem_bytes(a.LP, a.nslice, 1, a.mask != 0, 128 * 16, a.nstages);
@@ -692,9 +784,11 @@ void launch_g(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs&
 }
 
 void launch_h(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs& a, cudaStream_t s) {
+  if (a.tmem_cols > 512 || a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.mask ? 2 : 1, a.mask != 0, a.nstages))
+    throw Error(-6, "tensor-core H product: TMEM plan exceeds 512 columns");
   static bool attr = false;
   if (!attr) {
-    PCAONE_CUDA(cudaFuncSetAttribute(k_tc_h, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
+    PCAONE_CUDA(cudaFuncSetAttribute(k_tc_h, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
     attr = true;
   }
   const size_t smem = smem_bytes(a.LP, a.nslice, a.mask ? 2 : 1, a.mask != 0, 64 * 32, a.nstages);
@@ -703,19 +797,32 @@ void launch_h(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs&
   PCAONE_LAUNCH_CHECK();
 }
 
-void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv_bfloat16* w, double* colsum,
-                         cudaStream_t s) {
+void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv_bfloat16* w, double* wunit,
+                         double* colsum, int* E, double* rep, cudaStream_t s) {
   const int64_t n = (int64_t)npad * LP;
-  k_omega_slices<<<ceil_div(n, 256), 256, 0, s>>>(omg, npad, N, LP, S, w);
+  k_col_exponent<<<LP, 256, 0, s>>>(omg, N, LP, E);
   PCAONE_LAUNCH_CHECK();
-  k_omega_colsum<<<LP, 256, 0, s>>>(w, npad, N, LP, S, colsum);
+  k_omega_slices<<<ceil_div(n, 256), 256, 0, s>>>(omg, npad, N, LP, S, E, w, rep);
+  PCAONE_LAUNCH_CHECK();
+  k_units<<<ceil_div(S * LP, 128), 128, 0, s>>>(E, LP, S, 0, wunit);
+  PCAONE_LAUNCH_CHECK();
+  k_colreduce<<<LP, 256, 0, s>>>(rep, N, LP, colsum);
   PCAONE_LAUNCH_CHECK();
 }
 
-void launch_g_finish(const GFinishArgs& a, double* c_out, cudaStream_t s) {
-  const int64_t n = (int64_t)a.ldg * a.LP;
-  k_tc_g_finish<<<ceil_div(n, 256), 256, 0, s>>>(a);
+void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* c_out, cudaStream_t s) {
+  k_tc_g_finish<<<ceil_div((int64_t)a.nsnp * a.LP, 256), 256, 0, s>>>(a);
   PCAONE_LAUNCH_CHECK();
+  k_col_exponent<<<a.LP, 256, 0, s>>>(a.gh, a.nsnp, a.LP, Eh);
+  PCAONE_LAUNCH_CHECK();
+  k_tc_gh_slices<<<ceil_div((int64_t)a.ldg * a.LP, 256), 256, 0, s>>>(a, Eh);
+  PCAONE_LAUNCH_CHECK();
+  k_units<<<ceil_div(a.nslice * a.LP, 128), 128, 0, s>>>(Eh, a.LP, a.nslice, 0, hunit);
+  PCAONE_LAUNCH_CHECK();
+  if (a.mask) {
+    k_units<<<ceil_div(a.nslice * a.LP, 128), 128, 0, s>>>(Eh, a.LP, a.nslice, 1, hunit + a.nslice * a.LP);
+    PCAONE_LAUNCH_CHECK();
+  }
   k_colreduce<<<a.LP, 256, 0, s>>>(a.cpart, a.nsnp, a.LP, c_out);
   PCAONE_LAUNCH_CHECK();
 }
