@@ -159,6 +159,24 @@ int pcaone_gpu_get_perm(pcaone_gpu_ctx* ctx, int32_t* perm);
  * when standardize != 0), x and y of length N. */
 int pcaone_gpu_matvec(pcaone_gpu_ctx* ctx, const double* x, double* y, int standardize);
 
+/* ---- matvec without device allocation (no counterpart in the reference) --
+ * y = X X^T x like pcaone_gpu_matvec, for callers that cannot call cudaMalloc
+ * (code recorded into a CUDA graph, hosts whose memory manager owns all device
+ * memory, loops that cannot afford an allocation's synchronisation).  All
+ * pointers are device pointers the caller owns: d_packed holds nsnps rows of
+ * row_pitch bytes (the .bed body, row_pitch >= (nsamples+3)/4), d_F the allele
+ * frequencies (pcaone_gpu_counts), d_x and d_y nsamples doubles; the work is
+ * queued on `stream` (a cudaStream_t, NULL for the default stream) and is
+ * complete when that stream is.  The intermediate X^T x lives in a static
+ * device array of 2^21 doubles (16 MiB, held by every GPU that loads the
+ * library until the process exits), so nsnps is limited to 2,097,152:
+ * larger inputs return PCAONE_E_LIMIT.  The first call on a device resolves
+ * the array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  Calls share the array: calls whose work overlaps
+ * on the GPU race and must be serialised by the caller. */
+int pcaone_gpu_matvec_static(const uint8_t* d_packed, uint64_t row_pitch, uint64_t nsnps, uint32_t nsamples,
+                             const double* d_F, int standardize, const double* d_x, double* d_y, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

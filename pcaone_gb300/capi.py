@@ -30,6 +30,7 @@ EXPORTS = [
     "pcaone_gpu_set_flags", "pcaone_gpu_compute_g_and_h", "pcaone_gpu_compute_usv", "pcaone_gpu_run_halko",
     "pcaone_gpu_get_perm", "pcaone_gpu_matvec", "pcaone_gpu_load_synthetic", "pcaone_gpu_get_bed",
     "pcaone_gpu_set_profiling", "pcaone_gpu_kernel_stats", "pcaone_gpu_launch_count",
+    "pcaone_gpu_matvec_static",
 ]
 
 
@@ -88,6 +89,8 @@ def load(path: str = LIBPATH) -> ctypes.CDLL:
     lib.pcaone_gpu_set_profiling.argtypes = [c_void_p, c_int]
     lib.pcaone_gpu_kernel_stats.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p]
     lib.pcaone_gpu_launch_count.argtypes = []
+    lib.pcaone_gpu_matvec_static.argtypes = [c_void_p, c_uint64, c_uint64, c_uint32, c_void_p, c_int, c_void_p,
+                                             c_void_p, c_void_p]
     for name in EXPORTS:
         if name not in ("pcaone_gpu_default_params", "pcaone_gpu_last_error"):
             getattr(lib, name).restype = c_int
