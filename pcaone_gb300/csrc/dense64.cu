@@ -1,7 +1,14 @@
-// FP64 dense kernels of the RSVD driver: tall-skinny Gram / cross products,
+// Dense kernels of the RSVD driver: tall-skinny Gram / cross products,
 // Cholesky and triangular inverse of (k+p)^2 matrices, tall x small products,
 // the Householder sign rule, flipOmg, the Jacobi eigensolver for the small
 // SVD of B, mev, the EM fill and the Arnoldi matvec.
+//
+// All matrices are stored in FP64.  FP64 arithmetic runs at a small fraction
+// of the FP32 rate on this GPU, so the two O(rows * L^2) kernels (the Gram /
+// cross product and the tall x small product) compute in FP32 pairs
+// (double-float: error-free TwoProduct / TwoSum, about 44 significand bits),
+// which is far below the 24-bit integer slices the window products use; the
+// small L x L kernels stay in FP64.
 //
 // Tall matrices (N x L, M x L) are row-major with leading dimension LP (the
 // sketch width padded to a multiple of 8; padding columns are zero).  Small
@@ -18,14 +25,18 @@ constexpr int kRowsTile = 32;
 
 // part[b] = A[rows of block b]^T B[rows of block b] (na x nb entries, row-major
 // na x nb).  sym: A == B and only the upper triangle is formed (mirrored by the
-// reduction).  FP64 products and sums.
+// reduction).  Row tiles are staged in shared memory as float pairs; each
+// thread accumulates Q entries in FP32 pairs.
+template <int Q>
 __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict__ A, int lda, int na,
                                                        const double* __restrict__ B, int ldb, int nb, int64_t rows,
                                                        int64_t rows_per_block, int sym, double* __restrict__ part) {
-  extern __shared__ double sm[];
-  double* As = sm;                       // kRowsTile x na
-  double* Bs = sm + kRowsTile * na;      // kRowsTile x nb
-  uint16_t* pi = reinterpret_cast<uint16_t*>(Bs + kRowsTile * nb);
+  extern __shared__ float smf[];
+  float* Ah = smf;                       // kRowsTile x na
+  float* Al = Ah + kRowsTile * na;
+  float* Bh = Al + kRowsTile * na;       // kRowsTile x nb (not used when sym)
+  float* Bl = Bh + kRowsTile * nb;
+  uint16_t* pi = reinterpret_cast<uint16_t*>(Bl + kRowsTile * nb);
   uint16_t* pj = pi + na * nb;
   const int tid = threadIdx.x;
   int nent = 0;
@@ -47,31 +58,32 @@ __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict_
   }
   const int64_t r0 = blockIdx.x * rows_per_block;
   const int64_t r1 = min(r0 + rows_per_block, rows);
-  double acc[64];
-#pragma unroll
-  for (int q = 0; q < 64; ++q) acc[q] = 0.0;
+  FloatPair acc[Q];
   __syncthreads();
   for (int64_t rt = r0; rt < r1; rt += kRowsTile) {
     const int nr = (int)min((int64_t)kRowsTile, r1 - rt);
     for (int e = tid; e < kRowsTile * na; e += blockDim.x) {
       const int r = e / na, c = e % na;
-      As[e] = r < nr ? A[(rt + r) * lda + c] : 0.0;
+      fp_split(r < nr ? A[(rt + r) * lda + c] : 0.0, Ah[e], Al[e]);
     }
     if (!sym)
       for (int e = tid; e < kRowsTile * nb; e += blockDim.x) {
         const int r = e / nb, c = e % nb;
-        Bs[e] = r < nr ? B[(rt + r) * ldb + c] : 0.0;
+        fp_split(r < nr ? B[(rt + r) * ldb + c] : 0.0, Bh[e], Bl[e]);
       }
     __syncthreads();
-    const double* Bt = sym ? As : Bs;
+    const float* Th = sym ? Ah : Bh;
+    const float* Tl = sym ? Al : Bl;
     const int ldt = sym ? na : nb;
 #pragma unroll
-    for (int q = 0; q < 64; ++q) {
+    for (int q = 0; q < Q; ++q) {
       const int e = tid + q * 256;
       if (e < nent) {
         const int i = pi[e], j = pj[e];
-        double s = acc[q];
-        for (int r = 0; r < kRowsTile; ++r) s = fma(As[r * na + i], Bt[r * ldt + j], s);
+        FloatPair s = acc[q];
+#pragma unroll 8
+        for (int r = 0; r < kRowsTile; ++r)
+          fp_add_prod2(s, Ah[r * na + i], Al[r * na + i], Th[r * ldt + j], Tl[r * ldt + j]);
         acc[q] = s;
       }
     }
@@ -79,9 +91,9 @@ __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict_
   }
   double* out = part + (size_t)blockIdx.x * na * nb;
 #pragma unroll
-  for (int q = 0; q < 64; ++q) {
+  for (int q = 0; q < Q; ++q) {
     const int e = tid + q * 256;
-    if (e < nent) out[pi[e] * nb + pj[e]] = acc[q];
+    if (e < nent) out[pi[e] * nb + pj[e]] = fp_value(acc[q]);
   }
 }
 
@@ -166,31 +178,34 @@ __global__ void k_chol_inv(const double* __restrict__ W, int L, int LP, double s
 }
 
 // C[rows x n] = A[rows x LP] * B[LP x n]; B and a 32-row tile of A in shared
-// memory; thread (row r, column group cg) forms columns cg, cg+8, ...
-// C may alias A (ldc == LP, n <= LP): each CTA reads a row tile into shared
-// memory before it writes the same rows.
+// memory as float pairs; thread (row r, column group cg) forms columns cg,
+// cg+8, ... in FP32 pairs.  C may alias A (ldc == LP, n <= LP): each CTA reads
+// a row tile into shared memory before it writes the same rows.
 __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows, int LP,
                                                    const double* __restrict__ B, int ldb, int n, double* C,
                                                    int ldc) {
-  extern __shared__ double sm[];
-  double* Bs = sm;              // LP x n
-  double* As = sm + LP * n;     // 32 x LP
+  extern __shared__ float smf[];
+  float* Bh = smf;              // LP x n
+  float* Bl = Bh + LP * n;
+  float* Ah = Bl + LP * n;      // 32 x LP
+  float* Al = Ah + kRowsTile * LP;
   const int tid = threadIdx.x;
-  for (int e = tid; e < LP * n; e += blockDim.x) Bs[e] = B[(e / n) * ldb + (e % n)];
+  for (int e = tid; e < LP * n; e += blockDim.x) fp_split(B[(e / n) * ldb + (e % n)], Bh[e], Bl[e]);
   const int r = tid >> 3, cg = tid & 7;
   for (int64_t rt = (int64_t)blockIdx.x * kRowsTile; rt < rows; rt += (int64_t)gridDim.x * kRowsTile) {
     __syncthreads();
     for (int e = tid; e < kRowsTile * LP; e += blockDim.x) {
       const int64_t row = rt + e / LP;
-      As[e] = row < rows ? A[row * LP + (e % LP)] : 0.0;
+      fp_split(row < rows ? A[row * LP + (e % LP)] : 0.0, Ah[e], Al[e]);
     }
     __syncthreads();
     const int64_t row = rt + r;
     if (row < rows) {
       for (int c = cg; c < n; c += 8) {
-        double s = 0.0;
-        for (int t = 0; t < LP; ++t) s = fma(As[r * LP + t], Bs[t * n + c], s);
-        C[row * ldc + c] = s;
+        FloatPair s;
+#pragma unroll 8
+        for (int t = 0; t < LP; ++t) fp_add_prod2(s, Ah[r * LP + t], Al[r * LP + t], Bh[t * n + c], Bl[t * n + c]);
+        C[row * ldc + c] = fp_value(s);
       }
     }
   }
@@ -540,7 +555,18 @@ int cross_blocks(int64_t rows) { return (int)std::max<int64_t>(1, std::min<int64
 
 size_t cross_smem(int na, int nb, int sym) {
   (void)sym;
-  return sizeof(double) * kRowsTile * (na + nb) + 2 * sizeof(uint16_t) * na * nb + 64;
+  return 2 * sizeof(float) * kRowsTile * (na + nb) + 2 * sizeof(uint16_t) * na * nb + 64;
+}
+
+template <int Q>
+void launch_cross_q(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int64_t per,
+                    int sym, double* part, int nblocks, size_t smem, cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    PCAONE_CUDA(cudaFuncSetAttribute(k_cross_partial<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set = true;
+  }
+  k_cross_partial<Q><<<nblocks, 256, smem, s>>>(A, lda, na, B, ldb, nb, rows, per, sym, part);
 }
 
 void launch_cross(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int sym,
@@ -554,12 +580,20 @@ void launch_cross(const double* A, int lda, int na, const double* B, int ldb, in
   const int64_t per = round_up64((rows + nblocks - 1) / nblocks, kRowsTile);
   nblocks = (int)((rows + per - 1) / per);
   const size_t smem = cross_smem(na, nb, sym);
-  static bool attr_set = false;
-  if (!attr_set) {
-    PCAONE_CUDA(cudaFuncSetAttribute(k_cross_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr_set = true;
-  }
-  k_cross_partial<<<nblocks, 256, smem, s>>>(A, lda, na, sym ? A : B, sym ? lda : ldb, nb, rows, per, sym, part);
+  const int nent = sym ? na * (na + 1) / 2 : na * nb;
+  const int q = (nent + 255) / 256;
+  const double* Bv = sym ? A : B;
+  const int ldbv = sym ? lda : ldb;
+  if (q <= 4)
+    launch_cross_q<4>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, s);
+  else if (q <= 8)
+    launch_cross_q<8>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, s);
+  else if (q <= 16)
+    launch_cross_q<16>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, s);
+  else if (q <= 32)
+    launch_cross_q<32>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, s);
+  else
+    launch_cross_q<64>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, s);
   PCAONE_LAUNCH_CHECK();
   k_cross_reduce<<<ceil_div((int64_t)na * nb, 256), 256, 0, s>>>(part, nblocks, na, nb, sym, W, ldw);
   PCAONE_LAUNCH_CHECK();
@@ -584,7 +618,7 @@ void launch_gemm_tall(const double* A, int64_t rows, int LP, const double* B, in
     PCAONE_CUDA(cudaFuncSetAttribute(k_gemm_tall, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_set = true;
   }
-  const size_t smem = sizeof(double) * ((size_t)LP * n + (size_t)kRowsTile * LP);
+  const size_t smem = 2 * sizeof(float) * ((size_t)LP * n + (size_t)kRowsTile * LP);
   const int grid = (int)std::min<int64_t>((rows + kRowsTile - 1) / kRowsTile, 152 * 8);
   k_gemm_tall<<<grid, 256, smem, s>>>(A, rows, LP, B, ldb, n, C, ldc);
   PCAONE_LAUNCH_CHECK();

@@ -79,9 +79,20 @@ struct Context {
   // missing entries in working order (EM)
   int64_t nnz = -1;
   DBuf<int64_t> miss_rowptr;
+  std::vector<int64_t> miss_rowptr_host;
   DBuf<int32_t> miss_pos, miss_sample;
   DBuf<double> miss_value;
   bool miss_valid = false;
+  // the same entries grouped by (window, sample): bucket w*N + i lists, in
+  // position order, the positions of window w (bk_wsize positions each) where
+  // sample i is missing; bk_value holds their EM fill values
+  int64_t bk_wsize = 0;
+  int bk_nwin = 0;
+  bool bk_valid = false;
+  DBuf<int64_t> bk_ptr;
+  std::vector<int64_t> bk_ptr_host;
+  DBuf<int32_t> bk_cnt, bk_pos, bk_sample;
+  DBuf<double> bk_value;
 
   // ---- operator (RsvdOpData) ----
   bool have_op = false;
@@ -115,10 +126,13 @@ struct Context {
   bool tc = false;
   DBuf<uint8_t> bedp;                 // packed rows in working order (shuffled window method)
   const uint8_t* bed_work = nullptr;  // packed rows the tensor-core kernels read
-  DBuf<__nv_bfloat16> wsl, gt;        // W slices (3*LP x npad), Gh/Gm slices (6*LP x ldg)
+  DBuf<__nv_bfloat16> wsl, gt;        // W slices (3*LP x npad), Gh slices (3*LP x ldg)
   DBuf<double> colsum, cpart, cvec, wunit, hunit, ghbuf, wrep;
+  DBuf<int32_t> wint, ghint, gmint;   // represented W, Gh and Gm = 2 f Gh as integers (times a column unit)
+  DBuf<double> gmunit;                // units of the Gm integers (last of S rows)
+  // int64 sums of the missing-entry terms (k_seg_gather), cleared by the finish kernels
+  DBuf<unsigned long long> gisum, gesum, hisum, hesum;
   DBuf<int> wexp, hexp;
-  DBuf<float> part_m;
   DBuf<int> err;
   CUtensorMap map_bed_g{}, map_bed_h{}, map_w{}, map_gt{};
   int ldg = 0, win_max = 0;
@@ -180,6 +194,7 @@ static void load_common(Context& c, uint64_t nsnps, uint32_t nsamples) {
   c.have_op = false;
   c.omega_user.clear();
   c.miss_valid = false;
+  c.bk_valid = false;
   c.nnz = -1;
   c.counts_host.clear();
 }
@@ -295,24 +310,31 @@ static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
     need_hpart = std::max(need_hpart, (size_t)nsp * c.npad * LP);
   }
   c.wsl.ensure((size_t)3 * LP * c.npad, c.stream);
-  c.gt.ensure((size_t)6 * LP * c.ldg, c.stream);
+  c.gt.ensure((size_t)3 * LP * c.ldg, c.stream);
   c.colsum.ensure(LP, c.stream);
   c.cvec.ensure(LP, c.stream);
   c.cpart.ensure((size_t)win * LP, c.stream, false);
   c.ghbuf.ensure((size_t)win * LP, c.stream, false);
   c.wrep.ensure((size_t)c.npad * LP, c.stream, false);
+  c.wint.ensure((size_t)c.npad * LP, c.stream, false);
+  c.ghint.ensure((size_t)win * LP, c.stream, false);
+  c.gmint.ensure((size_t)win * LP, c.stream, false);
+  c.gmunit.ensure((size_t)3 * LP, c.stream);
+  c.gisum.ensure((size_t)win * LP, c.stream, true);
+  c.gesum.ensure((size_t)win * LP, c.stream, true);
+  c.hisum.ensure((size_t)c.npad * LP, c.stream, true);
+  c.hesum.ensure((size_t)c.npad * LP, c.stream, true);
   c.wunit.ensure((size_t)3 * LP, c.stream);
-  c.hunit.ensure((size_t)6 * LP, c.stream);
+  c.hunit.ensure((size_t)3 * LP, c.stream);
   c.wexp.ensure(LP, c.stream);
   c.hexp.ensure(LP, c.stream);
   c.err.ensure(1, c.stream);
   c.part.ensure(std::max(need_part, c.part.n), c.stream, false);
-  c.part_m.ensure(need_part, c.stream, false);
   c.hpart.ensure(std::max(need_hpart, c.hpart.n), c.stream, false);
   c.bed_work = c.bed.p;
   tc_make_bed_maps(c);
   tc::make_map_2d(&c.map_w, c.wsl.p, true, (uint64_t)c.npad, (uint64_t)3 * LP, (uint64_t)c.npad * 2, 64, LP, true);
-  tc::make_map_2d(&c.map_gt, c.gt.p, true, (uint64_t)c.ldg, (uint64_t)6 * LP, (uint64_t)c.ldg * 2, 64, LP, true);
+  tc::make_map_2d(&c.map_gt, c.gt.p, true, (uint64_t)c.ldg, (uint64_t)3 * LP, (uint64_t)c.ldg * 2, 64, LP, true);
   c.w_slices = 0;
 }
 
@@ -385,16 +407,12 @@ static void op_init(Context& c, const pcaone_gpu_params& p) {
   c.part.ensure(need_part, c.stream, false);
   c.hpart.ensure(need_hpart, c.stream, false);
   c.g32.ensure((size_t)std::max<int64_t>(1, win) * c.LP, c.stream, false);
+  c.bk_valid = false;  // the window size may have changed
   if (c.tc) {
     ensure_missing_total(c);
-    // one TMEM accumulator per slice (and per mask part): 3 slices of LP columns
-    // each, doubled when missing genotypes need the mask product, within 512
-    // TMEM per CTA: one accumulator per slice (three slices of LP columns,
-    // doubled for the mask product) plus at least one stage of A operands
-    const bool any_miss = c.counts_total_missing > 0;
-    if ((any_miss ? 2 : 1) * 3 * c.LP + (any_miss ? 64 : 32) > 512)
-      throw Error(PCAONE_E_LIMIT, "tensor-core form: k + oversamples too large for TMEM "
-                                  "(at most 64 with missing genotypes, 144 without)");
+    // TMEM per CTA: one accumulator per slice (3 x LP columns) plus at least
+    // one 32-column stage of the A operand (LP <= 112 always fits)
+    if (3 * c.LP + 32 > 512) throw Error(PCAONE_E_LIMIT, "tensor-core form: k + oversamples too large for TMEM");
     tc_setup(c, (int)std::max<int64_t>(1, win), lens);
   }
   upload_omega0(c);
@@ -506,6 +524,7 @@ static void build_missing(Context& c) {
     rowptr[p + 1] = rowptr[p] + c.counts_host[(size_t)snp * 4 + 1];
   }
   c.nnz = rowptr[c.M];
+  if (c.nnz > 0x7fffffffLL) throw Error(PCAONE_E_LIMIT, "more than 2^31-1 missing genotypes");
   c.miss_rowptr.ensure(rowptr.size(), c.stream, false);
   PCAONE_CUDA(cudaMemcpyAsync(c.miss_rowptr.p, rowptr.data(), rowptr.size() * sizeof(int64_t),
                               cudaMemcpyHostToDevice, c.stream));
@@ -515,6 +534,7 @@ static void build_missing(Context& c) {
   launch_missing_list(c.view(), c.permuted ? c.perm.p : nullptr, c.miss_rowptr.p, c.miss_pos.p, c.miss_sample.p,
                       c.stream);
   PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  c.miss_rowptr_host.swap(rowptr);
   c.miss_valid = true;
 }
 
@@ -528,6 +548,63 @@ static void fit_with_pi(Context& c) {
   c.fitted = true;
   PCAONE_CUDA(cudaStreamSynchronize(c.stream));
   c.t_em += secs(t0, clk::now());
+}
+
+// positions per SNP window of the current operator: the winSVD band blocks
+// (src/Halko.cpp:169-172) or the in-core sSVD blocks of at most 16384 SNPs
+static int64_t window_size(const Context& c) {
+  if (c.P.svd == PCAONE_SVD_WINDOW) return (c.M + c.P.bands - 1) / c.P.bands;
+  const int64_t nwin = (c.M + 16383) / 16384;
+  return (c.M + nwin - 1) / nwin;
+}
+
+// missing entries grouped by (window, sample), in working order: a count pass
+// over the packed rows, an exclusive scan, and a fill pass
+static void ensure_buckets(Context& c) {
+  const int64_t ws = window_size(c);
+  if (c.bk_valid && c.bk_wsize == ws) return;
+  const int64_t nwin = (c.M + ws - 1) / ws;
+  if (nwin > 65535) throw Error(PCAONE_E_LIMIT, "too many SNP windows for the missing-entry index");
+  const size_t nb = (size_t)nwin * c.N;
+  const int32_t* perm = c.permuted ? c.perm.p : nullptr;
+  c.bk_cnt.ensure(nb, c.stream, false);
+  launch_bucket_count(c.view(), perm, ws, (int)nwin, c.bk_cnt.p, c.stream);
+  std::vector<int32_t> cnt(nb);
+  PCAONE_CUDA(cudaMemcpyAsync(cnt.data(), c.bk_cnt.p, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  std::vector<int64_t> ptr(nb + 1);
+  ptr[0] = 0;
+  for (size_t b = 0; b < nb; ++b) ptr[b + 1] = ptr[b] + cnt[b];
+  const int64_t total = ptr[nb];
+  if (total != (int64_t)c.counts_total_missing)
+    throw Error(PCAONE_E_CUDA, "internal: missing-entry index disagrees with the genotype counts");
+  c.bk_ptr.ensure(nb + 1, c.stream, false);
+  PCAONE_CUDA(cudaMemcpyAsync(c.bk_ptr.p, ptr.data(), (nb + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, c.stream));
+  c.bk_pos.ensure((size_t)std::max<int64_t>(1, total), c.stream, false);
+  c.bk_sample.ensure((size_t)std::max<int64_t>(1, total), c.stream, false);
+  launch_bucket_fill(c.view(), perm, ws, (int)nwin, c.bk_ptr.p, c.bk_pos.p, c.bk_sample.p, c.stream);
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  c.bk_ptr_host.swap(ptr);
+  c.bk_wsize = ws;
+  c.bk_nwin = (int)nwin;
+  c.bk_valid = true;
+}
+
+// the missing-entry structures the window products read (the CSR list by
+// position and its (window, sample) grouping, with the EM fill values once
+// fitted): needed by the tensor-core form whenever a genotype is missing, and
+// by the FP32 form for the EM term
+static void prepare_missing(Context& c) {
+  ensure_missing_total(c);
+  const bool em = c.fitted && c.P.emu;
+  if (c.counts_total_missing <= 0 || !(c.tc || em)) return;
+  build_missing(c);
+  ensure_buckets(c);
+  if (em) {
+    c.bk_value.ensure((size_t)std::max<int64_t>(1, c.nnz), c.stream, false);
+    launch_em_fill(c.bk_pos.p, c.bk_sample.p, c.bk_value.p, c.nnz, c.permuted ? c.perm.p : nullptr, c.F.p, c.U.p,
+                   c.sigma.p, c.V.p, c.k, c.stream);
+  }
 }
 
 static void refresh_lut(Context& c) {
@@ -551,6 +628,7 @@ static void prepare_epoch0(Context& c, bool window) {
       PCAONE_CUDA(cudaStreamSynchronize(c.stream));
       c.permuted = true;
       c.miss_valid = false;
+      c.bk_valid = false;
       if (c.tc) {
         c.bedp.ensure((size_t)c.M * c.stride, c.stream, false);
         tc::launch_gather_rows(c.bed.p, c.bedp.p, c.stride, c.perm.p, c.M, c.stream);
@@ -559,6 +637,7 @@ static void prepare_epoch0(Context& c, bool window) {
       }
     }
   }
+  prepare_missing(c);
 }
 
 // tensor-core form of one window (prod_tc.cu)
@@ -566,18 +645,19 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   const int LP = c.LP, S = c.nslice_cur;
   if (c.w_slices != S) {
     tc::launch_omega_slices(c.Omg.p, c.npad, c.N, LP, S, c.wsl.p, c.wunit.p, c.colsum.p, c.wexp.p, c.wrep.p,
-                            c.stream);
+                            c.wint.p, c.stream);
     c.w_slices = S;
   }
   int chunk, nch, per, nsp;
   tc_shapes((int)n, c.npad, chunk, nch, per, nsp);
   if ((size_t)nch * n * LP > c.part.n || (size_t)nsp * c.npad * LP > c.hpart.n || n > c.win_max)
     throw Error(PCAONE_E_ARG, "internal: tensor-core window scratch too small");
-  const bool mask = true;  // per-CTA skip when its tile holds no missing genotype
-  SparseRows sp{};
-  if (c.fitted && c.P.emu && c.nnz > 0)
-    sp = SparseRows{c.miss_rowptr.p, c.miss_sample.p, c.miss_value.p, c.scale.p, c.permuted ? c.perm.p : nullptr, 1};
   const bool any_miss = c.counts_total_missing > 0;
+  const bool em = c.fitted && c.P.emu && c.nnz > 0;
+  const int32_t* perm = c.permuted ? c.perm.p : nullptr;
+  const int64_t win = any_miss && c.bk_wsize > 0 ? pos0 / c.bk_wsize : 0;
+  if (any_miss && (!c.bk_valid || !c.miss_valid || pos0 != win * c.bk_wsize))
+    throw Error(PCAONE_E_ARG, "internal: missing-entry index does not match the windows");
   const double flops = 2.0 * (double)c.N * (double)n * (double)c.L;
   auto mark = [&](int cls) {
     if (!c.profiling) return;
@@ -598,18 +678,32 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ga.chunk = chunk;
   ga.npad = c.npad;
   ga.nchunks = nch;
-  ga.mask = (mask && any_miss) ? 1 : 0;
-  ga.nstages = tc::stages_for(LP, S, 1, ga.mask ? 2 : 1, ga.mask != 0, 128 * 16);
-  ga.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ga.mask ? 2 : 1, ga.mask != 0, ga.nstages));
+  ga.nstages = tc::stages_for(LP, S, 128 * 16);
+  ga.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ga.nstages));
   ga.wscale = c.wunit.p;
-  ga.counts = c.counts.p;
-  ga.perm = c.permuted ? c.perm.p : nullptr;
-  ga.part_d = c.part.p;
-  ga.part_m = c.part_m.p;
+  ga.part = c.part.p;
   ga.err = c.err.p;
   mark(0);
   tc::launch_g(c.map_bed_g, c.map_w, ga, c.stream);
   close_mark();
+  if (any_miss) {
+    // f sum_i W_i (and sum_i e_i W_i) over each SNP's missing samples
+    SegGatherArgs sg{};
+    sg.e0 = c.miss_rowptr_host[pos0];
+    sg.e1 = c.miss_rowptr_host[pos0 + n];
+    sg.key = c.miss_pos.p;
+    sg.key_base = pos0;
+    sg.src = c.miss_sample.p;
+    sg.src_base = 0;
+    sg.L = c.L;
+    sg.LP = LP;
+    sg.R = c.wint.p;
+    sg.out = c.gisum.p;
+    sg.val = em ? c.miss_value.p : nullptr;
+    sg.R2 = c.wint.p;
+    sg.out2 = c.gesum.p;
+    launch_seg_gather(sg, c.stream);
+  }
   tc::GFinishArgs fa{};
   fa.pos0 = pos0;
   fa.nsnp = (int)n;
@@ -617,46 +711,64 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   fa.LP = LP;
   fa.nslice = S;
   fa.nchunks = nch;
-  fa.mask = ga.mask;
-  fa.ldg = round_up((int)n, 64);
-  fa.part_d = c.part.p;
-  fa.part_m = ga.mask ? c.part_m.p : nullptr;
+  // the B operand tensor map spans ldg columns; windows shorter than the
+  // longest one leave the tail zeroed by the slicing kernel
+  fa.ldg = c.ldg;
+  fa.part = c.part.p;
   fa.colsum = c.colsum.p;
   fa.F = c.F.p;
   fa.scale = c.scale.p;
-  fa.perm = c.permuted ? c.perm.p : nullptr;
-  fa.omg = c.Omg.p;
-  fa.sp = sp;
+  fa.perm = perm;
+  fa.wunit_m = c.wunit.p + (size_t)(S - 1) * LP;
+  fa.gisum = any_miss ? c.gisum.p : nullptr;
+  fa.gesum = (any_miss && em) ? c.gesum.p : nullptr;
   fa.G = c.G.p;
   fa.gh = c.ghbuf.p;
+  fa.ghint = c.ghint.p;
+  fa.gmint = c.gmint.p;
   fa.gt = c.gt.p;
   fa.cpart = c.cpart.p;
-  // the B operand tensor map spans ldg columns; windows shorter than the
-  // longest one leave the tail zeroed by the finish kernel
-  fa.ldg = c.ldg;
-  tc::launch_g_finish(fa, c.hexp.p, c.hunit.p, c.cvec.p, c.stream);
+  tc::launch_g_finish(fa, c.hexp.p, c.hunit.p, c.gmunit.p, c.cvec.p, c.stream);
   tc::HArgs ha{};
   ha.pos0 = pos0;
   ha.nsnp = (int)n;
+  ha.L = c.L;
   ha.LP = LP;
   ha.nslice = S;
   ha.per_split = per;
   ha.nsplit = nsp;
   ha.npad = c.npad;
-  ha.mask = ga.mask;
-  ha.nstages = tc::stages_for(LP, S, ha.mask ? 2 : 1, ha.mask ? 2 : 1, ha.mask != 0, 64 * 32);
-  ha.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ha.mask ? 2 : 1, ha.mask != 0, ha.nstages));
+  ha.nstages = tc::stages_for(LP, S, 64 * 32);
+  ha.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ha.nstages));
   ha.hscale = c.hunit.p;
   ha.hpart = c.hpart.p;
   ha.err = c.err.p;
+  ha.hisum = any_miss ? c.hisum.p : nullptr;
+  ha.gmunit_m = c.gmunit.p + (size_t)(S - 1) * LP;
+  ha.hesum = (any_miss && em) ? c.hesum.p : nullptr;
+  ha.hunit_m = c.hunit.p + (size_t)(S - 1) * LP;
+  if (any_miss) {
+    // sum_j Gm_j (and sum_j 2 e_j Gh_j) over each sample's missing SNPs of the window
+    SegGatherArgs sg{};
+    sg.e0 = c.bk_ptr_host[(size_t)win * c.N];
+    sg.e1 = c.bk_ptr_host[(size_t)(win + 1) * c.N];
+    sg.key = c.bk_sample.p;
+    sg.key_base = 0;
+    sg.src = c.bk_pos.p;
+    sg.src_base = pos0;
+    sg.L = c.L;
+    sg.LP = LP;
+    sg.R = c.gmint.p;
+    sg.out = c.hisum.p;
+    sg.val = em ? c.bk_value.p : nullptr;
+    sg.R2 = c.ghint.p;
+    sg.out2 = c.hesum.p;
+    launch_seg_gather(sg, c.stream);
+  }
   mark(1);
   tc::launch_h(c.map_bed_h, c.map_gt, ha, c.stream);
   close_mark();
   tc::launch_h_finish(c.N, c.npad, c.L, LP, c.hpart.p, nsp, c.cvec.p, Hx, c.stream);
-  if (sp.active) {
-    WindowArgs a{c.view(), c.permuted ? c.perm.p : nullptr, c.lut32.p, pos0, (int)n, c.LP, c.npad};
-    launch_window_h_sparse(a, sp, c.G.p, Hx, c.stream);
-  }
 }
 
 // one window: G[pos0 .. pos0+n) = X_w Omega;  Hx += X_w^T G_w
@@ -695,7 +807,14 @@ static void window_product(Context& c, int64_t pos0, int64_t n, double* Hx) {
   mark(1);
   launch_window_h(a, c.g32.p, c.hpart.p, nsp, c.stream);
   close_mark();
-  launch_window_h_finish(a, c.hpart.p, nsp, sp, c.G.p, Hx, c.stream);
+  launch_window_h_finish(a, c.hpart.p, nsp, Hx, c.stream);
+  if (sp.active) {
+    const int64_t win = c.bk_wsize > 0 ? pos0 / c.bk_wsize : 0;
+    if (!c.bk_valid || pos0 != win * c.bk_wsize)
+      throw Error(PCAONE_E_ARG, "internal: missing-entry index does not match the windows");
+    launch_h_buckets(win, c.N, c.L, c.LP, c.bk_ptr.p, c.bk_pos.p, c.bk_value.p, sp.perm, c.scale.p, c.g32.p, pos0,
+                     Hx, c.stream);
+  }
 }
 
 // NormalRsvdOpData::computeGandH, in-core branch (src/Halko.cpp:99-128)
@@ -704,8 +823,7 @@ static void compute_g_and_h_single(Context& c, int pi) {
   if (pi == 0) prepare_epoch0(c, false);
   if (pi > 0) update_omega_from_h(c);
   zero(c.H, c.stream);
-  const int64_t nwin = (c.M + 16383) / 16384;
-  const int64_t w = (c.M + nwin - 1) / nwin;
+  const int64_t w = window_size(c);
   for (int64_t pos = 0; pos < c.M; pos += w) window_product(c, pos, std::min(w, c.M - pos), c.H.p);
 }
 

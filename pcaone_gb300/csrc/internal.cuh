@@ -46,6 +46,71 @@ inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 //   counts  : nsnps x 4 int32 (n00, n01, n10, n11)
 //   F       : nsnps doubles (allele frequency of A1)
 // ---------------------------------------------------------------------------
+// Error-free FP32 accumulation of products (a "double-float" pair hi + lo).
+// FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU, so
+// long sums of products in the sparse missing-entry terms use FP32 pairs:
+// a * b = p + pe exactly (TwoProduct via fmaf), hi + p = s + se exactly
+// (TwoSum, Knuth), and the error terms gather in lo.  The result hi + lo
+// carries about 48 significand bits.  The _rn intrinsics keep the compiler
+// from contracting the steps into fused operations, which would break the
+// error-free identities.
+struct FloatPair {
+  float hi = 0.f, lo = 0.f;
+};
+__device__ __forceinline__ void fp_add_prod(FloatPair& acc, float a, float b) {
+  const float p = __fmul_rn(a, b);
+  const float pe = fmaf(a, b, -p);
+  const float s = __fadd_rn(acc.hi, p);
+  const float bv = __fsub_rn(s, acc.hi);
+  const float se = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bv)), __fsub_rn(p, bv));
+  acc.hi = s;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(se, pe));
+}
+// acc += a * b with a = ah + al and b = bh + bl given as float pairs: the
+// product of the high parts exactly (TwoProduct), the cross terms rounded
+// (al * bl, below 2^-48 relative, is dropped)
+__device__ __forceinline__ void fp_add_prod2(FloatPair& acc, float ah, float al, float bh, float bl) {
+  const float p = __fmul_rn(ah, bh);
+  const float pe = fmaf(ah, bh, -p);
+  const float cross = fmaf(ah, bl, fmaf(al, bh, pe));
+  const float s = __fadd_rn(acc.hi, p);
+  const float bv = __fsub_rn(s, acc.hi);
+  const float se = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bv)), __fsub_rn(p, bv));
+  acc.hi = s;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(se, cross));
+}
+__device__ __forceinline__ double fp_value(const FloatPair& acc) { return (double)acc.hi + (double)acc.lo; }
+// a double coefficient as hi + lo floats (hi = nearest float, lo = the rest)
+__device__ __forceinline__ void fp_split(double c, float& hi, float& lo) {
+  hi = (float)c;
+  lo = (float)(c - (double)hi);
+}
+
+// Segmented gather of integer rows over a range of missing-genotype entries,
+// in the order the entries are stored (k_seg_gather in util.cu):
+//   out[key_e][l]  += R[src_e][l]
+//   out2[key_e][l] += (rint(v_e * 2^24) * R2[src_e][l]) >> 8   (with values v_e)
+// key_e = key[e] - key_base (the output row), src_e = src[e] - src_base (the
+// source row); rows have LP entries, columns < L are summed.  The sums are
+// int64 (two's complement in unsigned storage) and flushed with atomics, so
+// they are exact and independent of the order of the flushes.  Entries with
+// the same key must be contiguous for few flushes.
+struct SegGatherArgs {
+  int64_t e0, e1;
+  const int32_t* key;
+  int64_t key_base;
+  const int32_t* src;
+  int64_t src_base;
+  int L, LP;
+  const int32_t* R;
+  unsigned long long* out;
+  const double* val;  // nullptr: no value products
+  const int32_t* R2;
+  unsigned long long* out2;
+};
+constexpr double kSegValueScale = 16777216.0;  // v quantised to 2^-24
+constexpr int kSegValueShift = 8;              // out2 is in units of 2^-16 of R2
+
 struct BedView {
   const uint8_t* bed;
   int64_t stride;
@@ -92,12 +157,9 @@ void launch_window_g_finish(const WindowArgs& a, const float* part, int nchunks,
 // hpart[c][i][l] = sum over SNPs of split c of x(i, pos0+j) * g32[j][l]
 int window_h_splits(const WindowArgs& a);
 void launch_window_h(const WindowArgs& a, const float* g32, float* hpart, int nsplit, cudaStream_t s);
-// Hx[i][l] += sum_c hpart[c][i][l] (+ sparse term), rows < nsamples
-void launch_window_h_finish(const WindowArgs& a, const float* hpart, int nsplit, const SparseRows& sp,
-                            const double* G, double* Hx, cudaStream_t s);
-
-// Hx[sample_e][:] += scale_j * value_e * G[pos][:] over the window's missing entries
-void launch_window_h_sparse(const WindowArgs& a, const SparseRows& sp, const double* G, double* Hx, cudaStream_t s);
+// Hx[i][l] += sum_c hpart[c][i][l], rows < nsamples (the EM term is added by
+// launch_h_buckets)
+void launch_window_h_finish(const WindowArgs& a, const float* hpart, int nsplit, double* Hx, cudaStream_t s);
 
 // dense FP64 helpers (dense64.cu); tall matrices are row-major with ld = LP
 int cross_blocks(int64_t rows);
@@ -132,6 +194,18 @@ void launch_matvec(const BedView& v, const double* F, const double* scale, const
 // misc (util.cu)
 void launch_missing_list(const BedView& v, const int32_t* perm, const int64_t* rowptr, int32_t* epos,
                          int32_t* sample, cudaStream_t s);
+// missing genotypes grouped by (window of wsize positions, sample): counts, then
+// positions / samples at the exclusive-scan offsets ptr (nwin * N + 1)
+void launch_bucket_count(const BedView& v, const int32_t* perm, int64_t wsize, int nwin, int32_t* cnt,
+                         cudaStream_t s);
+void launch_bucket_fill(const BedView& v, const int32_t* perm, int64_t wsize, int nwin, const int64_t* ptr,
+                        int32_t* bpos, int32_t* bsample, cudaStream_t s);
+// Hx[i] += the FP32-form EM term of window win: sum over the sample's missing
+// positions p of s_p v_e G32[p - rbase] (G32 = the window's FP32 G rows)
+void launch_h_buckets(int64_t win, int N, int L, int LP, const int64_t* ptr, const int32_t* bpos, const double* bval,
+                      const int32_t* perm, const double* scale, const float* Rf, int64_t rbase, double* Hx,
+                      cudaStream_t s);
+void launch_seg_gather(const SegGatherArgs& a, cudaStream_t s);
 void launch_flip_uv(double* U, int64_t nrows_u, double* V, int64_t nrows_v, int k, int* flag, cudaStream_t s);
 void launch_transpose_out(const double* A, int64_t rows, int lda, int cols, double* out, cudaStream_t s);
 

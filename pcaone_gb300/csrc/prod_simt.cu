@@ -223,23 +223,6 @@ __global__ void k_window_h_finish(int nsamples, int npad, int LP, const float* _
   Hx[idx] += acc;
 }
 
-// Sparse missing-value term of the H product (EM): Hx[sample_e][:] +=
-// scale_j * value_e * G[pos][:].  One warp per window row.
-__global__ void k_window_h_sparse(int64_t pos0, int nsnp, int LP, SparseRows sp, const double* __restrict__ G,
-                                  double* __restrict__ Hx) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= nsnp) return;
-  const int64_t pos = pos0 + warp;
-  const int64_t snp = sp.perm ? (int64_t)sp.perm[pos] : pos;
-  const double sc = sp.scale[snp];
-  for (int64_t e = sp.rowptr[pos]; e < sp.rowptr[pos + 1]; ++e) {
-    const double w = sc * sp.value[e];
-    double* dst = Hx + (size_t)sp.sample[e] * LP;
-    for (int l = lane; l < LP; l += 32) atomicAdd(dst + l, w * G[pos * LP + l]);
-  }
-}
-
 template <int LP>
 void launch_g_t(const WindowArgs& a, const float* omg32, float* part, int nchunks, cudaStream_t s) {
   const int chunk = round_up(ceil_div(a.npad, nchunks), kGStep);
@@ -313,20 +296,9 @@ void launch_window_g_finish(const WindowArgs& a, const float* part, int nchunks,
   PCAONE_LAUNCH_CHECK();
 }
 
-void launch_window_h_finish(const WindowArgs& a, const float* hpart, int nsplit, const SparseRows& sp,
-                            const double* G, double* Hx, cudaStream_t s) {
+void launch_window_h_finish(const WindowArgs& a, const float* hpart, int nsplit, double* Hx, cudaStream_t s) {
   const int64_t n = (int64_t)a.v.nsamples * a.LP;
   k_window_h_finish<<<ceil_div(n, 256), 256, 0, s>>>(a.v.nsamples, a.npad, a.LP, hpart, nsplit, Hx);
-  PCAONE_LAUNCH_CHECK();
-  if (sp.active) {
-    k_window_h_sparse<<<ceil_div((int64_t)a.nsnp * 32, 256), 256, 0, s>>>(a.pos0, a.nsnp, a.LP, sp, G, Hx);
-    PCAONE_LAUNCH_CHECK();
-  }
-}
-
-void launch_window_h_sparse(const WindowArgs& a, const SparseRows& sp, const double* G, double* Hx, cudaStream_t s) {
-  if (!sp.active) return;
-  k_window_h_sparse<<<ceil_div((int64_t)a.nsnp * 32, 256), 256, 0, s>>>(a.pos0, a.nsnp, a.LP, sp, G, Hx);
   PCAONE_LAUNCH_CHECK();
 }
 

@@ -1,38 +1,40 @@
 // Window block products on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
 // With d the raw dosage (0/1/2, missing -> 0), m the missing indicator, f the
-// allele frequency and s the per-SNP scale, the standardised genotype is
-//     x(i,j) = s_j * (d_ij/2 - f_j + f_j m_ij)
+// allele frequency, s the per-SNP scale and e the EM fill value of a missing
+// entry (0 under mean imputation), the standardised genotype is
+//     x(i,j) = s_j * (d_ij/2 - f_j + (f_j + e_ij) m_ij)
 // (mean imputation of missing entries, src/FilePlink.cpp:102-109, scaled as in
-// src/Data.cpp:351-362).  The products of one SNP window are formed from the
-// exact operands d and m, which are exact in BF16, and an affine epilogue:
-//   G_j  = s_j * ( 1/2 (D W)_j - f_j * colsum(W) + f_j (M W)_j )
-//   H_i += (D Gh)_i - c + (M Gm)_i,  Gh_j = 1/2 s_j G_j,  Gm_j = 2 f_j Gh_j,
-//                                     c = sum_j 2 f_j Gh_j
+// src/Data.cpp:351-362; the EM fill of src/Data.cpp:318-348).  The products of
+// one SNP window are formed from the dosages d, which are exact in BF16, an
+// affine epilogue, and a sparse term over the missing entries only:
+//   G_j  = s_j * ( 1/2 (D W)_j - f_j * colsum(W) + sum_{i missing} (f_j + e_ij) W_i )
+//   H_i += (D Gh)_i - c + sum_{j missing} 2 (f_j + e_ij) Gh_j,
+//          Gh_j = 1/2 s_j G_j,  c = sum_j 2 f_j Gh_j
 // where W is the test matrix Omega held as S integer slices (S = 1 or 3):
 // per column l a power-of-two unit u_ls = 2^(E_l - 7 - 8s) with
 // max_i |Omega_il| < 2^E_l, and W_il = sum_s u_ls * w_sil with integers
 // |w_sil| <= 128, exact in BF16 (Ozaki-style error-free splitting; three slices
 // carry 24 significand bits).  Each slice has its own TMEM accumulator: the
-// products d*w and m*w are integers of magnitude <= 256 and every partial sum of
-// a CTA (K <= 4096) stays below 2^24, so the tensor core accumulates exactly and
-// no rounding bias enters; the epilogue combines the slices in FP64 with their
-// units.  Gh and Gm are split the same way (per-column units over the window).
-// The centring terms use the same sliced values as the products, so the
+// products d*w are integers of magnitude <= 256 and every partial sum of a CTA
+// (K <= 4096) stays below 2^24, so the tensor core accumulates exactly and no
+// rounding bias enters; the epilogue combines the slices with their units.  Gh
+// is split the same way (per-column units over the window).  The centring and
+// missing-entry terms use the same represented values as the products, so the
 // operator applied is exactly X times the sliced matrix.
 //
-// Kernels (one CTA = 128 threads = one warpgroup; thread 0 issues TMA and MMA):
+// Kernels (one CTA = 384 threads in three roles, see role_wait below):
 //   k_tc_g : tile of 128 SNPs x one chunk of samples.  TMA brings the packed
 //            tile (128 rows x 16 bytes) and the W^T slice tiles (S*L rows x 64,
 //            128B swizzle, K-major B operand); decoder warps turn the packed
-//            bytes into the BF16 A operands D and M, written straight into
-//            TMEM (tcgen05.st); tcgen05.mma (A from TMEM, B from shared memory,
-//            the S slices concatenated along N) accumulates D*W and M*W in
-//            TMEM; the epilogue (tcgen05.ld) writes FP32 partial sums,
-//            combined in FP64 by k_tc_g_finish.
+//            bytes into the BF16 dosage operand D, written straight into TMEM
+//            (tcgen05.st); tcgen05.mma (A from TMEM, B from shared memory, the
+//            S slices concatenated along N) accumulates D*W in TMEM; the
+//            epilogue (tcgen05.ld) writes FP32 partial sums, combined in FP64
+//            by k_tc_g_finish.
 //   k_tc_h : tile of 128 samples x one split of the window's SNPs.  TMA brings
-//            the packed tile (64 SNP rows x 32 bytes) and the Gh^T / Gm^T slice
-//            tiles; decoder warps transpose into the D^T / M^T A operands.
+//            the packed tile (64 SNP rows x 32 bytes) and the Gh^T slice tiles;
+//            decoder warps transpose into the D^T A operand.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -49,8 +51,14 @@ namespace {
 
 constexpr int kThreads = 384;          // 12 warps: TMA producer, MMA issuer, 8 decode / TMEM-epilogue warps
 constexpr int kStepK = 64;              // K elements per pipeline stage (128 B of BF16 per row)
-constexpr int kMaxStages = 4;
+constexpr int kMaxStages = 8;
 constexpr long long kTimeoutCycles = 4000000000ll;  // about 2 s at 2 GHz
+
+// 2^e as a double (exact; the bit pattern directly for normal results)
+__device__ __forceinline__ double exp2i(int e) {
+  if (e < -1022 || e > 1023) return ldexp(1.0, e);
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -181,38 +189,27 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-constexpr uint16_t kBf16One = 0x3F80;
-
 
 // SWAR decode of two 2-bit codes held at bits 0-1 and 16-17 of x into two BF16
 // values (low and high half-words): dosage 00 -> 2.0 (0x4000), 10 -> 1.0
-// (0x3F80), 01 and 11 -> 0; missing indicator 01 -> 1.0.
+// (0x3F80), 01 (missing) and 11 -> 0.
 __device__ __forceinline__ uint32_t dosage_pair(uint32_t x) {
   const uint32_t lo = x & 0x00010001u, hi = (x >> 1) & 0x00010001u;
   return (0x40004000u - (hi << 7)) & ~(lo * 0xFFFFu);
 }
-__device__ __forceinline__ uint32_t missing_pair(uint32_t x) {
-  const uint32_t lo = x & 0x00010001u, hi = (x >> 1) & 0x00010001u;
-  return (lo & ~hi) * (uint32_t)kBf16One;
-}
 
 
 struct SmemLayout {
-  uint32_t a_d, a_m, b, p, stage_bytes;
+  uint32_t b, p, stage_bytes;
 };
 
-__host__ __device__ inline SmemLayout layout_for(int LP, int nslice, int bparts, bool mask, int pbytes) {
-  // the A operands live in TMEM; a stage holds the B slices and the packed tile
+// one pipeline stage in shared memory: the B slices (nslice * LP rows of 128
+// bytes, 128B-swizzled) and the packed tile; the A operand lives in TMEM
+__host__ __device__ inline SmemLayout layout_for(int LP, int nslice, int pbytes) {
   SmemLayout s{};
-  uint32_t off = 0;
-  (void)mask;
-  s.a_d = 0;
-  s.a_m = 0;
-  s.b = off;
-  off += (uint32_t)(bparts * nslice * LP * 128);
-  s.p = off;
-  off += (uint32_t)pbytes;
-  s.stage_bytes = (off + 1023u) & ~1023u;
+  s.b = 0;
+  s.p = (uint32_t)(nslice * LP * 128);
+  s.stage_bytes = (s.p + (uint32_t)pbytes + 1023u) & ~1023u;
   return s;
 }
 
@@ -271,11 +268,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ uint64_t full_bar[kMaxStages], dec_bar[kMaxStages], empty_bar[kMaxStages], acc_bar;
   __shared__ uint32_t tmem_sh;
   __shared__ volatile int abort_sh;
-  __shared__ int miss_sh;
   __shared__ float unit[3 * 112];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int LP = a.LP, S = a.nslice;
-  const SmemLayout lay = layout_for(LP, S, 1, a.mask != 0, 128 * 16);
+  const SmemLayout lay = layout_for(LP, S, 128 * 16);
   const int row0 = blockIdx.x * 128;                  // window-local first SNP of the tile
   const int kbeg = blockIdx.y * a.chunk;
   const int kend = min(kbeg + a.chunk, a.npad);
@@ -285,7 +281,6 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (tid == 0) {
     abort_sh = 0;
-    miss_sh = 0;
     for (int s = 0; s < nst; ++s) {
       mbar_init(&full_bar[s], 1);
       mbar_init(&dec_bar[s], kDecoders);
@@ -295,26 +290,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     fence_mbar_init();
   }
   for (int e = tid; e < S * LP; e += kThreads) unit[e] = (float)a.wscale[e];
-  __syncthreads();
-  if (a.mask) {  // does the tile hold a missing genotype? (the mask product is skipped if not)
-    int has = 0;
-    if (tid < 128 && row0 + tid < a.nsnp) {
-      const int64_t pos = a.pos0 + row0 + tid;
-      const int64_t snp = a.perm ? (int64_t)a.perm[pos] : pos;
-      has = a.counts[snp * 4 + 1] > 0;
-    }
-    if (__syncthreads_or(has) && tid == 0) miss_sh = 1;
-  }
   if (warp == 0) tmem_alloc(&tmem_sh, (uint32_t)a.tmem_cols);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_sh;
-  const bool use_m = a.mask && miss_sh;
-  // TMEM columns: accumulators [0, a_col0), then per stage A_D (32 columns =
-  // 64 BF16 K elements) and A_M (32 more when the mask product is formed)
-  const uint32_t a_col0 = (uint32_t)((a.mask ? 2 : 1) * ncat);
-  const uint32_t a_stride = a.mask ? 64u : 32u;
+  // TMEM columns: accumulators [0, ncat), then per stage the dosage operand
+  // (32 columns = 64 BF16 K elements)
+  const uint32_t a_col0 = (uint32_t)ncat;
 
   if (warp == 0) {
     // ---- TMA producer ----
@@ -348,13 +331,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         tc_fence_after();
         uint8_t* base = smem + st * lay.stage_bytes;
         const uint32_t bb = smem_u32(base + lay.b);
-        const uint32_t ad = tmem + a_col0 + st * a_stride, am = ad + 32;
+        const uint32_t ad = tmem + a_col0 + st * 32;
 #pragma unroll
-        for (int kk = 0; kk < kStepK / 16; ++kk) {
-          const uint32_t acc = (kb | kk) != 0;
-          mma_cat(tmem, ad + kk * 8, bb + kk * 32, ncat, acc);
-          if (use_m) mma_cat(tmem + ncat, am + kk * 8, bb + kk * 32, ncat, acc);
-        }
+        for (int kk = 0; kk < kStepK / 16; ++kk) mma_cat(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
         mma_commit(&empty_bar[st]);
       }
       mma_commit(&acc_bar);  // arrives once every MMA above has completed
@@ -362,7 +341,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp >= kDecodeWarp0) {
     // ---- decoders: TMEM lane quarter q4 = warp % 4 (row r = SNP 32*q4 + lane of
     // the tile), K half ch: samples 32ch .. 32ch+31 of the step (8 packed bytes)
-    // -> 16 columns of BF16 pairs into the stage's A_D (and A_M) in TMEM ----
+    // -> 16 columns of BF16 pairs into the stage's operand in TMEM ----
     const int q4 = warp & 3, ch = (warp - kDecodeWarp0) >> 2;
     const int r = q4 * 32 + lane;
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
@@ -371,18 +350,14 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
       uint8_t* base = smem + st * lay.stage_bytes;
       const uint2 pk = *reinterpret_cast<const uint2*>(base + lay.p + r * 16 + ch * 8);
-      uint32_t wd[16], wm[16];
+      uint32_t wd[16];
 #pragma unroll
       for (int e = 0; e < 16; ++e) {
         const uint32_t w32 = e < 8 ? pk.x : pk.y;
         const int sh = 4 * (e & 7);
-        const uint32_t x = ((w32 >> sh) & 3u) | (((w32 >> (sh + 2)) & 3u) << 16);
-        wd[e] = dosage_pair(x);
-        wm[e] = missing_pair(x);
+        wd[e] = dosage_pair(((w32 >> sh) & 3u) | (((w32 >> (sh + 2)) & 3u) << 16));
       }
-      const uint32_t acol = tmem + lane_off + a_col0 + st * a_stride + ch * 16;
-      tmem_st16(acol, wd);
-      if (use_m) tmem_st16(acol + 32, wm);
+      tmem_st16(tmem + lane_off + a_col0 + st * 32 + ch * 16, wd);
       tmem_wait_st();
       tc_fence_before();
       mbar_arrive(&dec_bar[st]);
@@ -395,23 +370,19 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
     float v[8];
     if (!abort_sh) {
-      for (int part = 0; part < (a.mask ? 2 : 1); ++part) {
-        const bool live = ok && (part == 0 || use_m);
-        float* out = part == 0 ? a.part_d : a.part_m;
-        for (int c0 = chalf * (LP / 2); c0 < (chalf + 1) * (LP / 2); c0 += 8) {
-          float sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-          if (live) {
-            for (int s = S - 1; s >= 0; --s) {
-              tmem_ld8(lane_base + part * ncat + s * LP + c0, v);
+      for (int c0 = chalf * (LP / 2); c0 < (chalf + 1) * (LP / 2); c0 += 8) {
+        float sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (ok) {
+          for (int s = S - 1; s >= 0; --s) {
+            tmem_ld8(lane_base + s * LP + c0, v);
 #pragma unroll
-              for (int t = 0; t < 8; ++t) sum[t] = fmaf(unit[s * LP + c0 + t], v[t], sum[t]);
-            }
+            for (int t = 0; t < 8; ++t) sum[t] = fmaf(unit[s * LP + c0 + t], v[t], sum[t]);
           }
-          if (j < a.nsnp) {
-            float* dst = out + ((size_t)blockIdx.y * a.nsnp + j) * LP + c0;
-            *reinterpret_cast<float4*>(dst) = make_float4(sum[0], sum[1], sum[2], sum[3]);
-            *reinterpret_cast<float4*>(dst + 4) = make_float4(sum[4], sum[5], sum[6], sum[7]);
-          }
+        }
+        if (j < a.nsnp) {
+          float* dst = a.part + ((size_t)blockIdx.y * a.nsnp + j) * LP + c0;
+          *reinterpret_cast<float4*>(dst) = make_float4(sum[0], sum[1], sum[2], sum[3]);
+          *reinterpret_cast<float4*>(dst + 4) = make_float4(sum[4], sum[5], sum[6], sum[7]);
         }
       }
     }
@@ -432,20 +403,23 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ uint64_t full_bar[kMaxStages], dec_bar[kMaxStages], empty_bar[kMaxStages], acc_bar;
   __shared__ uint32_t tmem_sh;
   __shared__ volatile int abort_sh;
-  __shared__ float unit[6 * 112];
+  __shared__ float unit[3 * 112];
+  __shared__ float munit[2 * 112];  // units of the missing-entry sums (Gm integers, EM products)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int LP = a.LP, S = a.nslice;
-  const bool mask = a.mask != 0;
-  const SmemLayout lay = layout_for(LP, S, mask ? 2 : 1, mask, 64 * 32);
+  const SmemLayout lay = layout_for(LP, S, 64 * 32);
   const int samp0 = blockIdx.x * 128;
   const int jb = blockIdx.y * a.per_split;
   const int je = min(jb + a.per_split, a.nsnp);
   const int nk = je > jb ? (je - jb + kStepK - 1) / kStepK : 0;
   const int nst = a.nstages;
-  const int bparts = mask ? 2 : 1;
   const int ncat = S * LP;
 
-  for (int e = tid; e < bparts * ncat; e += kThreads) unit[e] = (float)a.hscale[e];
+  for (int e = tid; e < ncat; e += kThreads) unit[e] = (float)a.hscale[e];
+  for (int e = tid; e < LP; e += kThreads) {
+    munit[e] = a.hisum ? (float)a.gmunit_m[e] : 0.f;
+    munit[LP + e] = a.hesum ? (float)(2.0 * exp2i(-24 + kSegValueShift) * a.hunit_m[e]) : 0.f;
+  }
   if (tid == 0) {
     abort_sh = 0;
     for (int s = 0; s < nst; ++s) {
@@ -461,12 +435,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_sh;
-  const uint32_t a_col0 = (uint32_t)(bparts * ncat);
-  const uint32_t a_stride = mask ? 64u : 32u;
+  const uint32_t a_col0 = (uint32_t)ncat;
 
   if (warp == 0) {
     if (lane == 0) {
-      const uint32_t tx_bytes = 64 * 32 + (uint32_t)(bparts * ncat * 128);
+      const uint32_t tx_bytes = 64 * 32 + (uint32_t)(ncat * 128);
       int issued = 0;
       for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
         tma_prefetch_2d(&map_bed, samp0 >> 2, (int)(a.pos0 + jb + kb * kStepK));
@@ -479,8 +452,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int j0 = jb + kb * kStepK;
         mbar_expect_tx(&full_bar[st], tx_bytes);
         tma_load_2d(base + lay.p, &map_bed, samp0 >> 2, (int)(a.pos0 + j0), &full_bar[st]);
-        for (int r = 0; r < bparts * S; ++r)
-          tma_load_2d(base + lay.b + r * LP * 128, &map_g, j0, r * LP, &full_bar[st]);
+        for (int r = 0; r < S; ++r) tma_load_2d(base + lay.b + r * LP * 128, &map_g, j0, r * LP, &full_bar[st]);
         issued = kb + 1;
       }
       if (abort_sh) {
@@ -495,13 +467,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         tc_fence_after();
         uint8_t* base = smem + st * lay.stage_bytes;
         const uint32_t bb = smem_u32(base + lay.b);
-        const uint32_t ad = tmem + a_col0 + st * a_stride, am = ad + 32;
+        const uint32_t ad = tmem + a_col0 + st * 32;
 #pragma unroll
-        for (int kk = 0; kk < kStepK / 16; ++kk) {
-          const uint32_t acc = (kb | kk) != 0;
-          mma_cat(tmem, ad + kk * 8, bb + kk * 32, ncat, acc);
-          if (mask) mma_cat(tmem + ncat, am + kk * 8, bb + ncat * 128 + kk * 32, ncat, acc);
-        }
+        for (int kk = 0; kk < kStepK / 16; ++kk) mma_cat(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
         mma_commit(&empty_bar[st]);
       }
       mma_commit(&acc_bar);
@@ -518,17 +486,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int st = kb % nst;
       if (!role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
       const uint8_t* pt = smem + st * lay.stage_bytes + lay.p + (ch * 32) * 32 + (r >> 2);
-      uint32_t wd[16], wm[16];
+      uint32_t wd[16];
 #pragma unroll
       for (int e = 0; e < 16; ++e) {
         const uint32_t b0 = pt[(2 * e) * 32], b1 = pt[(2 * e + 1) * 32];
-        const uint32_t x = ((b0 >> sh) & 3u) | (((b1 >> sh) & 3u) << 16);
-        wd[e] = dosage_pair(x);
-        wm[e] = missing_pair(x);
+        wd[e] = dosage_pair(((b0 >> sh) & 3u) | (((b1 >> sh) & 3u) << 16));
       }
-      const uint32_t acol = tmem + lane_off + a_col0 + st * a_stride + ch * 16;
-      tmem_st16(acol, wd);
-      if (mask) tmem_st16(acol + 32, wm);
+      tmem_st16(tmem + lane_off + a_col0 + st * 32 + ch * 16, wd);
       tmem_wait_st();
       tc_fence_before();
       mbar_arrive(&dec_bar[st]);
@@ -544,12 +508,31 @@ __global__ void __launch_bounds__(kThreads, 1)
         // smallest units first, so the FP32 sum rounds as little as possible
         float sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         if (ok) {
-          for (int part = bparts - 1; part >= 0; --part) {
-            for (int s = S - 1; s >= 0; --s) {
-              const int r = part * S + s;
-              tmem_ld8(lane_base + r * LP + c0, v);
+          for (int s = S - 1; s >= 0; --s) {
+            tmem_ld8(lane_base + s * LP + c0, v);
 #pragma unroll
-              for (int t = 0; t < 8; ++t) sum[t] = fmaf(unit[r * LP + c0 + t], v[t], sum[t]);
+            for (int t = 0; t < 8; ++t) sum[t] = fmaf(unit[s * LP + c0 + t], v[t], sum[t]);
+          }
+        }
+        // the first split also adds the missing-entry terms of its samples
+        // (int64 sums from k_seg_gather, read and cleared here)
+        if (blockIdx.y == 0 && a.hisum) {
+          unsigned long long* hs = a.hisum + (size_t)i * LP + c0;
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            if (c0 + t < a.L) {
+              sum[t] = fmaf(__ll2float_rn((long long)hs[t]), munit[c0 + t], sum[t]);
+              hs[t] = 0ull;
+            }
+          }
+          if (a.hesum) {
+            unsigned long long* he = a.hesum + (size_t)i * LP + c0;
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+              if (c0 + t < a.L) {
+                sum[t] = fmaf(__ll2float_rn((long long)he[t]), munit[LP + c0 + t], sum[t]);
+                he[t] = 0ull;
+              }
             }
           }
         }
@@ -589,29 +572,39 @@ __global__ void k_col_exponent(const double* __restrict__ A, int64_t rows, int L
   }
 }
 
-// Error-free split of v into S integer slices with units 2^(E-7-8s):
-// w_s = rint(r / u_s), r -= w_s u_s.  Returns the represented value.
-__device__ __forceinline__ double split_store(double v, int E, int S, __nv_bfloat16* dst, size_t slice_stride) {
-  double r = v, rep = 0.0;
-  for (int s = 0; s < S; ++s) {
-    const double u = ldexp(1.0, E - 7 - 8 * s);
-    const double w = rint(r / u);
-    dst[(size_t)s * slice_stride] = __double2bfloat16(w);  // |w| <= 128: exact
-    r -= w * u;
-    rep += w * u;
+// Split v (|v| < 2^E) into S integer slices: m = rint(v * 2^(8S-1-E)) has
+// |m| <= 2^(8S-1), and its balanced base-256 digits w_s (m = sum_s w_s
+// 256^(S-1-s), |w_s| <= 128, exact in BF16) are the slices, with units
+// u_s = 2^(E-7-8s).  Returns the represented value m * u_(S-1).  Integer
+// digit arithmetic keeps the FP64 work to one multiply and one conversion.
+// *m_out (optional) receives m.
+__device__ __forceinline__ double split_store(double v, int E, int S, __nv_bfloat16* dst, size_t slice_stride,
+                                              int* m_out = nullptr) {
+  const int m = __double2int_rn(v * exp2i(8 * S - 1 - E));
+  if (m_out) *m_out = m;
+  int rest = m;
+  for (int s = S - 1; s > 0; --s) {
+    const int w = ((rest + 128) & 255) - 128;
+    dst[(size_t)s * slice_stride] = __float2bfloat16_rn((float)w);
+    rest = (rest - w) >> 8;
   }
-  return rep;
+  dst[0] = __float2bfloat16_rn((float)rest);
+  return (double)m * exp2i(E - 8 * S + 1);
 }
 
-// W slices of Omega (S*LP rows x npad, K-major), their units, and the column
-// sums of the represented W over the real samples.
+// W slices of Omega (S*LP rows x npad, K-major) and the represented W, in FP64
+// and as the integer m (|m| <= 2^23; the value is m times the last slice unit).
 __global__ void k_omega_slices(const double* __restrict__ omg, int npad, int N, int LP, int S,
-                               const int* __restrict__ E, __nv_bfloat16* __restrict__ w, double* __restrict__ rep) {
+                               const int* __restrict__ E, __nv_bfloat16* __restrict__ w, double* __restrict__ rep,
+                               int32_t* __restrict__ wint) {
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (idx >= (int64_t)npad * LP) return;
   const int i = (int)(idx / LP), l = (int)(idx % LP);
   const double v = i < N ? omg[idx] : 0.0;
-  rep[idx] = split_store(v, E[l], S, w + (size_t)l * npad + i, (size_t)LP * npad);
+  int m = 0;
+  const double r = split_store(v, E[l], S, w + (size_t)l * npad + i, (size_t)LP * npad, &m);
+  rep[idx] = r;
+  wint[idx] = m;
 }
 
 __global__ void k_units(const int* __restrict__ E, int LP, int S, int eoff, double* __restrict__ unit) {
@@ -621,8 +614,12 @@ __global__ void k_units(const int* __restrict__ E, int LP, int S, int eoff, doub
   unit[idx] = ldexp(1.0, E[l] + eoff - 7 - 8 * s);
 }
 
-// G rows: FP64 epilogue of the chunk partials plus the EM sparse term, and
-// Gh = 1/2 s G (FP64) for the H operand.
+// G rows of the window: FP64 sum of the chunk partials, the centring term, and
+// the missing-entry term
+//   sum_{i missing} (f + e_i) W_i = f u_l sum_i m_il + 2^-16 u_l sum_i q(e_i m_il)
+// from the exact integer sums of the represented W (W_il = m_il u_l) gathered
+// by k_seg_gather (gisum, and gesum with EM fill values), which are read and
+// cleared here; then Gh = 1/2 s G (FP64) for the H operand.
 __global__ void k_tc_g_finish(GFinishArgs a) {
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (idx >= (int64_t)a.nsnp * a.LP) return;
@@ -633,27 +630,30 @@ __global__ void k_tc_g_finish(GFinishArgs a) {
     const int64_t pos = a.pos0 + j;
     const int64_t snp = a.perm ? (int64_t)a.perm[pos] : pos;
     const double f = a.F[snp], s = a.scale[snp];
-    double pd = 0.0, pm = 0.0;
-    for (int c = 0; c < a.nchunks; ++c) {
-      pd += (double)a.part_d[((size_t)c * a.nsnp + j) * LP + l];
-      if (a.part_m) pm += (double)a.part_m[((size_t)c * a.nsnp + j) * LP + l];
+    double pd = 0.0;
+    for (int c = 0; c < a.nchunks; ++c) pd += (double)a.part[((size_t)c * a.nsnp + j) * LP + l];
+    double miss = 0.0;
+    if (a.gisum) {
+      miss = f * a.wunit_m[l] * (double)(long long)a.gisum[idx];
+      a.gisum[idx] = 0ull;
+      if (a.gesum) {
+        miss += exp2i(-24 + kSegValueShift) * a.wunit_m[l] * (double)(long long)a.gesum[idx];
+        a.gesum[idx] = 0ull;
+      }
     }
-    double g = s * (0.5 * pd - f * a.colsum[l] + f * pm);
-    if (a.sp.active) {
-      double sacc = 0.0;
-      for (int64_t e = a.sp.rowptr[pos]; e < a.sp.rowptr[pos + 1]; ++e)
-        sacc += a.sp.value[e] * a.omg[(size_t)a.sp.sample[e] * LP + l];
-      g += s * sacc;
-    }
+    const double g = s * (0.5 * pd - f * a.colsum[l] + miss);
     a.G[pos * LP + l] = g;
     gh = 0.5 * s * g;
   }
   a.gh[idx] = gh;
 }
 
-// Gh and Gm = 2 f Gh slices (columns nsnp .. ldg-1 zeroed) with per-column
-// exponents Eh (Gm uses Eh + 1 since |Gm| <= 2 |Gh|), and the terms of
-// c = sum_j Gm_j, all from the represented (sliced) Gh.
+// Gh slices (columns nsnp .. ldg-1 zeroed) with per-column exponents Eh, the
+// represented Gh as integers (ghint, for the EM term of H), and Gm = 2 f Gh
+// represented as an integer per entry (exponent Eh + 1: |Gm| <= 2 |Gh|; the
+// value is gmint * u'_l, u'_l the last slice unit) together with its terms of
+// c = sum_j Gm_j, so that the centring and missing-entry terms of H use the
+// same represented Gm.
 __global__ void k_tc_gh_slices(GFinishArgs a, const int* __restrict__ Eh) {
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (idx >= (int64_t)a.ldg * a.LP) return;
@@ -661,20 +661,23 @@ __global__ void k_tc_gh_slices(GFinishArgs a, const int* __restrict__ Eh) {
   const int S = a.nslice, LP = a.LP;
   const size_t sstride = (size_t)LP * a.ldg;
   __nv_bfloat16* dh = a.gt + (size_t)l * a.ldg + j;
-  __nv_bfloat16* dm = a.gt + (size_t)S * LP * a.ldg + (size_t)l * a.ldg + j;
   if (j < a.nsnp && l < a.L) {
     const int64_t pos = a.pos0 + j;
     const int64_t snp = a.perm ? (int64_t)a.perm[pos] : pos;
-    const double f = a.F[snp];
-    const double ghq = split_store(a.gh[(size_t)j * LP + l], Eh[l], S, dh, sstride);
-    const double gm = 2.0 * f * ghq;
-    if (a.mask) split_store(gm, Eh[l] + 1, S, dm, sstride);
-    a.cpart[(size_t)j * LP + l] = gm;
+    int mh = 0;
+    const double ghq = split_store(a.gh[(size_t)j * LP + l], Eh[l], S, dh, sstride, &mh);
+    a.ghint[(size_t)j * LP + l] = mh;
+    const int e = Eh[l] + 1;
+    const int m = __double2int_rn(2.0 * a.F[snp] * ghq * exp2i(8 * S - 1 - e));
+    a.gmint[(size_t)j * LP + l] = m;
+    a.cpart[(size_t)j * LP + l] = (double)m * exp2i(e - 8 * S + 1);
   } else {
     for (int s = 0; s < S; ++s) dh[s * sstride] = __float2bfloat16(0.f);
-    if (a.mask)
-      for (int s = 0; s < S; ++s) dm[s * sstride] = __float2bfloat16(0.f);
-    if (j < a.nsnp) a.cpart[(size_t)j * LP + l] = 0.0;
+    if (j < a.nsnp) {
+      a.ghint[(size_t)j * LP + l] = 0;
+      a.gmint[(size_t)j * LP + l] = 0;
+      a.cpart[(size_t)j * LP + l] = 0.0;
+    }
   }
 }
 
@@ -692,6 +695,8 @@ __global__ void k_colreduce(const double* __restrict__ part, int rows, int LP, d
   if (threadIdx.x == 0) out[l] = red[0];
 }
 
+// H rows: FP64 sum of the split partials (the first carries the
+// missing-entry terms) minus c.
 __global__ void k_tc_h_finish(int nsamples, int npad, int L, int LP, const float* __restrict__ hpart, int nsplit,
                               const double* __restrict__ c, double* __restrict__ Hx) {
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -743,24 +748,20 @@ void make_map_2d(CUtensorMap* map, const void* base, bool bf16, uint64_t inner, 
   if (r != CUDA_SUCCESS) throw Error(-2, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-int stages_for(int LP, int nslice, int bparts, int acc_parts, bool mask, int pbytes) {
-  const SmemLayout l = layout_for(LP, nslice, bparts, mask, pbytes);
+int stages_for(int LP, int nslice, int pbytes) {
+  const SmemLayout l = layout_for(LP, nslice, pbytes);
   const int budget = 212 * 1024;  // dynamic shared memory (static use is under 12 KB)
   const int by_smem = budget / (int)l.stage_bytes;
-  // TMEM: accumulators (acc_parts x slices x LP columns) + per-stage A operands
-  // within the 512 columns of an SM
-  const int acc = acc_parts * nslice * LP;
-  const int a_stride = mask ? 64 : 32;
-  const int by_tmem = (512 - acc) / a_stride;
+  // TMEM: slice accumulators + 32 columns of A operand per stage, within the
+  // 512 columns of an SM
+  const int by_tmem = (512 - nslice * LP) / 32;
   return std::max(1, std::min(kMaxStages, std::min(by_smem, by_tmem)));
 }
 
-int tmem_cols_needed(int LP, int nslice, int bparts, bool mask, int nstages) {
-  return bparts * nslice * LP + nstages * (mask ? 64 : 32);
-}
+int tmem_cols_needed(int LP, int nslice, int nstages) { return nslice * LP + nstages * 32; }
 
-size_t smem_bytes(int LP, int nslice, int bparts, bool mask, int pbytes, int nstages) {
-  return (size_t)layout_for(LP, nslice, bparts, mask, pbytes).stage_bytes * nstages + 1024;
+size_t smem_bytes(int LP, int nslice, int pbytes, int nstages) {
+  return (size_t)layout_for(LP, nslice, pbytes).stage_bytes * nstages + 1024;
 }
 
 int tmem_cols_for(int ncols) {
@@ -770,39 +771,43 @@ int tmem_cols_for(int ncols) {
 }
 
 void launch_g(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs& a, cudaStream_t s) {
-  if (a.tmem_cols > 512 || a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.mask ? 2 : 1, a.mask != 0, a.nstages))
-    throw Error(-6, "tensor-core G product: TMEM plan exceeds 512 columns");
+  if (a.nstages < 1 || a.nstages > kMaxStages || a.tmem_cols > 512 ||
+      a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.nstages))
+    throw Error(-6, "tensor-core G product: pipeline plan exceeds TMEM or the stage limit");
   static bool attr = false;
   if (!attr) {
     PCAONE_CUDA(cudaFuncSetAttribute(k_tc_g, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
     attr = true;
   }
-  const size_t smem = smem_bytes(a.LP, a.nslice, 1, a.mask != 0, 128 * 16, a.nstages);
+  const size_t smem = smem_bytes(a.LP, a.nslice, 128 * 16, a.nstages);
+  if (smem > 214 * 1024) throw Error(-6, "tensor-core G product: pipeline plan exceeds shared memory");
   dim3 grid((a.nsnp + 127) / 128, a.nchunks);
   k_tc_g<<<grid, kThreads, smem, s>>>(map_bed, map_w, a);
   PCAONE_LAUNCH_CHECK();
 }
 
 void launch_h(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs& a, cudaStream_t s) {
-  if (a.tmem_cols > 512 || a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.mask ? 2 : 1, a.mask != 0, a.nstages))
-    throw Error(-6, "tensor-core H product: TMEM plan exceeds 512 columns");
+  if (a.nstages < 1 || a.nstages > kMaxStages || a.tmem_cols > 512 ||
+      a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.nstages))
+    throw Error(-6, "tensor-core H product: pipeline plan exceeds TMEM or the stage limit");
   static bool attr = false;
   if (!attr) {
     PCAONE_CUDA(cudaFuncSetAttribute(k_tc_h, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
     attr = true;
   }
-  const size_t smem = smem_bytes(a.LP, a.nslice, a.mask ? 2 : 1, a.mask != 0, 64 * 32, a.nstages);
+  const size_t smem = smem_bytes(a.LP, a.nslice, 64 * 32, a.nstages);
+  if (smem > 214 * 1024) throw Error(-6, "tensor-core H product: pipeline plan exceeds shared memory");
   dim3 grid(a.npad / 128, a.nsplit);
   k_tc_h<<<grid, kThreads, smem, s>>>(map_bed, map_g, a);
   PCAONE_LAUNCH_CHECK();
 }
 
 void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv_bfloat16* w, double* wunit,
-                         double* colsum, int* E, double* rep, cudaStream_t s) {
+                         double* colsum, int* E, double* rep, int32_t* wint, cudaStream_t s) {
   const int64_t n = (int64_t)npad * LP;
   k_col_exponent<<<LP, 256, 0, s>>>(omg, N, LP, E);
   PCAONE_LAUNCH_CHECK();
-  k_omega_slices<<<ceil_div(n, 256), 256, 0, s>>>(omg, npad, N, LP, S, E, w, rep);
+  k_omega_slices<<<ceil_div(n, 256), 256, 0, s>>>(omg, npad, N, LP, S, E, w, rep, wint);
   PCAONE_LAUNCH_CHECK();
   k_units<<<ceil_div(S * LP, 128), 128, 0, s>>>(E, LP, S, 0, wunit);
   PCAONE_LAUNCH_CHECK();
@@ -810,7 +815,7 @@ void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv
   PCAONE_LAUNCH_CHECK();
 }
 
-void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* c_out, cudaStream_t s) {
+void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* gmunit, double* c_out, cudaStream_t s) {
   k_tc_g_finish<<<ceil_div((int64_t)a.nsnp * a.LP, 256), 256, 0, s>>>(a);
   PCAONE_LAUNCH_CHECK();
   k_col_exponent<<<a.LP, 256, 0, s>>>(a.gh, a.nsnp, a.LP, Eh);
@@ -819,10 +824,8 @@ void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* c_out
   PCAONE_LAUNCH_CHECK();
   k_units<<<ceil_div(a.nslice * a.LP, 128), 128, 0, s>>>(Eh, a.LP, a.nslice, 0, hunit);
   PCAONE_LAUNCH_CHECK();
-  if (a.mask) {
-    k_units<<<ceil_div(a.nslice * a.LP, 128), 128, 0, s>>>(Eh, a.LP, a.nslice, 1, hunit + a.nslice * a.LP);
-    PCAONE_LAUNCH_CHECK();
-  }
+  k_units<<<ceil_div(a.nslice * a.LP, 128), 128, 0, s>>>(Eh, a.LP, a.nslice, 1, gmunit);
+  PCAONE_LAUNCH_CHECK();
   k_colreduce<<<a.LP, 256, 0, s>>>(a.cpart, a.nsnp, a.LP, c_out);
   PCAONE_LAUNCH_CHECK();
 }

@@ -18,64 +18,70 @@ struct GArgs {
   int chunk;              // samples per CTA (multiple of 64)
   int npad;               // padded sample count
   int nchunks;            // gridDim.y
-  int mask;               // form the missing-mask product too
   int nstages;            // pipeline depth
   int tmem_cols;          // TMEM columns allocated per CTA
   const double* wscale;   // S x LP units of the W slices
-  const int32_t* counts;  // per SNP (n00, n01, n10, n11)
-  const int32_t* perm;    // position -> SNP (counts lookup); nullptr = identity
-  float* part_d;          // [nchunks][nsnp][LP]
-  float* part_m;          // [nchunks][nsnp][LP] (mask)
+  float* part;            // [nchunks][nsnp][LP]
   int* err;               // set to 1 when a bounded wait gave up
 };
 
-// H += X_w^T * Gh (+ M^T * Gm) for one SNP window
+// H += X_w^T * Gh for one SNP window (dosage part; the first split's
+// epilogue adds the missing-entry sums gathered by k_seg_gather)
 struct HArgs {
   int64_t pos0;
   int nsnp;
+  int L;
   int LP;
   int nslice;
   int per_split;          // SNPs per CTA along K (multiple of 64)
   int nsplit;             // gridDim.y
   int npad;               // gridDim.x * 128
-  int mask;
   int nstages;
   int tmem_cols;
-  const double* hscale;   // (mask ? 2 : 1) * S x LP units of the Gh / Gm slices
+  const double* hscale;   // S x LP units of the Gh slices
   float* hpart;           // [nsplit][npad][LP]
   int* err;
+  unsigned long long* hisum;  // npad x LP int64 sums of Gm over missing entries (nullptr: none), cleared
+  const double* gmunit_m;     // per column unit of the Gm integers
+  unsigned long long* hesum;  // npad x LP int64 EM product sums (nullptr: no EM), cleared
+  const double* hunit_m;      // per column unit of the Gh integers
 };
 
 struct GFinishArgs {
   int64_t pos0;
   int nsnp;
-  int L, LP, nslice, nchunks, mask;
-  int ldg;                       // columns of the Gh/Gm operand (window length rounded up to 64)
-  const float* part_d;
-  const float* part_m;           // nullptr when no mask product
+  int L, LP, nslice, nchunks;
+  int ldg;                       // columns of the Gh operand (window length rounded up to 64)
+  const float* part;             // chunk partials of D W
   const double* colsum;          // column sums of the sliced W
   const double* F;
   const double* scale;
   const int32_t* perm;
-  const double* omg;             // FP64 Omega (EM sparse term)
-  SparseRows sp;
+  const double* wunit_m;         // per column unit of the integer W (the last slice unit)
+  unsigned long long* gisum;     // nsnp x LP int64 sums over missing entries (nullptr: none), cleared
+  unsigned long long* gesum;     // nsnp x LP int64 EM product sums (nullptr: no EM), cleared
   double* G;                     // nsnps x LP (FP64)
-  double* gh;                    // nsnp x LP (FP64) Gh of the window
-  __nv_bfloat16* gt;             // (2*nslice*LP) x ldg, K-major B operand of the H product
+  double* gh;                    // nsnp x LP (FP64): Gh of the window
+  int32_t* ghint;                // nsnp x LP: Gh as represented by its slices, as integers
+  int32_t* gmint;                // nsnp x LP: Gm = 2 f Gh represented as integers
+  __nv_bfloat16* gt;             // (nslice*LP) x ldg, K-major B operand of the H product
   double* cpart;                 // nsnp x LP partial terms of c
 };
 
 void make_map_2d(CUtensorMap* map, const void* base, bool bf16, uint64_t inner, uint64_t outer, uint64_t pitch_bytes,
                  uint32_t box_inner, uint32_t box_outer, bool swizzle128);
-// pipeline stages: shared memory holds bparts B slice groups, TMEM acc_parts accumulator groups
-int stages_for(int LP, int nslice, int bparts, int acc_parts, bool mask, int pbytes);
+// pipeline stages within shared memory (B slices + packed tile per stage) and
+// TMEM (nslice * LP accumulator columns + 32 A columns per stage)
+int stages_for(int LP, int nslice, int pbytes);
 int tmem_cols_for(int ncols);
-int tmem_cols_needed(int LP, int nslice, int bparts, bool mask, int nstages);
+int tmem_cols_needed(int LP, int nslice, int nstages);
 void launch_g(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs& a, cudaStream_t s);
 void launch_h(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs& a, cudaStream_t s);
 void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv_bfloat16* w, double* wunit,
-                         double* colsum, int* E, double* rep, cudaStream_t s);
-void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* c_out, cudaStream_t s);
+                         double* colsum, int* E, double* rep, int32_t* wint, cudaStream_t s);
+// G finish, Gh slices and their units (hunit), Gm integers with their units
+// (gmunit: S x LP, the last slice row is the unit of gmint), c
+void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* gmunit, double* c_out, cudaStream_t s);
 void launch_h_finish(int nsamples, int npad, int L, int LP, const float* hpart, int nsplit, const double* c,
                      double* Hx, cudaStream_t s);
 void launch_gather_rows(const uint8_t* src, uint8_t* dst, int64_t stride, const int32_t* perm, int64_t nrows,

@@ -11,7 +11,7 @@ no public dataset is used.  Generation is split in two halves:
 * genotype sampling, which is a pure function of (seed, SNP index, sample
   index) through a counter-based SplitMix64 hash.  ``sample_packed_bed`` below
   is the numpy form; the CUDA library carries the same arithmetic
-  (``pcaone_gpu_synth_bed``) for workloads too large to draw on the host, and
+  (``pcaone_gpu_load_synthetic``) for workloads too large to draw on the host, and
   both produce identical bytes.
 
 PLINK .bed coding of one genotype (2 bits, little-endian inside each byte,
@@ -220,6 +220,10 @@ WORKLOADS = {
     # scaled-down c2 (0.5 GB packed, still larger than L2) for profiling captures
     "c2s": dict(nsamples=20_000, nsnps=100_000, npop=5, fst=[0.01, 0.02, 0.05, 0.1, 0.2],
                 anc="uniform", anc_range=(0.01, 0.5), mcar=0.005, k=20, p=20, maxp=6, bands=64),
+    # the c2 window shape (7,812 SNPs x 100,000 samples) with 1/8 of the SNPs
+    # (1.56 GB packed) for profiling captures of single window launches
+    "c2p": dict(nsamples=100_000, nsnps=62_500, npop=5, fst=[0.01, 0.02, 0.05, 0.1, 0.2],
+                anc="uniform", anc_range=(0.01, 0.5), mcar=0.005, k=20, p=20, maxp=6, bands=8),
     "c4": dict(nsamples=50_000, nsnps=300_000, npop=4, fst=0.05, anc="uniform", anc_range=(0.05, 0.5),
                miss_sample_beta=(1, 20), miss_snp_beta=(1, 50), k=10, p=10, maxp=6, bands=64),
 }
