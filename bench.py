@@ -14,8 +14,15 @@ counts and allele frequencies -> window-based RSVD (winSVD, 7 epochs for the
 * ``e2e``: the same through the C-ABI with host buffers: pinned host .bed body
   -> pcaone_gpu_load_bed (H2D inside the timed region) -> run_halko -> U, S, V
   back to the host.
-* ``roofline``: the dominant kernel (the window H product), algorithmic flops
-  2*N*SNPs*L per launch over its CUDA-event time on the library's stream.
+* ``roofline``: the dominant kernel (the window H or G product), algorithmic
+  flops 2*N*SNPs*L per launch over its CUDA-event time on the library's
+  stream; ``executed_tflops`` counts the MMA work actually issued (three
+  integer BF16 slices of the sketch, padded to a multiple of 16 columns).
+  ``traffic`` is the DRAM bytes per launch of that kernel from an ncu capture
+  of a window of the same shape (workload c2p: the c2 window, 7,812 SNPs x
+  100,000 samples).
+* EM workloads (``c4``: ``--emu``) report the EM iterations and, with
+  ``--warm-start``, the learned start's statistics.
 * ``cpu_baseline`` / ``--impl reference``: the oracle (numpy/LAPACK restatement
   of the reference's Eigen/OpenMP path) on a bounded sample of the same
   workload, scaled to the full workload by N*M.
@@ -115,14 +122,33 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
+# DRAM bytes per launch of the tensor-core window products on the c2 window
+# shape (ncu, workload c2p; profiles/k_tc_window_c2p.md)
+NCU_TRAFFIC_C2_WINDOW = {"g": 255.3e6, "h": 227.2e6}
+
+
 def workload_params(name: str, precision: str):
     from pcaone_gb300 import capi, synthetic
     wl = synthetic.WORKLOADS[name]
     prec = {"fp32": capi.PREC_FP32, "bf16": capi.PREC_BF16, "bf16x3": capi.PREC_BF16X3,
             "fp8": capi.PREC_FP8}[precision]
-    p = capi.default_params(svd=2, k=wl["k"], oversamples=wl["p"], maxp=wl["maxp"], bands=wl["bands"],
-                            perm=1, standardize=1, precision=prec)
+    p = capi.default_params(svd=wl.get("svd", 2), k=wl["k"], oversamples=wl["p"], maxp=wl["maxp"],
+                            bands=wl["bands"], perm=wl.get("perm", 1), standardize=1, precision=prec)
+    if wl.get("emu"):
+        p.emu = 1
+        p.tolem = wl.get("tolem", 1e-5)
+        p.maxiter = wl.get("maxiter", 100)
     return wl, p
+
+
+def workload_desc(name: str, wl: dict, model, bps: int) -> str:
+    N, M = model.nsamples, model.nsnps
+    d = (f"{name}: N={N} x M={M} PLINK ({M * bps / 1e9:.1f} GB packed), {model.npop} populations, k={wl['k']}, "
+         f"p={wl['p']}, {'winSVD ' + str(wl['bands']) + ' windows' if wl.get('svd', 2) == 2 else 'sSVD'}, "
+         f"{wl['maxp'] + 1} epochs")
+    if wl.get("emu"):
+        d += f", EM to tol {wl.get('tolem', 1e-5):g} (at most {wl.get('maxiter', 100)} iterations)"
+    return d
 
 
 _cpu_sample_cache = {}
@@ -142,14 +168,16 @@ def cpu_sample_run(name: str):
         H.build_rng_lib()
     packed = _cpu_sample_cache[name]
     t0 = time.perf_counter()
-    d = H.OracleData(packed, n, perm=True, bands=wl["bands"])
+    d = H.OracleData(packed, n, perm=bool(wl.get("perm", 1)), bands=wl["bands"])
     H.run_pca_with_halko(d, wl["k"], wl["p"], maxp=wl["maxp"])
     t = time.perf_counter() - t0
     scale = (wl["nsamples"] * wl["nsnps"]) / (n * m)
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     desc = (f"numpy/LAPACK restatement of the reference's in-core path (decode, AF, standardise, shuffle, "
-            f"winSVD {wl['maxp'] + 1} epochs, k={wl['k']}, p={wl['p']}, 64 windows) on the first {n} samples x "
-            f"{m} SNPs of the same population model; {t:.2f} s measured, scaled by N*M x{scale:.1f}")
+            f"winSVD {wl['maxp'] + 1} epochs, k={wl['k']}, p={wl['p']}, {wl['bands']} windows) on the first {n} "
+            f"samples x {m} SNPs of the same population model; {t:.2f} s measured, scaled by N*M x{scale:.1f}")
+    if wl.get("emu"):
+        desc += "; one RSVD pass (EM iterations not included)"
     return t, t * scale, desc, cores
 
 
@@ -197,7 +225,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{wl_name}: N={wl['nsamples']} x M={wl['nsnps']} PLINK, k={wl['k']}, "
-                               f"p={wl['p']}, winSVD 64 windows, {wl['maxp'] + 1} epochs"},
+                               f"p={wl['p']}, winSVD {wl['bands']} windows, {wl['maxp'] + 1} epochs"},
         "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": desc},
         "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -210,6 +238,9 @@ def run_ours(args):
     from pcaone_gb300 import capi, synthetic
     torch.cuda.set_device(local)
     wl, params = workload_params(args.workload, args.precision)
+    if args.maxiter is not None:
+        params.maxiter = args.maxiter
+        wl = dict(wl, maxiter=args.maxiter)
     model = synthetic.model_for(args.workload, seed=1)
     N, M = model.nsamples, model.nsnps
     bps = (N + 3) // 4
@@ -217,6 +248,8 @@ def run_ours(args):
     peaks, peak_kind = load_peaks()
 
     ctx = capi.Context(local)
+    if args.warm_start:
+        ctx.set_warm_start(capi.mlp_default_params())
     # the resident source matrix (value path) and a pinned host copy (e2e path)
     src = capi.Context(local)
     src.load_synthetic(model)
@@ -227,9 +260,13 @@ def run_ours(args):
     src.close()
     torch.cuda.synchronize()
 
+    em_iters = []
+
     def step_device():
         ctx.load_bed_device(dev_src.data_ptr(), bps, M, N)
-        return ctx.run_halko(params)
+        out = ctx.run_halko(params)
+        em_iters.append(out[3])
+        return out
 
     def step_e2e():
         ctx.load_bed_ptr(pinned.data_ptr(), M, N)
@@ -283,16 +320,29 @@ def run_ours(args):
     ks = kstats[dom]
     achieved = ks["flops"] / (ks["ms"] / 1e3) / 1e12 if ks["ms"] > 0 else 0.0
     peak = peaks.get("bf16_tflops", PEAKS_FALLBACK["bf16_tflops"])
+    tc = args.precision != "fp32"
+    LPtc = (L + 15) // 16 * 16
+    executed = achieved * (3 * LPtc / L) if tc else achieved
+    per_launch_s = ks["ms"] / 1e3 / max(1, ks["launches"])
+    c2_shape = args.workload in ("c2", "c2p")
+    traffic = NCU_TRAFFIC_C2_WINDOW[dom[0]] if (tc and c2_shape) else None
     roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": None, "kernel": f"k_window_{dom[0]}",
+            "frac": achieved / peak, "traffic": traffic,
+            "kernel": f"k_tc_{dom[0]}" if tc else f"k_window_{dom[0]}",
+            "executed_tflops": executed, "executed_frac": executed / peak,
+            "hbm_gbs": (traffic / per_launch_s / 1e9) if traffic else None,
             "note": (f"{args.precision} form; {ks['launches']} launches, {ks['ms']:.1f} ms of "
-                     f"{sum(times) * 1e3:.1f} ms; peak = {peak_kind} bf16 dense")}
-    if args.precision == "fp32":
+                     f"{sum(times) * 1e3:.1f} ms; achieved = algorithmic 2*N*SNPs*L per launch / event time; "
+                     f"peak = {peak_kind} bf16 dense; traffic per launch from ncu (c2 window shape)")}
+    if not tc:
         roof["note"] += "; the FP32 form runs on CUDA cores, not the tensor pipe"
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         t_s, t_full, desc, cores = cpu_sample_run(args.workload)
+        if wl.get("emu"):
+            t_full *= (em_iters[-1] + 2) if em_iters else 1
+            desc += f"; scaled by {em_iters[-1] + 2 if em_iters else 1} RSVD passes (EM iterations + 2)"
         cpu = {"value": t_full, "unit": "s", "cores": cores, "kind": "port", "sample": desc}
 
     if rank == 0:
@@ -300,19 +350,22 @@ def run_ours(args):
             "metric": "sec_to_topk_pcs", "value": t_dev, "unit": "s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": args.precision, "data": "synthetic",
-            "config": {"workload": f"{args.workload}: N={N} x M={M} PLINK ({M * bps / 1e9:.1f} GB packed), "
-                                   f"{model.npop} populations, k={wl['k']}, p={wl['p']}, winSVD 64 windows, "
-                                   f"{wl['maxp'] + 1} epochs",
+            "config": {"workload": workload_desc(args.workload, wl, model, bps),
                        "precision": args.precision, "l2": "inputs larger than L2 (packed matrix resident in HBM)",
                        "replicas": ws},
             "clocks": clocks.summary(),
             "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": int(launches / max(1, args.steps)),
+            "gpu_launches": int(launches),
             "roofline": roof,
             "cpu_baseline": cpu,
             "kernels": kstats,
             "pcs": {"S_top": [float(x) for x in S[:5]]},
         }
+        if wl.get("emu"):
+            line["em"] = {"iterations": em_iters[-1] if em_iters else None, "tolem": params.tolem,
+                          "warm_start": bool(args.warm_start)}
+            if args.warm_start:
+                line["em"]["mlp"] = ctx.mlp_stats()
         print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -326,6 +379,8 @@ def main():
     ap.add_argument("--workload", default="c2")
     ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16", "bf16x3", "fp8"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--warm-start", action="store_true", help="learned EM warm start (EM workloads)")
+    ap.add_argument("--maxiter", type=int, default=None, help="EM iteration cap (EM workloads)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -35,10 +35,10 @@ extern "C" {
 
 /* precision of the block products G = X*Omega and H = X^T*G */
 #define PCAONE_PREC_FP32 0    /* FP32 SIMT products, FP64 window sums */
-#define PCAONE_PREC_BF16 1    /* tcgen05 tensor-core products: exact BF16 dosages and missing
-                                 mask; the test matrix and G split per column into three
-                                 integer BF16 slices (24 bits), exact integer accumulation in
-                                 TMEM, FP32/FP64 epilogue */
+#define PCAONE_PREC_BF16 1    /* tcgen05 tensor-core products: exact BF16 dosages; the test
+                                 matrix and G split per column into three integer BF16 slices
+                                 (24 bits), exact integer accumulation in TMEM, FP32/FP64
+                                 epilogue; missing genotypes as an exact sparse term */
 #define PCAONE_PREC_FP8 2     /* reserved: FP8 e4m3 operands (not built yet) */
 #define PCAONE_PREC_BF16X3 3  /* same as PCAONE_PREC_BF16 */
 
@@ -76,6 +76,35 @@ typedef struct {
   int standardize;  /* 1: per-SNP genetic standardisation (scale == -9) */
   int precision;    /* PCAONE_PREC_* */
 } pcaone_gpu_params;
+
+/* Learned warm start of the EM imputation (no reference counterpart; it
+ * replaces only the mean-fill start of run_pca_with_halko's EM loop,
+ * src/Halko.cpp:290-320).  After the first, mean-imputed computeUSV a small
+ * MLP (64 -> 256 -> 256 -> 1, BF16 weights, FP32 accumulation, Adam) is
+ * trained on the GPU on randomly drawn observed genotypes and fills every
+ * missing genotype; EM then iterates from that fill exactly as without it.
+ * Inputs of entry (SNP s, sample i): the 32 flanking SNP dosages of sample i
+ * in file order, the sample's top-q scores, the SNP's top-q loadings, its
+ * allele frequency and the sample's and SNP's missing fractions
+ * (q = min(k, 14)). */
+typedef struct {
+  int enable;           /* 1: use the learned start when emu is set */
+  int train_entries;    /* observed genotypes drawn for training */
+  int holdout_entries;  /* further observed genotypes for the held-out error */
+  int epochs;           /* passes over the training genotypes */
+  int batch;            /* minibatch size */
+  float lr;             /* Adam step size */
+  uint64_t seed;        /* draws and initial weights */
+} pcaone_gpu_mlp_params;
+
+/* Number of FP32 parameters of the network (W1 64x256, b1, W2 256x256, b2,
+ * w3 256, b3 in this order; W row = input). */
+#define PCAONE_MLP_PARAMS 82689
+#define PCAONE_MLP_INPUTS 64
+
+/* Fills p with the defaults (enabled, 524288 training and 65536 held-out
+ * genotypes, 4 epochs, batch 4096, lr 1e-3). */
+void pcaone_gpu_mlp_default_params(pcaone_gpu_mlp_params* p);
 
 /* Fills p with the reference's defaults (src/Cmd.hpp:29-95). */
 void pcaone_gpu_default_params(pcaone_gpu_params* p);
@@ -153,6 +182,23 @@ int pcaone_gpu_run_halko(pcaone_gpu_ctx* ctx, const pcaone_gpu_params* params, d
 /* The working SNP order: perm[i] = original SNP of column i (Data::perm,
  * src/Data.hpp:49); identity when no shuffle was applied. */
 int pcaone_gpu_get_perm(pcaone_gpu_ctx* ctx, int32_t* perm);
+
+/* Learned warm start for the next pcaone_gpu_run_halko calls with emu set
+ * (NULL or enable = 0: plain mean-fill EM). */
+int pcaone_gpu_set_warm_start(pcaone_gpu_ctx* ctx, const pcaone_gpu_mlp_params* p);
+/* Statistics of the last learned start: [0] mean squared error of the last
+ * training epoch, [1] held-out mean squared error of the MLP, [2] held-out
+ * mean squared error of the mean fill, [3] training seconds, [4] seconds to
+ * fill the missing genotypes, [5] missing genotypes filled (both orderings).
+ * Errors are on the centred scale d/2 - f. */
+int pcaone_gpu_mlp_stats(pcaone_gpu_ctx* ctx, double out[6]);
+/* One forward and backward pass of the network on caller data, for checks:
+ * X (B x 64, row-major), y (B) targets, params (PCAONE_MLP_PARAMS FP32
+ * values; the forward pass uses their BF16 rounding).  Writes out (B), the
+ * mean squared error *loss and grads (PCAONE_MLP_PARAMS, the gradient of the
+ * loss with respect to the rounded weights and the biases). */
+int pcaone_gpu_mlp_forward_backward(int device, const float* X, const float* y, int B, const float* params,
+                                    float* out, float* loss, float* grads);
 
 /* ---- Arnoldi matvec: replaces ArnoldiOpData::perform_op (Arnoldi.cpp:18-46) */
 /* y = X X^T x over the loaded genotypes (X samples x SNPs, centred, scaled

@@ -30,8 +30,10 @@ EXPORTS = [
     "pcaone_gpu_set_flags", "pcaone_gpu_compute_g_and_h", "pcaone_gpu_compute_usv", "pcaone_gpu_run_halko",
     "pcaone_gpu_get_perm", "pcaone_gpu_matvec", "pcaone_gpu_load_synthetic", "pcaone_gpu_get_bed",
     "pcaone_gpu_set_profiling", "pcaone_gpu_kernel_stats", "pcaone_gpu_launch_count",
-    "pcaone_gpu_matvec_static",
+    "pcaone_gpu_matvec_static", "pcaone_gpu_mlp_default_params", "pcaone_gpu_set_warm_start",
+    "pcaone_gpu_mlp_stats", "pcaone_gpu_mlp_forward_backward",
 ]
+MLP_PARAMS, MLP_INPUTS = 82689, 64
 
 
 class Params(ctypes.Structure):
@@ -39,6 +41,11 @@ class Params(ctypes.Structure):
                 ("seed", c_int), ("rand", c_int), ("perm", c_int), ("emu", c_int), ("maxiter", c_int),
                 ("tol", c_double), ("tolem", c_double), ("ploidy", c_int), ("standardize", c_int),
                 ("precision", c_int)]
+
+
+class MlpParams(ctypes.Structure):
+    _fields_ = [("enable", c_int), ("train_entries", c_int), ("holdout_entries", c_int), ("epochs", c_int),
+                ("batch", c_int), ("lr", ctypes.c_float), ("seed", c_uint64)]
 
 
 class Desc(ctypes.Structure):
@@ -91,8 +98,14 @@ def load(path: str = LIBPATH) -> ctypes.CDLL:
     lib.pcaone_gpu_launch_count.argtypes = []
     lib.pcaone_gpu_matvec_static.argtypes = [c_void_p, c_uint64, c_uint64, c_uint32, c_void_p, c_int, c_void_p,
                                              c_void_p, c_void_p]
+    lib.pcaone_gpu_mlp_default_params.argtypes = [P(MlpParams)]
+    lib.pcaone_gpu_mlp_default_params.restype = None
+    lib.pcaone_gpu_set_warm_start.argtypes = [c_void_p, P(MlpParams)]
+    lib.pcaone_gpu_mlp_stats.argtypes = [c_void_p, c_void_p]
+    lib.pcaone_gpu_mlp_forward_backward.argtypes = [c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
+                                                    c_void_p]
     for name in EXPORTS:
-        if name not in ("pcaone_gpu_default_params", "pcaone_gpu_last_error"):
+        if name not in ("pcaone_gpu_default_params", "pcaone_gpu_last_error", "pcaone_gpu_mlp_default_params"):
             getattr(lib, name).restype = c_int
     lib.pcaone_gpu_launch_count.restype = ctypes.c_ulonglong
     _lib = lib
@@ -107,6 +120,35 @@ def default_params(**kw) -> Params:
             raise AttributeError(k)
         setattr(p, k, v)
     return p
+
+
+def mlp_default_params(**kw) -> MlpParams:
+    p = MlpParams()
+    load().pcaone_gpu_mlp_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p
+
+
+def mlp_forward_backward(X: np.ndarray, y: np.ndarray, params: np.ndarray, device: int = 0):
+    """One forward + backward pass of the warm-start network on the GPU:
+    returns (out, loss, grads)."""
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    B = X.shape[0]
+    if X.shape != (B, MLP_INPUTS) or y.shape != (B,) or params.shape != (MLP_PARAMS,):
+        raise ValueError("shapes: X (B, 64), y (B,), params (82689,)")
+    out = np.empty(B, np.float32)
+    grads = np.empty(MLP_PARAMS, np.float32)
+    loss = ctypes.c_float(0)
+    rc = load().pcaone_gpu_mlp_forward_backward(device, X.ctypes.data, y.ctypes.data, B, params.ctypes.data,
+                                                out.ctypes.data, ctypes.byref(loss), grads.ctypes.data)
+    if rc != PCAONE_OK:
+        raise PcaoneError(rc, "pcaone_gpu_mlp_forward_backward failed")
+    return out, float(loss.value), grads
 
 
 def _ptr(a):
@@ -236,6 +278,16 @@ class Context:
         self._check(self.lib.pcaone_gpu_run_halko(self.h, ctypes.byref(params), _ptr(U), _ptr(S),
                                                   _ptr(V) if want_v else None, ctypes.byref(it)))
         return U, S, (V if want_v else None), it.value
+
+    def set_warm_start(self, p):
+        """Learned EM warm start for the next run_halko calls (None disables)."""
+        self._check(self.lib.pcaone_gpu_set_warm_start(self.h, ctypes.byref(p) if p is not None else None))
+
+    def mlp_stats(self):
+        out = np.zeros(6)
+        self._check(self.lib.pcaone_gpu_mlp_stats(self.h, _ptr(out)))
+        return {"train_mse": out[0], "holdout_mse": out[1], "holdout_mse_mean_fill": out[2], "train_s": out[3],
+                "fill_s": out[4], "filled": int(out[5])}
 
     def perm(self):
         out = np.empty(self.nsnps, dtype=np.int32)

@@ -20,6 +20,7 @@
 
 #include "../../include/pcaone_gpu.h"
 #include "internal.cuh"
+#include "mlp.cuh"
 #include "prod_tc.cuh"
 
 namespace pcaone {
@@ -93,6 +94,15 @@ struct Context {
   std::vector<int64_t> bk_ptr_host;
   DBuf<int32_t> bk_cnt, bk_pos, bk_sample;
   DBuf<double> bk_value;
+  bool bk_stale = true;  // bk_value does not yet hold the current fill values
+
+  // learned warm start of the EM imputation (mlp.cu)
+  pcaone_gpu_mlp_params warm{};
+  bool prefilled = false;  // the fill values come from the warm start; skip the next EM fit
+  double warm_stats[6] = {0, 0, 0, 0, 0, 0};
+  std::unique_ptr<mlp::Net> net;
+  DBuf<int32_t> wpos, wsmp;
+  DBuf<float> wX, wy, smiss;
 
   // ---- operator (RsvdOpData) ----
   bool have_op = false;
@@ -546,6 +556,7 @@ static void fit_with_pi(Context& c) {
   launch_em_fill(c.miss_pos.p, c.miss_sample.p, c.miss_value.p, c.nnz, c.permuted ? c.perm.p : nullptr, c.F.p,
                  c.U.p, c.sigma.p, c.V.p, c.k, c.stream);
   c.fitted = true;
+  c.bk_stale = true;
   PCAONE_CUDA(cudaStreamSynchronize(c.stream));
   c.t_em += secs(t0, clk::now());
 }
@@ -588,6 +599,7 @@ static void ensure_buckets(Context& c) {
   c.bk_wsize = ws;
   c.bk_nwin = (int)nwin;
   c.bk_valid = true;
+  c.bk_stale = true;
 }
 
 // the missing-entry structures the window products read (the CSR list by
@@ -600,10 +612,11 @@ static void prepare_missing(Context& c) {
   if (c.counts_total_missing <= 0 || !(c.tc || em)) return;
   build_missing(c);
   ensure_buckets(c);
-  if (em) {
+  if (em && c.bk_stale) {
     c.bk_value.ensure((size_t)std::max<int64_t>(1, c.nnz), c.stream, false);
     launch_em_fill(c.bk_pos.p, c.bk_sample.p, c.bk_value.p, c.nnz, c.permuted ? c.perm.p : nullptr, c.F.p, c.U.p,
                    c.sigma.p, c.V.p, c.k, c.stream);
+    c.bk_stale = false;
   }
 }
 
@@ -613,7 +626,12 @@ static void refresh_lut(Context& c) {
 
 // the pi == 0 data preparation shared by both operators
 static void prepare_epoch0(Context& c, bool window) {
-  if (c.update && c.P.emu) fit_with_pi(c);
+  if (c.update && c.P.emu) {
+    if (c.prefilled)
+      c.prefilled = false;  // the learned start already holds the first fill
+    else
+      fit_with_pi(c);
+  }
   if (c.standardize) c.scaled = true;  // Data::standardize_E scales in place, once
   refresh_lut(c);
   if (window) {
@@ -958,6 +976,92 @@ static void outputs(Context& c, double* U, double* S, double* V) {
 static void flip_uv(Context& c) { launch_flip_uv(c.U.p, c.N, c.V.p, c.M, c.k, c.flag.p, c.stream); }
 
 // run_pca_with_halko (src/Halko.cpp:271-320), PLINK input, no LD output
+// Learned warm start (mlp.cu): train the network on observed genotypes drawn
+// at random, measure it on further held-out ones, then fill every missing
+// genotype (in both orderings of the missing-entry lists) with its clamped
+// prediction; the next EM iteration starts from that fill.
+static void warm_start(Context& c) {
+  const auto t0 = clk::now();
+  const pcaone_gpu_mlp_params& w = c.warm;
+  if (w.train_entries <= 0 || w.batch <= 0 || w.epochs < 0 || w.holdout_entries < 0)
+    throw Error(PCAONE_E_ARG, "invalid warm-start parameters");
+  build_missing(c);
+  ensure_buckets(c);
+  if (!c.net) c.net.reset(new mlp::Net(c.stream));
+  mlp::Net& net = *c.net;
+  net.init(w.seed);
+  const int32_t* perm = c.permuted ? c.perm.p : nullptr;
+  c.smiss.ensure(c.N, c.stream, false);
+  mlp::sample_missing(c.bk_ptr.p, c.bk_nwin, c.N, c.M, c.smiss.p, c.stream);
+  mlp::FeatureArgs fa{c.bed.p, c.stride, c.M, c.N, perm, c.F.p, c.U.p, c.V.p, c.smiss.p, c.counts.p, c.k,
+                      std::min(c.k, 14), std::sqrt((double)c.N), std::sqrt((double)c.M)};
+  const int T = (w.train_entries / w.batch) * w.batch, Hn = w.holdout_entries;
+  if (T <= 0) throw Error(PCAONE_E_ARG, "warm start: fewer training genotypes than one batch");
+  const int D = T + Hn;
+  c.wpos.ensure(D, c.stream, false);
+  c.wsmp.ensure(D, c.stream, false);
+  c.wX.ensure((size_t)D * mlp::kIn, c.stream, false);
+  c.wy.ensure(D, c.stream, false);
+  mlp::draw_observed(c.view(), perm, w.seed ^ 0x5eedULL, D, c.wpos.p, c.wsmp.p, c.stream);
+  mlp::features(fa, c.wpos.p, c.wsmp.p, D, c.wX.p, c.wy.p, c.stream);
+  double last = 0.0;
+  for (int e = 0; e < w.epochs; ++e) {
+    double sum = 0.0;
+    for (int b0 = 0; b0 < T; b0 += w.batch) {
+      net.forward(c.wX.p + (size_t)b0 * mlp::kIn, w.batch, true);
+      net.backward(c.wX.p + (size_t)b0 * mlp::kIn, c.wy.p + b0, w.batch);
+      net.adam(w.lr);
+      if (e + 1 == w.epochs) sum += net.loss_host();
+    }
+    last = sum / T;
+  }
+  // held-out error of the network and of the mean fill (prediction 0)
+  double mse = 0.0, mse0 = 0.0;
+  if (Hn > 0) {
+    std::vector<float> out(Hn), y(Hn);
+    for (int b0 = 0; b0 < Hn; b0 += w.batch) {
+      const int nb = std::min(w.batch, Hn - b0);
+      net.forward(c.wX.p + (size_t)(T + b0) * mlp::kIn, nb, false);
+      PCAONE_CUDA(cudaMemcpyAsync(out.data() + b0, net.out(), nb * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+    }
+    PCAONE_CUDA(cudaMemcpyAsync(y.data(), c.wy.p + T, Hn * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+    for (int r = 0; r < Hn; ++r) {
+      mse += ((double)out[r] - y[r]) * ((double)out[r] - y[r]);
+      mse0 += (double)y[r] * y[r];
+    }
+    mse /= Hn;
+    mse0 /= Hn;
+  }
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  const auto t1 = clk::now();
+  // fill the missing genotypes: CSR by position (G side) and buckets (H side)
+  c.bk_value.ensure((size_t)std::max<int64_t>(1, c.nnz), c.stream, false);
+  const int chunk = 65536;
+  c.wX.ensure(std::max((size_t)D * mlp::kIn, (size_t)chunk * mlp::kIn), c.stream, false);
+  for (int pass = 0; pass < 2; ++pass) {
+    const int32_t* ppos = pass == 0 ? c.miss_pos.p : c.bk_pos.p;
+    const int32_t* psmp = pass == 0 ? c.miss_sample.p : c.bk_sample.p;
+    double* val = pass == 0 ? c.miss_value.p : c.bk_value.p;
+    for (int64_t e0 = 0; e0 < c.nnz; e0 += chunk) {
+      const int nb = (int)std::min<int64_t>(chunk, c.nnz - e0);
+      mlp::features(fa, ppos + e0, psmp + e0, nb, c.wX.p, nullptr, c.stream);
+      net.forward(c.wX.p, nb, false);
+      mlp::fill(net.out(), ppos + e0, perm, c.F.p, nb, val + e0, c.stream);
+    }
+  }
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  c.fitted = true;
+  c.prefilled = true;
+  c.bk_stale = false;
+  c.warm_stats[0] = last;
+  c.warm_stats[1] = mse;
+  c.warm_stats[2] = mse0;
+  c.warm_stats[3] = secs(t0, t1);
+  c.warm_stats[4] = secs(t1, clk::now());
+  c.warm_stats[5] = 2.0 * (double)c.nnz;
+}
+
 static int run_halko(Context& c, const pcaone_gpu_params& p) {
   op_init(c, p);
   int em_iters = 0;
@@ -971,6 +1075,9 @@ static int run_halko(Context& c, const pcaone_gpu_params& p) {
   c.standardize = false;
   compute_usv(c, p.maxp, p.tol);
   flip_uv(c);
+  c.prefilled = false;
+  ensure_missing_total(c);
+  if (c.warm.enable && c.counts_total_missing > 0 && p.maxiter > 0) warm_start(c);
   for (int it = 0; it < p.maxiter; ++it) {
     c.update = true;
     c.standardize = false;
@@ -1249,6 +1356,67 @@ int pcaone_gpu_run_halko(pcaone_gpu_ctx* ctx, const pcaone_gpu_params* params, d
     pcaone::outputs(c, U, S, V);
     c.t_total = pcaone::secs(t0, pcaone::clk::now());
   });
+}
+
+void pcaone_gpu_mlp_default_params(pcaone_gpu_mlp_params* p) {
+  if (!p) return;
+  p->enable = 1;
+  p->train_entries = 524288;
+  p->holdout_entries = 65536;
+  p->epochs = 4;
+  p->batch = 4096;
+  p->lr = 1e-3f;
+  p->seed = 20251;
+}
+
+int pcaone_gpu_set_warm_start(pcaone_gpu_ctx* ctx, const pcaone_gpu_mlp_params* p) {
+  return guarded(ctx, [&](Context& c) {
+    if (!p || !p->enable) {
+      c.warm = pcaone_gpu_mlp_params{};
+      return;
+    }
+    if (p->train_entries < p->batch || p->batch <= 0 || p->epochs < 0 || p->holdout_entries < 0 || !(p->lr > 0.f))
+      throw Error(PCAONE_E_ARG, "invalid warm-start parameters");
+    c.warm = *p;
+  });
+}
+
+int pcaone_gpu_mlp_stats(pcaone_gpu_ctx* ctx, double out[6]) {
+  return guarded(ctx, [&](Context& c) {
+    if (!out) throw Error(PCAONE_E_ARG, "null output");
+    for (int i = 0; i < 6; ++i) out[i] = c.warm_stats[i];
+  });
+}
+
+int pcaone_gpu_mlp_forward_backward(int device, const float* X, const float* y, int B, const float* params,
+                                    float* out, float* loss, float* grads) {
+  if (!X || !y || !params || !out || !loss || !grads || B <= 0) return PCAONE_E_ARG;
+  cudaStream_t s = nullptr;
+  try {
+    PCAONE_CUDA(cudaSetDevice(device));
+    PCAONE_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    {
+      pcaone::mlp::Net net(s);
+      net.set_params(params);
+      net.ensure_batch(B);
+      PCAONE_CUDA(cudaMemcpyAsync(net.X(), X, (size_t)B * pcaone::mlp::kIn * sizeof(float), cudaMemcpyHostToDevice, s));
+      PCAONE_CUDA(cudaMemcpyAsync(net.y(), y, (size_t)B * sizeof(float), cudaMemcpyHostToDevice, s));
+      net.forward(net.X(), B, true);
+      net.backward(net.X(), net.y(), B);
+      PCAONE_CUDA(cudaMemcpyAsync(out, net.out(), (size_t)B * sizeof(float), cudaMemcpyDeviceToHost, s));
+      PCAONE_CUDA(cudaMemcpyAsync(grads, net.grad(), (size_t)pcaone::mlp::kParams * sizeof(float),
+                                  cudaMemcpyDeviceToHost, s));
+      *loss = net.loss_host() / (float)B;
+    }
+    cudaStreamDestroy(s);
+    return PCAONE_OK;
+  } catch (const Error& e) {
+    if (s) cudaStreamDestroy(s);
+    return e.code;
+  } catch (const std::exception&) {
+    if (s) cudaStreamDestroy(s);
+    return PCAONE_E_ARG;
+  }
 }
 
 int pcaone_gpu_get_perm(pcaone_gpu_ctx* ctx, int32_t* perm) {

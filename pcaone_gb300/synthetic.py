@@ -224,8 +224,10 @@ WORKLOADS = {
     # (1.56 GB packed) for profiling captures of single window launches
     "c2p": dict(nsamples=100_000, nsnps=62_500, npop=5, fst=[0.01, 0.02, 0.05, 0.1, 0.2],
                 anc="uniform", anc_range=(0.01, 0.5), mcar=0.005, k=20, p=20, maxp=6, bands=8),
+    # EM imputation (-d 2 -S: no shuffle, the reference's shuffled EMU path has a defect)
     "c4": dict(nsamples=50_000, nsnps=300_000, npop=4, fst=0.05, anc="uniform", anc_range=(0.05, 0.5),
-               miss_sample_beta=(1, 20), miss_snp_beta=(1, 50), k=10, p=10, maxp=6, bands=64),
+               miss_sample_beta=(1, 20), miss_snp_beta=(1, 50), k=10, p=10, maxp=6, bands=64,
+               emu=True, tolem=1e-6, maxiter=100, perm=0),
 }
 
 
