@@ -137,6 +137,24 @@ int pcaone_gpu_load_bed(pcaone_gpu_ctx* ctx, const uint8_t* packed, uint64_t nsn
  * magic like src/FilePlink.hpp:24-27 and the size like FilePlink.cpp:125-126. */
 int pcaone_gpu_load_bed_file_image(pcaone_gpu_ctx* ctx, const uint8_t* image, uint64_t image_bytes,
                                    uint64_t nsnps, uint32_t nsamples);
+/* Dense input: the FileBinary matrix (FileBin, src/FileBinary.hpp:7-40,
+ * src/FileBinary.cpp:54-64): values of nsnps rows x nsamples (host float32,
+ * row by SNP), held on the device as FP16 (the storage of imputed dosages;
+ * values that are not FP16 numbers are rounded to the nearest one) and
+ * centred per SNP by the mean of the stored values.  The reference runs this
+ * input with -C 0 (no standardisation).  Dense input runs in the tensor-core
+ * form, without EM; pcaone_gpu_counts, pcaone_gpu_get_bed and the matvec
+ * return PCAONE_E_ARG for it. */
+int pcaone_gpu_load_dense(pcaone_gpu_ctx* ctx, const float* values, uint64_t nsnps, uint32_t nsamples);
+/* Same from the bytes of a FileBinary file: uint32 SNPs, uint32 samples, then
+ * the float32 rows (values 4-byte aligned in memory). */
+int pcaone_gpu_load_binary_file_image(pcaone_gpu_ctx* ctx, const uint8_t* image, uint64_t image_bytes);
+/* Test and benchmark input: continuous dosages (allele count plus N(0, sd^2)
+ * noise, clipped to [0, 2], as FP16) of the seeded model of
+ * pcaone_gb300/synthetic.py (sample_dosages), generated on the device (host
+ * arrays freq nsnps x npop, weights nsamples x npop). */
+int pcaone_gpu_load_synthetic_dense(pcaone_gpu_ctx* ctx, uint64_t nsnps, uint32_t nsamples, int npop,
+                                    const double* freq, const double* weights, double sd, uint64_t seed);
 /* Same, from device memory already holding the packed rows (row pitch
  * src_pitch bytes). */
 int pcaone_gpu_load_bed_device(pcaone_gpu_ctx* ctx, const void* dev_packed, uint64_t src_pitch,

@@ -187,8 +187,34 @@ class OracleData:
         # feed the reference's own Omega into the restatement)
         self.omega0 = None if omega0 is None else np.asfortranarray(omega0, dtype=np.float64)
 
+    @classmethod
+    def from_dense(cls, values: np.ndarray, *, perm: bool = False, seed: int = 112, bands: int = 64,
+                   rand: int = 1, svd_t: int = 2, omega0: Optional[np.ndarray] = None) -> "OracleData":
+        """FileBinary input (src/FileBinary.cpp:54-64): values M x N (float32
+        as read), each SNP centred by its mean in float64; run with -C 0, so
+        standardize_E does nothing (src/Data.cpp:353)."""
+        self = cls.__new__(cls)
+        v = np.asarray(values, dtype=np.float32)
+        self.nsnps, self.nsamples = int(v.shape[0]), int(v.shape[1])
+        self.counts = None
+        self.F = None
+        G = v.T.astype(np.float64)
+        self.G = np.asfortranarray(G - G.mean(axis=0)[None, :])
+        self.C = np.zeros((self.nsnps, self.nsamples), dtype=bool)
+        self.emu = self.missme = False
+        self.perm = perm
+        self.perm_idx = None
+        self.seed, self.bands, self.rand, self.ploidy = seed, bands, rand, 2
+        self.svd_t = svd_t
+        self.mev = True
+        self.omega0 = None if omega0 is None else np.asfortranarray(omega0, dtype=np.float64)
+        return self
+
     def standardize_E(self) -> None:
-        """src/Data.cpp:351-362: column i scaled with F(i) (column order as is)."""
+        """src/Data.cpp:351-362: column i scaled with F(i) (column order as is);
+        nothing for FileBinary input run with -C 0."""
+        if self.F is None:
+            return
         self.G *= standardize_scale(self.F, self.ploidy)[None, :]
 
     def fit_with_pi(self, U: np.ndarray, S: np.ndarray, VT: np.ndarray) -> None:

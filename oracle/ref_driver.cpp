@@ -5,9 +5,10 @@
 // (the reference's text writers keep 6 significant digits, src/Data.cpp:215).
 //
 // usage: ref_driver OUTDIR <PCAone command-line options, e.g. -b prefix -k 10 -d 2>
+//        (PLINK -b input, or FileBinary -B input with -C 0)
 //
 // Outputs (numpy .npy, float64 column-major / int64):
-//   F.npy         allele frequencies after the AF pass (src/FilePlink.cpp:33-62)
+//   F.npy         allele frequencies after the AF pass (src/FilePlink.cpp:33-62; PLINK only)
 //   U.npy S.npy V.npy   final operator state (src/Halko.cpp:46-97)
 //   perm.npy      the in-core column permutation (src/RSVD.hpp:61-78), if any
 //   Omg0.npy      the initial random test matrix (src/Halko.cpp:15-23)
@@ -20,6 +21,7 @@
 #include <string>
 #include <vector>
 
+#include "FileBinary.hpp"
 #include "FilePlink.hpp"
 #include "Halko.hpp"
 #include "Utils.hpp"
@@ -77,13 +79,13 @@ int main(int argc, char** argv) {
   Param params((int)args.size(), args.data());
   cao.cao.open(outdir + "/ref.log");
   cao.is_screen = false;
-  if (params.file_t != FileType::PLINK) {
-    std::fprintf(stderr, "only PLINK input is driven here\n");
+  if (params.file_t != FileType::PLINK && params.file_t != FileType::BINARY) {
+    std::fprintf(stderr, "only PLINK and binary input are driven here\n");
     return 2;
   }
-  Data* data = new FileBed(params);
+  Data* data = params.file_t == FileType::PLINK ? (Data*)new FileBed(params) : (Data*)new FileBin(params);
   data->prepare();
-  dump1(outdir, "F", data->F);
+  if (params.file_t == FileType::PLINK) dump1(outdir, "F", data->F);
   if (dump_g0) dump(outdir, "G0", data->G);
 
   // operator selection and call sequence of run_pca_with_halko (src/Halko.cpp:271-320)

@@ -31,7 +31,8 @@ EXPORTS = [
     "pcaone_gpu_get_perm", "pcaone_gpu_matvec", "pcaone_gpu_load_synthetic", "pcaone_gpu_get_bed",
     "pcaone_gpu_set_profiling", "pcaone_gpu_kernel_stats", "pcaone_gpu_launch_count",
     "pcaone_gpu_matvec_static", "pcaone_gpu_mlp_default_params", "pcaone_gpu_set_warm_start",
-    "pcaone_gpu_mlp_stats", "pcaone_gpu_mlp_forward_backward",
+    "pcaone_gpu_mlp_stats", "pcaone_gpu_mlp_forward_backward", "pcaone_gpu_load_dense",
+    "pcaone_gpu_load_binary_file_image", "pcaone_gpu_load_synthetic_dense",
 ]
 MLP_PARAMS, MLP_INPUTS = 82689, 64
 
@@ -98,6 +99,10 @@ def load(path: str = LIBPATH) -> ctypes.CDLL:
     lib.pcaone_gpu_launch_count.argtypes = []
     lib.pcaone_gpu_matvec_static.argtypes = [c_void_p, c_uint64, c_uint64, c_uint32, c_void_p, c_int, c_void_p,
                                              c_void_p, c_void_p]
+    lib.pcaone_gpu_load_dense.argtypes = [c_void_p, c_void_p, c_uint64, c_uint32]
+    lib.pcaone_gpu_load_binary_file_image.argtypes = [c_void_p, c_void_p, c_uint64]
+    lib.pcaone_gpu_load_synthetic_dense.argtypes = [c_void_p, c_uint64, c_uint32, c_int, c_void_p, c_void_p,
+                                                    c_double, c_uint64]
     lib.pcaone_gpu_mlp_default_params.argtypes = [P(MlpParams)]
     lib.pcaone_gpu_mlp_default_params.restype = None
     lib.pcaone_gpu_set_warm_start.argtypes = [c_void_p, P(MlpParams)]
@@ -278,6 +283,26 @@ class Context:
         self._check(self.lib.pcaone_gpu_run_halko(self.h, ctypes.byref(params), _ptr(U), _ptr(S),
                                                   _ptr(V) if want_v else None, ctypes.byref(it)))
         return U, S, (V if want_v else None), it.value
+
+    def load_dense(self, values: np.ndarray):
+        """FileBinary matrix (SNPs x samples), held as FP16 on the device."""
+        v = np.ascontiguousarray(values, dtype=np.float32)
+        self._check(self.lib.pcaone_gpu_load_dense(self.h, v.ctypes.data, v.shape[0], v.shape[1]))
+        self.nsnps, self.nsamples = v.shape
+
+    def load_synthetic_dense(self, model, sd: float = 0.1):
+        """Continuous dosages of ``model`` generated on the device (FP16)."""
+        fr = np.ascontiguousarray(model.freq, dtype=np.float64)
+        w = np.ascontiguousarray(model.weights, dtype=np.float64)
+        self._check(self.lib.pcaone_gpu_load_synthetic_dense(self.h, model.nsnps, model.nsamples, model.npop,
+                                                             _ptr(fr), _ptr(w), float(sd), model.seed))
+        self.nsnps, self.nsamples = model.nsnps, model.nsamples
+
+    def load_binary_file_image(self, image: bytes):
+        buf = np.frombuffer(image, dtype=np.uint8)
+        self._check(self.lib.pcaone_gpu_load_binary_file_image(self.h, buf.ctypes.data, buf.size))
+        m, n = np.frombuffer(image[:8], dtype=np.uint32)
+        self.nsnps, self.nsamples = int(m), int(n)
 
     def set_warm_start(self, p):
         """Learned EM warm start for the next run_halko calls (None disables)."""

@@ -1,8 +1,11 @@
 // PLINK 2-bit genotype kernels: padding sanitation, integer counts and allele
-// frequency, per-SNP decode tables, and the synthetic-genotype generator.
+// frequency, per-SNP decode tables, and the synthetic-genotype generator; and
+// the conversion of dense (FileBinary) rows to FP16 with their means.
 //
 // Code map (reference src/Common.hpp:50-59, BED2GENO = {1, -9, 0.5, 0} on the
 // g/2 scale):  00 two copies of A1, 01 missing, 10 one copy, 11 no copy.
+#include <cuda_fp16.h>
+
 #include "internal.cuh"
 
 namespace pcaone {
@@ -170,6 +173,86 @@ void launch_synth(uint8_t* bed, int64_t stride, int64_t snp0, int64_t nsnps, int
   if (total == 0) return;
   k_synth<<<ceil_div(total, 256), 256, 0, s>>>(bed, stride, snp0, nsnps, nsamples, npop, freq, weights,
                                                  miss_sample, miss_snp, sa, sb, sm);
+  PCAONE_LAUNCH_CHECK();
+}
+
+namespace {
+
+// One warp per row: float32 values -> FP16 (round to nearest) in a row of
+// npad values (zeros past N), and the row's mean of the FP16 values, exact up
+// to the final division: every FP16 value is an integer multiple of 2^-24, so
+// the row sum is an exact int64 of units 2^-24 (rows of |values| <= 65504 and
+// N <= 2^23).
+__global__ void k_dense_rows(const float* __restrict__ src, int64_t nrows, int N, int npad,
+                             __half* __restrict__ dst, double* __restrict__ mean) {
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= nrows) return;
+  const float* row = src + r * N;
+  __half* out = dst + r * npad;
+  long long sum = 0;
+  for (int i = lane; i < npad; i += 32) {
+    const __half h = i < N ? __float2half_rn(row[i]) : __float2half_rn(0.f);
+    out[i] = h;
+    sum += (long long)llrint((double)__half2float(h) * 16777216.0);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) mean[r] = (double)sum / 16777216.0 / (double)N;
+}
+
+}  // namespace
+
+namespace {
+
+// Continuous dosages of the synthetic model (pcaone_gb300/synthetic.py
+// sample_dosages): allele count from the two allele draws plus sd times a
+// Box-Muller normal from two further hashed uniforms, clipped to [0, 2].  The
+// allele draws match the numpy generator bit for bit; the noise uses the
+// device log/cos, so a value can land on the other side of an FP16 rounding
+// boundary than numpy's in rare cases.
+__global__ void k_synth_dense(float* __restrict__ out, int64_t snp0, int64_t nsnps, int nsamples, int npop,
+                              const double* __restrict__ freq, const double* __restrict__ weights, double sd,
+                              uint64_t sa, uint64_t sb, uint64_t s1, uint64_t s2) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= nsnps * nsamples) return;
+  const int64_t jl = idx / nsamples;
+  const int i = (int)(idx - jl * nsamples);
+  const int64_t j = snp0 + jl;
+  double p = 0.0;
+  for (int k = 0; k < npop; ++k) p = __dadd_rn(p, __dmul_rn(weights[(int64_t)i * npop + k], freq[jl * npop + k]));
+  const uint64_t ctr = ((uint64_t)j << 32) | (uint64_t)i;
+  const double d = (double)((u01(ctr, sa) < p) + (u01(ctr, sb) < p));
+  const double z = sqrt(-2.0 * log(fmax(u01(ctr, s1), 1e-300))) * cos(6.283185307179586 * u01(ctr, s2));
+  out[idx] = (float)fmin(fmax(d + sd * z, 0.0), 2.0);
+}
+
+}  // namespace
+
+void launch_synth_dense(float* out, int64_t snp0, int64_t nsnps, int nsamples, int npop, const double* freq,
+                        const double* weights, double sd, uint64_t seed, cudaStream_t s) {
+  auto host_mix = [](uint64_t x) {
+    uint64_t z = x + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  // stream keys as in pcaone_gb300/synthetic.py (KEY_ALLELE_A, KEY_ALLELE_B, KEY_DOSAGE_NOISE, +1)
+  const uint64_t base = seed * 0x2545F4914F6CDD1Dull;
+  const uint64_t sa = host_mix(base + 0x243F6A8885A308D3ull);
+  const uint64_t sb = host_mix(base + 0x13198A2E03707344ull);
+  const uint64_t s1 = host_mix(base + 0xD05Eull);
+  const uint64_t s2 = host_mix(base + 0xD05Full);
+  const int64_t total = nsnps * nsamples;
+  if (total == 0) return;
+  k_synth_dense<<<ceil_div(total, 256), 256, 0, s>>>(out, snp0, nsnps, nsamples, npop, freq, weights, sd, sa, sb,
+                                                     s1, s2);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_dense_rows(const float* src, int64_t nrows, int N, int npad, uint8_t* dst, double* mean, cudaStream_t s) {
+  if (nrows == 0) return;
+  k_dense_rows<<<ceil_div(nrows * 32, 256), 256, 0, s>>>(src, nrows, N, npad, reinterpret_cast<__half*>(dst), mean);
   PCAONE_LAUNCH_CHECK();
 }
 

@@ -71,6 +71,9 @@ struct Context {
   int64_t M = 0;
   int64_t stride = 0;
   bool have_data = false;
+  // dense input (FileBinary values as FP16, rows of npad values): `bed` holds the
+  // FP16 rows (stride = 2 npad bytes), F the per-SNP means
+  bool dense = false;
   DBuf<uint8_t> bed;
   DBuf<int32_t> counts;
   DBuf<double> F;
@@ -189,14 +192,15 @@ struct Context {
 // ------------------------------------------------------------------------
 // data
 // ------------------------------------------------------------------------
-static void load_common(Context& c, uint64_t nsnps, uint32_t nsamples) {
+static void load_common(Context& c, uint64_t nsnps, uint32_t nsamples, bool dense = false) {
   if (nsamples == 0 || nsnps == 0) throw Error(PCAONE_E_ARG, "empty genotype matrix");
   if (nsnps > 0x7fffffffull) throw Error(PCAONE_E_LIMIT, "more than 2^31-1 SNPs");
   if (nsamples > 0x7fffff00u) throw Error(PCAONE_E_LIMIT, "too many samples");
   c.N = (int)nsamples;
   c.M = (int64_t)nsnps;
   c.npad = round_up(c.N, 128);
-  c.stride = c.npad / 4;
+  c.dense = dense;
+  c.stride = dense ? (int64_t)c.npad * 2 : c.npad / 4;
   c.bed.ensure((size_t)c.M * c.stride, c.stream, true);
   c.counts.ensure((size_t)c.M * 4, c.stream, false);
   c.F.ensure((size_t)c.M, c.stream, false);
@@ -265,8 +269,59 @@ static void load_synthetic(Context& c, uint64_t nsnps, uint32_t nsamples, int np
   finish_load(c);
 }
 
+// FileBinary values (src/FileBinary.cpp:54-64): float32 SNP rows, held as FP16
+// (the storage of imputed dosages); each SNP is centred by the mean of its
+// stored values, computed exactly (int64 sums of value * 2^24).
+static void load_dense(Context& c, const float* values, uint64_t nsnps, uint32_t nsamples) {
+  if (!values) throw Error(PCAONE_E_ARG, "null values");
+  load_common(c, nsnps, nsamples, true);
+  c.counts_host.assign((size_t)c.M * 4, 0);
+  c.counts_total_missing = 0;
+  const int64_t rows_per = std::max<int64_t>(1, (int64_t)(64u << 20) / ((int64_t)nsamples * 4));
+  DBuf<float> stage;
+  stage.ensure((size_t)std::min<int64_t>(rows_per, c.M) * nsamples, c.stream, false);
+  for (int64_t j0 = 0; j0 < c.M; j0 += rows_per) {
+    const int64_t n = std::min<int64_t>(rows_per, c.M - j0);
+    PCAONE_CUDA(cudaMemcpyAsync(stage.p, values + (size_t)j0 * nsamples, (size_t)n * nsamples * sizeof(float),
+                                cudaMemcpyHostToDevice, c.stream));
+    launch_dense_rows(stage.p, n, (int)nsamples, c.npad, c.bed.p + j0 * c.stride, c.F.p + j0, c.stream);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  }
+  c.have_data = true;
+}
+
+// synthetic continuous dosages of the seeded model (pcaone_gb300/synthetic.py
+// sample_dosages), generated on the device and held like load_dense
+static void load_synthetic_dense(Context& c, uint64_t nsnps, uint32_t nsamples, int npop, const double* freq,
+                                 const double* weights, double sd, uint64_t seed) {
+  if (npop <= 0 || !freq || !weights || !(sd >= 0.0)) throw Error(PCAONE_E_ARG, "bad model arrays");
+  load_common(c, nsnps, nsamples, true);
+  c.counts_host.assign((size_t)c.M * 4, 0);
+  c.counts_total_missing = 0;
+  DBuf<double> dw, dfreq;
+  DBuf<float> stage;
+  dw.ensure((size_t)nsamples * npop, c.stream, false);
+  PCAONE_CUDA(cudaMemcpyAsync(dw.p, weights, (size_t)nsamples * npop * 8, cudaMemcpyHostToDevice, c.stream));
+  const int64_t chunk = std::max<int64_t>(1, (int64_t)(256u << 20) / ((int64_t)nsamples * 4));
+  const int64_t rows = std::min<int64_t>(chunk, (int64_t)nsnps);
+  dfreq.ensure((size_t)rows * npop, c.stream, false);
+  stage.ensure((size_t)rows * nsamples, c.stream, false);
+  for (int64_t j0 = 0; j0 < (int64_t)nsnps; j0 += chunk) {
+    const int64_t n = std::min<int64_t>(chunk, (int64_t)nsnps - j0);
+    PCAONE_CUDA(cudaMemcpyAsync(dfreq.p, freq + j0 * npop, (size_t)n * npop * 8, cudaMemcpyHostToDevice, c.stream));
+    launch_synth_dense(stage.p, j0, n, (int)nsamples, npop, dfreq.p, dw.p, sd, seed, c.stream);
+    launch_dense_rows(stage.p, n, (int)nsamples, c.npad, c.bed.p + j0 * c.stride, c.F.p + j0, c.stream);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  }
+  c.have_data = true;
+}
+
 static void need_data(const Context& c) {
   if (!c.have_data) throw Error(PCAONE_E_ARG, "no genotype data loaded");
+}
+static void need_plink(const Context& c) {
+  need_data(c);
+  if (c.dense) throw Error(PCAONE_E_ARG, "not available for dense (FileBinary) input");
 }
 static void need_op(const Context& c) {
   need_data(c);
@@ -288,10 +343,19 @@ static void upload_omega0(Context& c) {
 // tensor-core buffers, launch shapes and TMA descriptors for windows of up to
 // `win` SNPs
 static void tc_make_bed_maps(Context& c) {
-  tc::make_map_2d(&c.map_bed_g, c.bed_work, false, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 16, 128,
-                  false);
-  tc::make_map_2d(&c.map_bed_h, c.bed_work, false, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 32, 64,
-                  false);
+  if (c.dense) {
+    // FP16 rows: G tiles of 64 samples x 128 SNPs (128-byte swizzle), H tiles
+    // of 128 samples x 64 SNPs
+    tc::make_map_2d(&c.map_bed_g, c.bed_work, tc::kMapF16, (uint64_t)c.npad, (uint64_t)c.M, (uint64_t)c.stride, 64,
+                    128, true);
+    tc::make_map_2d(&c.map_bed_h, c.bed_work, tc::kMapF16, (uint64_t)c.npad, (uint64_t)c.M, (uint64_t)c.stride, 128,
+                    64, false);
+    return;
+  }
+  tc::make_map_2d(&c.map_bed_g, c.bed_work, tc::kMapU8, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 16,
+                  128, false);
+  tc::make_map_2d(&c.map_bed_h, c.bed_work, tc::kMapU8, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 32,
+                  64, false);
 }
 
 static void tc_shapes(int win, int npad, int& chunk, int& nchunks, int& per_split, int& nsplit) {
@@ -343,8 +407,9 @@ static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
   c.hpart.ensure(std::max(need_hpart, c.hpart.n), c.stream, false);
   c.bed_work = c.bed.p;
   tc_make_bed_maps(c);
-  tc::make_map_2d(&c.map_w, c.wsl.p, true, (uint64_t)c.npad, (uint64_t)3 * LP, (uint64_t)c.npad * 2, 64, LP, true);
-  tc::make_map_2d(&c.map_gt, c.gt.p, true, (uint64_t)c.ldg, (uint64_t)3 * LP, (uint64_t)c.ldg * 2, 64, LP, true);
+  const int sl = c.dense ? tc::kMapF16 : tc::kMapBF16;  // slice digits: FP16 for dense input, else BF16
+  tc::make_map_2d(&c.map_w, c.wsl.p, sl, (uint64_t)c.npad, (uint64_t)3 * LP, (uint64_t)c.npad * 2, 64, LP, true);
+  tc::make_map_2d(&c.map_gt, c.gt.p, sl, (uint64_t)c.ldg, (uint64_t)3 * LP, (uint64_t)c.ldg * 2, 64, LP, true);
   c.w_slices = 0;
 }
 
@@ -359,6 +424,9 @@ static void op_init(Context& c, const pcaone_gpu_params& p) {
     throw Error(PCAONE_E_ARG, "the -w/--batches must be a power of 2 and the minimun is 4.");
   if (p.precision != PCAONE_PREC_FP32 && p.precision != PCAONE_PREC_BF16 && p.precision != PCAONE_PREC_BF16X3)
     throw Error(PCAONE_E_ARG, "precision form not available in this build of the operator");
+  if (c.dense && p.precision == PCAONE_PREC_FP32)
+    throw Error(PCAONE_E_ARG, "dense (FileBinary) input runs in the tensor-core form only");
+  if (c.dense && p.emu) throw Error(PCAONE_E_ARG, "EM imputation needs PLINK input (no missing genotypes in dense input)");
   c.P = p;
   c.k = p.k;
   c.L = L;
@@ -632,7 +700,9 @@ static void prepare_epoch0(Context& c, bool window) {
     else
       fit_with_pi(c);
   }
-  if (c.standardize) c.scaled = true;  // Data::standardize_E scales in place, once
+  // Data::standardize_E scales in place, once; FileBinary input runs with
+  // -C 0, where standardize_E does nothing (src/Data.cpp:353)
+  if (c.standardize && !c.dense) c.scaled = true;
   refresh_lut(c);
   if (window) {
     c.bandsize = 1;
@@ -663,7 +733,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   const int LP = c.LP, S = c.nslice_cur;
   if (c.w_slices != S) {
     tc::launch_omega_slices(c.Omg.p, c.npad, c.N, LP, S, c.wsl.p, c.wunit.p, c.colsum.p, c.wexp.p, c.wrep.p,
-                            c.wint.p, c.stream);
+                            c.wint.p, c.dense, c.stream);
     c.w_slices = S;
   }
   int chunk, nch, per, nsp;
@@ -696,11 +766,12 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ga.chunk = chunk;
   ga.npad = c.npad;
   ga.nchunks = nch;
-  ga.nstages = tc::stages_for(LP, S, 128 * 16);
+  ga.nstages = tc::stages_for(LP, S, tc::g_tile_bytes(c.dense));
   ga.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ga.nstages));
   ga.wscale = c.wunit.p;
   ga.part = c.part.p;
   ga.err = c.err.p;
+  ga.dense = c.dense ? 1 : 0;
   mark(0);
   tc::launch_g(c.map_bed_g, c.map_w, ga, c.stream);
   close_mark();
@@ -723,6 +794,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
     launch_seg_gather(sg, c.stream);
   }
   tc::GFinishArgs fa{};
+  fa.vfac = c.dense ? 1.0 : 0.5;
   fa.pos0 = pos0;
   fa.nsnp = (int)n;
   fa.L = c.L;
@@ -756,11 +828,12 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ha.per_split = per;
   ha.nsplit = nsp;
   ha.npad = c.npad;
-  ha.nstages = tc::stages_for(LP, S, 64 * 32);
+  ha.nstages = tc::stages_for(LP, S, tc::h_tile_bytes(c.dense));
   ha.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ha.nstages));
   ha.hscale = c.hunit.p;
   ha.hpart = c.hpart.p;
   ha.err = c.err.p;
+  ha.dense = c.dense ? 1 : 0;
   ha.hisum = any_miss ? c.hisum.p : nullptr;
   ha.gmunit_m = c.gmunit.p + (size_t)(S - 1) * LP;
   ha.hesum = (any_miss && em) ? c.hesum.p : nullptr;
@@ -1102,7 +1175,7 @@ static int run_halko(Context& c, const pcaone_gpu_params& p) {
 }
 
 static void matvec(Context& c, const double* x, double* y, int standardize) {
-  need_data(c);
+  need_plink(c);
   const int N = c.N;
   c.mv_x.ensure(N, c.stream, false);
   c.mv_y.ensure(N, c.stream, false);
@@ -1261,6 +1334,37 @@ int pcaone_gpu_load_bed_file_image(pcaone_gpu_ctx* ctx, const uint8_t* image, ui
   });
 }
 
+int pcaone_gpu_load_dense(pcaone_gpu_ctx* ctx, const float* values, uint64_t nsnps, uint32_t nsamples) {
+  return guarded(ctx, [&](Context& c) {
+    pcaone::load_dense(c, values, nsnps, nsamples);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_load_synthetic_dense(pcaone_gpu_ctx* ctx, uint64_t nsnps, uint32_t nsamples, int npop,
+                                    const double* freq, const double* weights, double sd, uint64_t seed) {
+  return guarded(ctx, [&](Context& c) {
+    pcaone::load_synthetic_dense(c, nsnps, nsamples, npop, freq, weights, sd, seed);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_load_binary_file_image(pcaone_gpu_ctx* ctx, const uint8_t* image, uint64_t image_bytes) {
+  return guarded(ctx, [&](Context& c) {
+    // FileBin (src/FileBinary.hpp:17-18): uint32 SNPs, uint32 samples, float32 rows
+    if (!image || image_bytes < 8) throw Error(PCAONE_E_FORMAT, "truncated binary image");
+    uint32_t hdr[2];
+    std::memcpy(hdr, image, 8);
+    const uint64_t need = 8 + (uint64_t)hdr[0] * hdr[1] * 4;
+    if (image_bytes < need)
+      throw Error(PCAONE_E_FORMAT, "truncated binary file: " + std::to_string(image_bytes) + " bytes, expected " +
+                                       std::to_string(need));
+    if (((uintptr_t)(image + 8) & 3u) != 0) throw Error(PCAONE_E_ARG, "binary image values must be 4-byte aligned");
+    pcaone::load_dense(c, reinterpret_cast<const float*>(image + 8), hdr[0], hdr[1]);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
 int pcaone_gpu_load_bed_device(pcaone_gpu_ctx* ctx, const void* dev_packed, uint64_t src_pitch, uint64_t nsnps,
                                uint32_t nsamples) {
   return guarded(ctx, [&](Context& c) {
@@ -1282,7 +1386,7 @@ int pcaone_gpu_load_synthetic(pcaone_gpu_ctx* ctx, uint64_t nsnps, uint32_t nsam
 
 int pcaone_gpu_get_bed(pcaone_gpu_ctx* ctx, uint8_t* packed) {
   return guarded(ctx, [&](Context& c) {
-    pcaone::need_data(c);
+    pcaone::need_plink(c);
     if (!packed) throw Error(PCAONE_E_ARG, "null buffer");
     const size_t bps = ((size_t)c.N + 3) / 4;
     PCAONE_CUDA(cudaMemcpy2DAsync(packed, bps, c.bed.p, c.stride, bps, c.M, cudaMemcpyDeviceToHost, c.stream));
@@ -1292,7 +1396,7 @@ int pcaone_gpu_get_bed(pcaone_gpu_ctx* ctx, uint8_t* packed) {
 
 int pcaone_gpu_counts(pcaone_gpu_ctx* ctx, int32_t* counts, double* F) {
   return guarded(ctx, [&](Context& c) {
-    pcaone::need_data(c);
+    pcaone::need_plink(c);
     if (counts)
       PCAONE_CUDA(cudaMemcpyAsync(counts, c.counts.p, (size_t)c.M * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost,
                                   c.stream));

@@ -206,6 +206,11 @@ void launch_h_buckets(int64_t win, int N, int L, int LP, const int64_t* ptr, con
                       const int32_t* perm, const double* scale, const float* Rf, int64_t rbase, double* Hx,
                       cudaStream_t s);
 void launch_seg_gather(const SegGatherArgs& a, cudaStream_t s);
+// synthetic continuous dosages of SNPs [snp0, snp0 + nsnps) into out (nsnps x nsamples float32)
+void launch_synth_dense(float* out, int64_t snp0, int64_t nsnps, int nsamples, int npop, const double* freq,
+                        const double* weights, double sd, uint64_t seed, cudaStream_t s);
+// dense rows: float32 -> FP16 rows of npad values (bytes at dst) and the exact row means
+void launch_dense_rows(const float* src, int64_t nrows, int N, int npad, uint8_t* dst, double* mean, cudaStream_t s);
 void launch_flip_uv(double* U, int64_t nrows_u, double* V, int64_t nrows_v, int k, int* flag, cudaStream_t s);
 void launch_transpose_out(const double* A, int64_t rows, int lda, int cols, double* out, cudaStream_t s);
 

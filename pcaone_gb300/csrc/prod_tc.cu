@@ -35,6 +35,13 @@
 //   k_tc_h : tile of 128 samples x one split of the window's SNPs.  TMA brings
 //            the packed tile (64 SNP rows x 32 bytes) and the Gh^T slice tiles;
 //            decoder warps transpose into the D^T A operand.
+//
+// Dense input (FileBinary values held as FP16, src/FileBinary.cpp:54-64): the
+// same kernels with kDense, where the A tile is FP16 values instead of packed
+// codes (copied, or transposed for H, into TMEM), the slices are FP16 integer
+// digits (both operands of kind::f16 FP16), the centring is by the per-SNP
+// mean mu with no scale (x = v - mu), and the FP32 accumulation is ordinary
+// rounding arithmetic since the values are not integers.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -184,9 +191,13 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
   return d;
 }
 
-// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, M x N
+// Instruction descriptor, kind::f16: D FP32, A and B both BF16 (or both FP16),
+// both K-major, M x N
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 
@@ -221,11 +232,13 @@ __host__ __device__ inline SmemLayout layout_for(int LP, int nslice, int pbytes)
 // MMA shape limit for M = 128: N <= 256 columns.
 constexpr int kMaxNTmemA = 256;
 
+template <bool kF16>
 __device__ __forceinline__ void mma_cat(uint32_t tmem_col0, uint32_t a_tmem, uint32_t b_addr, int ncols,
                                         uint32_t accumulate) {
   for (int n0 = 0; n0 < ncols; n0 += kMaxNTmemA) {
     const int n = min(kMaxNTmemA, ncols - n0);
-    mma_bf16_ta(tmem_col0 + n0, a_tmem, desc_sw128(b_addr + n0 * 128), idesc_bf16(128, n), accumulate);
+    mma_bf16_ta(tmem_col0 + n0, a_tmem, desc_sw128(b_addr + n0 * 128), kF16 ? idesc_f16(128, n) : idesc_bf16(128, n),
+                accumulate);
   }
 }
 
@@ -261,8 +274,12 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // ---------------------------------------------------------------------------
 // G product
 // ---------------------------------------------------------------------------
+template <bool kDense>
 __global__ void __launch_bounds__(kThreads, 1)
     k_tc_g(const __grid_constant__ CUtensorMap map_bed, const __grid_constant__ CUtensorMap map_w, GArgs a) {
+  // A tile per stage: 128 SNP rows x 64 samples, packed (16 B per row) or FP16
+  // (128 B per row, 128-byte swizzle)
+  constexpr int kTileBytes = kDense ? 128 * 128 : 128 * 16;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   __shared__ uint64_t full_bar[kMaxStages], dec_bar[kMaxStages], empty_bar[kMaxStages], acc_bar;
@@ -271,7 +288,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ float unit[3 * 112];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int LP = a.LP, S = a.nslice;
-  const SmemLayout lay = layout_for(LP, S, 128 * 16);
+  const SmemLayout lay = layout_for(LP, S, kTileBytes);
   const int row0 = blockIdx.x * 128;                  // window-local first SNP of the tile
   const int kbeg = blockIdx.y * a.chunk;
   const int kend = min(kbeg + a.chunk, a.npad);
@@ -302,19 +319,20 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     // ---- TMA producer ----
     if (lane == 0) {
-      const uint32_t tx_bytes = 128 * 16 + (uint32_t)(ncat * 128);
+      const uint32_t tx_bytes = kTileBytes + (uint32_t)(ncat * 128);
+      const int kdiv = kDense ? 0 : 2;  // inner TMA coordinate: samples, or packed bytes
       int issued = 0;
       for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
-        tma_prefetch_2d(&map_bed, (kbeg + kb * kStepK) >> 2, (int)(a.pos0 + row0));
+        tma_prefetch_2d(&map_bed, (kbeg + kb * kStepK) >> kdiv, (int)(a.pos0 + row0));
       for (int kb = 0; kb < nk; ++kb) {
         const int st = kb % nst;
         if (kb + kPrefetchSteps < nk)
-          tma_prefetch_2d(&map_bed, (kbeg + (kb + kPrefetchSteps) * kStepK) >> 2, (int)(a.pos0 + row0));
+          tma_prefetch_2d(&map_bed, (kbeg + (kb + kPrefetchSteps) * kStepK) >> kdiv, (int)(a.pos0 + row0));
         if (kb >= nst && !role_wait(&empty_bar[st], (uint32_t)(kb / nst - 1) & 1u, &abort_sh)) break;
         uint8_t* base = smem + st * lay.stage_bytes;
         const int k0 = kbeg + kb * kStepK;
         mbar_expect_tx(&full_bar[st], tx_bytes);
-        tma_load_2d(base + lay.p, &map_bed, k0 >> 2, (int)(a.pos0 + row0), &full_bar[st]);
+        tma_load_2d(base + lay.p, &map_bed, k0 >> kdiv, (int)(a.pos0 + row0), &full_bar[st]);
         for (int s = 0; s < S; ++s) tma_load_2d(base + lay.b + s * LP * 128, &map_w, k0, s * LP, &full_bar[st]);
         issued = kb + 1;
       }
@@ -333,7 +351,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t bb = smem_u32(base + lay.b);
         const uint32_t ad = tmem + a_col0 + st * 32;
 #pragma unroll
-        for (int kk = 0; kk < kStepK / 16; ++kk) mma_cat(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
+        for (int kk = 0; kk < kStepK / 16; ++kk) mma_cat<kDense>(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
         mma_commit(&empty_bar[st]);
       }
       mma_commit(&acc_bar);  // arrives once every MMA above has completed
@@ -349,13 +367,28 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int st = kb % nst;
       if (!role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
       uint8_t* base = smem + st * lay.stage_bytes;
-      const uint2 pk = *reinterpret_cast<const uint2*>(base + lay.p + r * 16 + ch * 8);
       uint32_t wd[16];
+      if (kDense) {
+        // row r holds 8 chunks of 16 B (8 FP16 values each), chunk c stored at
+        // position c ^ (r & 7) by the 128-byte swizzle; this thread takes
+        // chunks 4ch .. 4ch+3 (samples 32ch .. 32ch+31)
 #pragma unroll
-      for (int e = 0; e < 16; ++e) {
-        const uint32_t w32 = e < 8 ? pk.x : pk.y;
-        const int sh = 4 * (e & 7);
-        wd[e] = dosage_pair(((w32 >> sh) & 3u) | (((w32 >> (sh + 2)) & 3u) << 16));
+        for (int q = 0; q < 4; ++q) {
+          const int cpos = (ch * 4 + q) ^ (r & 7);
+          const uint4 v = *reinterpret_cast<const uint4*>(base + lay.p + r * 128 + cpos * 16);
+          wd[4 * q] = v.x;
+          wd[4 * q + 1] = v.y;
+          wd[4 * q + 2] = v.z;
+          wd[4 * q + 3] = v.w;
+        }
+      } else {
+        const uint2 pk = *reinterpret_cast<const uint2*>(base + lay.p + r * 16 + ch * 8);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          const uint32_t w32 = e < 8 ? pk.x : pk.y;
+          const int sh = 4 * (e & 7);
+          wd[e] = dosage_pair(((w32 >> sh) & 3u) | (((w32 >> (sh + 2)) & 3u) << 16));
+        }
       }
       tmem_st16(tmem + lane_off + a_col0 + st * 32 + ch * 16, wd);
       tmem_wait_st();
@@ -396,8 +429,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 // ---------------------------------------------------------------------------
 // H product
 // ---------------------------------------------------------------------------
+template <bool kDense>
 __global__ void __launch_bounds__(kThreads, 1)
     k_tc_h(const __grid_constant__ CUtensorMap map_bed, const __grid_constant__ CUtensorMap map_g, HArgs a) {
+  // A tile per stage: 64 SNP rows x 128 samples, packed (32 B per row) or FP16
+  // (256 B per row, unswizzled)
+  constexpr int kRowBytes = kDense ? 256 : 32;
+  constexpr int kTileBytes = 64 * kRowBytes;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   __shared__ uint64_t full_bar[kMaxStages], dec_bar[kMaxStages], empty_bar[kMaxStages], acc_bar;
@@ -407,7 +445,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ float munit[2 * 112];  // units of the missing-entry sums (Gm integers, EM products)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int LP = a.LP, S = a.nslice;
-  const SmemLayout lay = layout_for(LP, S, 64 * 32);
+  const SmemLayout lay = layout_for(LP, S, kTileBytes);
   const int samp0 = blockIdx.x * 128;
   const int jb = blockIdx.y * a.per_split;
   const int je = min(jb + a.per_split, a.nsnp);
@@ -439,19 +477,20 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (warp == 0) {
     if (lane == 0) {
-      const uint32_t tx_bytes = 64 * 32 + (uint32_t)(ncat * 128);
+      const uint32_t tx_bytes = kTileBytes + (uint32_t)(ncat * 128);
+      const int scol = kDense ? samp0 : (samp0 >> 2);  // inner TMA coordinate
       int issued = 0;
       for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
-        tma_prefetch_2d(&map_bed, samp0 >> 2, (int)(a.pos0 + jb + kb * kStepK));
+        tma_prefetch_2d(&map_bed, scol, (int)(a.pos0 + jb + kb * kStepK));
       for (int kb = 0; kb < nk; ++kb) {
         const int st = kb % nst;
         if (kb + kPrefetchSteps < nk)
-          tma_prefetch_2d(&map_bed, samp0 >> 2, (int)(a.pos0 + jb + (kb + kPrefetchSteps) * kStepK));
+          tma_prefetch_2d(&map_bed, scol, (int)(a.pos0 + jb + (kb + kPrefetchSteps) * kStepK));
         if (kb >= nst && !role_wait(&empty_bar[st], (uint32_t)(kb / nst - 1) & 1u, &abort_sh)) break;
         uint8_t* base = smem + st * lay.stage_bytes;
         const int j0 = jb + kb * kStepK;
         mbar_expect_tx(&full_bar[st], tx_bytes);
-        tma_load_2d(base + lay.p, &map_bed, samp0 >> 2, (int)(a.pos0 + j0), &full_bar[st]);
+        tma_load_2d(base + lay.p, &map_bed, scol, (int)(a.pos0 + j0), &full_bar[st]);
         for (int r = 0; r < S; ++r) tma_load_2d(base + lay.b + r * LP * 128, &map_g, j0, r * LP, &full_bar[st]);
         issued = kb + 1;
       }
@@ -469,7 +508,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t bb = smem_u32(base + lay.b);
         const uint32_t ad = tmem + a_col0 + st * 32;
 #pragma unroll
-        for (int kk = 0; kk < kStepK / 16; ++kk) mma_cat(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
+        for (int kk = 0; kk < kStepK / 16; ++kk) mma_cat<kDense>(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
         mma_commit(&empty_bar[st]);
       }
       mma_commit(&acc_bar);
@@ -485,12 +524,23 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int kb = 0; kb < nk; ++kb) {
       const int st = kb % nst;
       if (!role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
-      const uint8_t* pt = smem + st * lay.stage_bytes + lay.p + (ch * 32) * 32 + (r >> 2);
       uint32_t wd[16];
+      if (kDense) {
+        // value of SNP row j, sample r at j*256 + 2r: lanes read neighbouring
+        // 2-byte values; two SNPs per 32-bit column
+        const uint16_t* pt = reinterpret_cast<const uint16_t*>(smem + st * lay.stage_bytes + lay.p) + r;
 #pragma unroll
-      for (int e = 0; e < 16; ++e) {
-        const uint32_t b0 = pt[(2 * e) * 32], b1 = pt[(2 * e + 1) * 32];
-        wd[e] = dosage_pair(((b0 >> sh) & 3u) | (((b1 >> sh) & 3u) << 16));
+        for (int e = 0; e < 16; ++e) {
+          const uint32_t v0 = pt[(ch * 32 + 2 * e) * 128], v1 = pt[(ch * 32 + 2 * e + 1) * 128];
+          wd[e] = v0 | (v1 << 16);
+        }
+      } else {
+        const uint8_t* pt = smem + st * lay.stage_bytes + lay.p + (ch * 32) * 32 + (r >> 2);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          const uint32_t b0 = pt[(2 * e) * 32], b1 = pt[(2 * e + 1) * 32];
+          wd[e] = dosage_pair(((b0 >> sh) & 3u) | (((b1 >> sh) & 3u) << 16));
+        }
       }
       tmem_st16(tmem + lane_off + a_col0 + st * 32 + ch * 16, wd);
       tmem_wait_st();
@@ -577,32 +627,36 @@ __global__ void k_col_exponent(const double* __restrict__ A, int64_t rows, int L
 // 256^(S-1-s), |w_s| <= 128, exact in BF16) are the slices, with units
 // u_s = 2^(E-7-8s).  Returns the represented value m * u_(S-1).  Integer
 // digit arithmetic keeps the FP64 work to one multiply and one conversion.
+// The digits are stored as BF16 or (f16) FP16 bit patterns, exact in both.
 // *m_out (optional) receives m.
-__device__ __forceinline__ double split_store(double v, int E, int S, __nv_bfloat16* dst, size_t slice_stride,
+__device__ __forceinline__ uint16_t digit_bits(int w, bool f16) {
+  return f16 ? __half_as_ushort(__int2half_rn(w)) : __bfloat16_as_ushort(__float2bfloat16_rn((float)w));
+}
+__device__ __forceinline__ double split_store(double v, int E, int S, uint16_t* dst, size_t slice_stride, bool f16,
                                               int* m_out = nullptr) {
   const int m = __double2int_rn(v * exp2i(8 * S - 1 - E));
   if (m_out) *m_out = m;
   int rest = m;
   for (int s = S - 1; s > 0; --s) {
     const int w = ((rest + 128) & 255) - 128;
-    dst[(size_t)s * slice_stride] = __float2bfloat16_rn((float)w);
+    dst[(size_t)s * slice_stride] = digit_bits(w, f16);
     rest = (rest - w) >> 8;
   }
-  dst[0] = __float2bfloat16_rn((float)rest);
+  dst[0] = digit_bits(rest, f16);
   return (double)m * exp2i(E - 8 * S + 1);
 }
 
 // W slices of Omega (S*LP rows x npad, K-major) and the represented W, in FP64
 // and as the integer m (|m| <= 2^23; the value is m times the last slice unit).
 __global__ void k_omega_slices(const double* __restrict__ omg, int npad, int N, int LP, int S,
-                               const int* __restrict__ E, __nv_bfloat16* __restrict__ w, double* __restrict__ rep,
-                               int32_t* __restrict__ wint) {
+                               const int* __restrict__ E, uint16_t* __restrict__ w, double* __restrict__ rep,
+                               int32_t* __restrict__ wint, int f16) {
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (idx >= (int64_t)npad * LP) return;
   const int i = (int)(idx / LP), l = (int)(idx % LP);
   const double v = i < N ? omg[idx] : 0.0;
   int m = 0;
-  const double r = split_store(v, E[l], S, w + (size_t)l * npad + i, (size_t)LP * npad, &m);
+  const double r = split_store(v, E[l], S, w + (size_t)l * npad + i, (size_t)LP * npad, f16 != 0, &m);
   rep[idx] = r;
   wint[idx] = m;
 }
@@ -641,9 +695,9 @@ __global__ void k_tc_g_finish(GFinishArgs a) {
         a.gesum[idx] = 0ull;
       }
     }
-    const double g = s * (0.5 * pd - f * a.colsum[l] + miss);
+    const double g = s * (a.vfac * pd - f * a.colsum[l] + miss);
     a.G[pos * LP + l] = g;
-    gh = 0.5 * s * g;
+    gh = a.vfac * s * g;
   }
   a.gh[idx] = gh;
 }
@@ -660,19 +714,26 @@ __global__ void k_tc_gh_slices(GFinishArgs a, const int* __restrict__ Eh) {
   const int j = (int)(idx / a.LP), l = (int)(idx % a.LP);
   const int S = a.nslice, LP = a.LP;
   const size_t sstride = (size_t)LP * a.ldg;
-  __nv_bfloat16* dh = a.gt + (size_t)l * a.ldg + j;
+  uint16_t* dh = reinterpret_cast<uint16_t*>(a.gt) + (size_t)l * a.ldg + j;
+  const bool f16 = a.vfac == 1.0;  // dense input: FP16 operands
   if (j < a.nsnp && l < a.L) {
     const int64_t pos = a.pos0 + j;
     const int64_t snp = a.perm ? (int64_t)a.perm[pos] : pos;
     int mh = 0;
-    const double ghq = split_store(a.gh[(size_t)j * LP + l], Eh[l], S, dh, sstride, &mh);
+    const double ghq = split_store(a.gh[(size_t)j * LP + l], Eh[l], S, dh, sstride, f16, &mh);
     a.ghint[(size_t)j * LP + l] = mh;
-    const int e = Eh[l] + 1;
-    const int m = __double2int_rn(2.0 * a.F[snp] * ghq * exp2i(8 * S - 1 - e));
-    a.gmint[(size_t)j * LP + l] = m;
-    a.cpart[(size_t)j * LP + l] = (double)m * exp2i(e - 8 * S + 1);
+    if (f16) {
+      // dense: c = sum_j mu_j Gh_j (no missing entries)
+      a.gmint[(size_t)j * LP + l] = 0;
+      a.cpart[(size_t)j * LP + l] = a.F[snp] * ghq;
+    } else {
+      const int e = Eh[l] + 1;
+      const int m = __double2int_rn(2.0 * a.F[snp] * ghq * exp2i(8 * S - 1 - e));
+      a.gmint[(size_t)j * LP + l] = m;
+      a.cpart[(size_t)j * LP + l] = (double)m * exp2i(e - 8 * S + 1);
+    }
   } else {
-    for (int s = 0; s < S; ++s) dh[s * sstride] = __float2bfloat16(0.f);
+    for (int s = 0; s < S; ++s) dh[s * sstride] = 0;
     if (j < a.nsnp) {
       a.ghint[(size_t)j * LP + l] = 0;
       a.gmint[(size_t)j * LP + l] = 0;
@@ -735,13 +796,16 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 }  // namespace
 
-void make_map_2d(CUtensorMap* map, const void* base, bool bf16, uint64_t inner, uint64_t outer, uint64_t pitch_bytes,
+void make_map_2d(CUtensorMap* map, const void* base, int dtype, uint64_t inner, uint64_t outer, uint64_t pitch_bytes,
                  uint32_t box_inner, uint32_t box_outer, bool swizzle128) {
   const cuuint64_t dims[2] = {inner, outer};
   const cuuint64_t strides[1] = {pitch_bytes};
   const cuuint32_t box[2] = {box_inner, box_outer};
   const cuuint32_t es[2] = {1, 1};
-  const CUresult r = encode_fn()(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 2,
+  const CUtensorMapDataType t = dtype == kMapBF16   ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                : dtype == kMapF16  ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                    : CU_TENSOR_MAP_DATA_TYPE_UINT8;
+  const CUresult r = encode_fn()(map, t, 2,
                                  const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                                  swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -770,19 +834,38 @@ int tmem_cols_for(int ncols) {
   return c;
 }
 
+template <bool kDense>
+void launch_g_t(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs& a, size_t smem, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    PCAONE_CUDA(cudaFuncSetAttribute(k_tc_g<kDense>, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
+    attr = true;
+  }
+  dim3 grid((a.nsnp + 127) / 128, a.nchunks);
+  k_tc_g<kDense><<<grid, kThreads, smem, s>>>(map_bed, map_w, a);
+}
+
+template <bool kDense>
+void launch_h_t(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs& a, size_t smem, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    PCAONE_CUDA(cudaFuncSetAttribute(k_tc_h<kDense>, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
+    attr = true;
+  }
+  dim3 grid(a.npad / 128, a.nsplit);
+  k_tc_h<kDense><<<grid, kThreads, smem, s>>>(map_bed, map_g, a);
+}
+
 void launch_g(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs& a, cudaStream_t s) {
   if (a.nstages < 1 || a.nstages > kMaxStages || a.tmem_cols > 512 ||
       a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.nstages))
     throw Error(-6, "tensor-core G product: pipeline plan exceeds TMEM or the stage limit");
-  static bool attr = false;
-  if (!attr) {
-    PCAONE_CUDA(cudaFuncSetAttribute(k_tc_g, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
-    attr = true;
-  }
-  const size_t smem = smem_bytes(a.LP, a.nslice, 128 * 16, a.nstages);
+  const size_t smem = smem_bytes(a.LP, a.nslice, g_tile_bytes(a.dense != 0), a.nstages);
   if (smem > 214 * 1024) throw Error(-6, "tensor-core G product: pipeline plan exceeds shared memory");
-  dim3 grid((a.nsnp + 127) / 128, a.nchunks);
-  k_tc_g<<<grid, kThreads, smem, s>>>(map_bed, map_w, a);
+  if (a.dense)
+    launch_g_t<true>(map_bed, map_w, a, smem, s);
+  else
+    launch_g_t<false>(map_bed, map_w, a, smem, s);
   PCAONE_LAUNCH_CHECK();
 }
 
@@ -790,24 +873,22 @@ void launch_h(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs&
   if (a.nstages < 1 || a.nstages > kMaxStages || a.tmem_cols > 512 ||
       a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.nstages))
     throw Error(-6, "tensor-core H product: pipeline plan exceeds TMEM or the stage limit");
-  static bool attr = false;
-  if (!attr) {
-    PCAONE_CUDA(cudaFuncSetAttribute(k_tc_h, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
-    attr = true;
-  }
-  const size_t smem = smem_bytes(a.LP, a.nslice, 64 * 32, a.nstages);
+  const size_t smem = smem_bytes(a.LP, a.nslice, h_tile_bytes(a.dense != 0), a.nstages);
   if (smem > 214 * 1024) throw Error(-6, "tensor-core H product: pipeline plan exceeds shared memory");
-  dim3 grid(a.npad / 128, a.nsplit);
-  k_tc_h<<<grid, kThreads, smem, s>>>(map_bed, map_g, a);
+  if (a.dense)
+    launch_h_t<true>(map_bed, map_g, a, smem, s);
+  else
+    launch_h_t<false>(map_bed, map_g, a, smem, s);
   PCAONE_LAUNCH_CHECK();
 }
 
 void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv_bfloat16* w, double* wunit,
-                         double* colsum, int* E, double* rep, int32_t* wint, cudaStream_t s) {
+                         double* colsum, int* E, double* rep, int32_t* wint, bool f16, cudaStream_t s) {
   const int64_t n = (int64_t)npad * LP;
   k_col_exponent<<<LP, 256, 0, s>>>(omg, N, LP, E);
   PCAONE_LAUNCH_CHECK();
-  k_omega_slices<<<ceil_div(n, 256), 256, 0, s>>>(omg, npad, N, LP, S, E, w, rep, wint);
+  k_omega_slices<<<ceil_div(n, 256), 256, 0, s>>>(omg, npad, N, LP, S, E, reinterpret_cast<uint16_t*>(w), rep,
+                                                  wint, f16 ? 1 : 0);
   PCAONE_LAUNCH_CHECK();
   k_units<<<ceil_div(S * LP, 128), 128, 0, s>>>(E, LP, S, 0, wunit);
   PCAONE_LAUNCH_CHECK();

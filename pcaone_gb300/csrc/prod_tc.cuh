@@ -23,6 +23,7 @@ struct GArgs {
   const double* wscale;   // S x LP units of the W slices
   float* part;            // [nchunks][nsnp][LP]
   int* err;               // set to 1 when a bounded wait gave up
+  int dense;              // 1: FP16 values (FileBinary input) instead of packed codes
 };
 
 // H += X_w^T * Gh for one SNP window (dosage part; the first split's
@@ -45,9 +46,11 @@ struct HArgs {
   const double* gmunit_m;     // per column unit of the Gm integers
   unsigned long long* hesum;  // npad x LP int64 EM product sums (nullptr: no EM), cleared
   const double* hunit_m;      // per column unit of the Gh integers
+  int dense;                  // 1: FP16 values instead of packed codes
 };
 
 struct GFinishArgs {
+  double vfac;                   // 1/2 for dosages (x = s (d/2 - f)), 1 for dense values (x = v - mu)
   int64_t pos0;
   int nsnp;
   int L, LP, nslice, nchunks;
@@ -68,8 +71,12 @@ struct GFinishArgs {
   double* cpart;                 // nsnp x LP partial terms of c
 };
 
-void make_map_2d(CUtensorMap* map, const void* base, bool bf16, uint64_t inner, uint64_t outer, uint64_t pitch_bytes,
+constexpr int kMapU8 = 0, kMapBF16 = 1, kMapF16 = 2;
+void make_map_2d(CUtensorMap* map, const void* base, int dtype, uint64_t inner, uint64_t outer, uint64_t pitch_bytes,
                  uint32_t box_inner, uint32_t box_outer, bool swizzle128);
+// A tile bytes per pipeline stage of the G and H products
+inline int g_tile_bytes(bool dense) { return dense ? 128 * 128 : 128 * 16; }
+inline int h_tile_bytes(bool dense) { return dense ? 64 * 256 : 64 * 32; }
 // pipeline stages within shared memory (B slices + packed tile per stage) and
 // TMEM (nslice * LP accumulator columns + 32 A columns per stage)
 int stages_for(int LP, int nslice, int pbytes);
@@ -78,7 +85,7 @@ int tmem_cols_needed(int LP, int nslice, int nstages);
 void launch_g(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs& a, cudaStream_t s);
 void launch_h(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs& a, cudaStream_t s);
 void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv_bfloat16* w, double* wunit,
-                         double* colsum, int* E, double* rep, int32_t* wint, cudaStream_t s);
+                         double* colsum, int* E, double* rep, int32_t* wint, bool f16, cudaStream_t s);
 // G finish, Gh slices and their units (hunit), Gm integers with their units
 // (gmunit: S x LP, the last slice row is the unit of gmint), c
 void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* gmunit, double* c_out, cudaStream_t s);

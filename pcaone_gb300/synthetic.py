@@ -148,6 +148,53 @@ def sample_codes(model: PopulationModel, snp_lo: int, snp_hi: int) -> np.ndarray
     return code
 
 
+KEY_DOSAGE_NOISE = 0xD05E
+
+
+def sample_dosages(model: PopulationModel, sd: float = 0.1, snp_lo: int = 0, snp_hi: Optional[int] = None,
+                   ) -> np.ndarray:
+    """Continuous dosages of SNPs [snp_lo, snp_hi) x all samples (float16,
+    M' x N): the sampled allele count d in {0, 1, 2} (missing genotypes of the
+    model are drawn as observed) plus Gaussian noise of standard deviation sd
+    (Box-Muller on two hashed uniforms), clipped to [0, 2] and rounded to
+    float16, the storage of imputed dosages."""
+    snp_hi = model.nsnps if snp_hi is None else snp_hi
+    code = sample_codes(model, snp_lo, snp_hi)
+    n = model.nsamples
+    j = np.arange(snp_lo, snp_hi, dtype=np.uint64)[:, None]
+    i = np.arange(n, dtype=np.uint64)[None, :]
+    counter = (j << np.uint64(32)) | i
+    # allele counts without the missing draw: recompute from the two allele draws
+    fr = model.freq[snp_lo:snp_hi]
+    p = np.zeros((snp_hi - snp_lo, n), dtype=np.float64)
+    for k in range(model.npop):
+        p = p + model.weights[None, :, k] * fr[:, k:k + 1]
+    ua = uniform01(model.seed, KEY_ALLELE_A, counter)
+    ub = uniform01(model.seed, KEY_ALLELE_B, counter)
+    d = (ua < p).astype(np.float64) + (ub < p).astype(np.float64)
+    u1 = uniform01(model.seed, KEY_DOSAGE_NOISE, counter)
+    u2 = uniform01(model.seed, KEY_DOSAGE_NOISE + 1, counter)
+    z = np.sqrt(-2.0 * np.log(np.maximum(u1, 1e-300))) * np.cos(2.0 * np.pi * u2)
+    del code
+    return np.clip(d + sd * z, 0.0, 2.0).astype(np.float16)
+
+
+def write_binary(path: str, values: np.ndarray) -> None:
+    """The reference's FileBinary format (src/FileBinary.hpp:17-18,
+    src/FileBinary.cpp:21-46): uint32 SNPs, uint32 samples, then float32
+    values SNP by SNP."""
+    v = np.ascontiguousarray(values, dtype=np.float32)
+    with open(path, "wb") as f:
+        f.write(np.array([v.shape[0], v.shape[1]], dtype=np.uint32).tobytes())
+        f.write(v.tobytes())
+
+
+def read_binary(path: str) -> np.ndarray:
+    with open(path, "rb") as f:
+        m, n = np.frombuffer(f.read(8), dtype=np.uint32)
+        return np.frombuffer(f.read(), dtype=np.float32).reshape(int(m), int(n))
+
+
 def pack_codes(code: np.ndarray, pad_garbage: bool = False, seed: int = 0) -> np.ndarray:
     """Pack (m, N) 2-bit codes into (m, ceil(N/4)) bytes, PLINK SNP-major order."""
     m, n = code.shape
@@ -224,6 +271,13 @@ WORKLOADS = {
     # (1.56 GB packed) for profiling captures of single window launches
     "c2p": dict(nsamples=100_000, nsnps=62_500, npop=5, fst=[0.01, 0.02, 0.05, 0.1, 0.2],
                 anc="uniform", anc_range=(0.01, 0.5), mcar=0.005, k=20, p=20, maxp=6, bands=8),
+    # continuous dosages held as FP16 (FileBinary input, -C 0): c5 is 1M SNPs x 100k
+    # samples (200 GB FP16, run without the shuffle: a shuffled copy would not
+    # fit), c5s the same model at 100k SNPs (20 GB)
+    "c5": dict(nsamples=100_000, nsnps=1_000_000, npop=6, fst=[0.01, 0.02, 0.04, 0.06, 0.1, 0.15],
+               anc="uniform", anc_range=(0.05, 0.5), k=20, p=20, maxp=6, bands=64, dense=True, sd=0.1, perm=0),
+    "c5s": dict(nsamples=100_000, nsnps=100_000, npop=6, fst=[0.01, 0.02, 0.04, 0.06, 0.1, 0.15],
+                anc="uniform", anc_range=(0.05, 0.5), k=20, p=20, maxp=6, bands=64, dense=True, sd=0.1),
     # EM imputation (-d 2 -S: no shuffle, the reference's shuffled EMU path has a defect)
     "c4": dict(nsamples=50_000, nsnps=300_000, npop=4, fst=0.05, anc="uniform", anc_range=(0.05, 0.5),
                miss_sample_beta=(1, 20), miss_snp_beta=(1, 50), k=10, p=10, maxp=6, bands=64,

@@ -28,6 +28,7 @@ class RunOptions:
     tol: float = 1e-4
     tolem: float = 1e-5
     noshuffle: bool = False
+    scale: int = -9
     extra: dict = field(default_factory=dict)
 
     @property
@@ -67,7 +68,9 @@ def parse_options(opts) -> RunOptions:
             o.noshuffle = True
         elif a == "--emu":
             o.emu = True
-        elif a == "-b":
+        elif a in ("-C", "--scale"):
+            o.scale = int(next(it))
+        elif a in ("-b", "-B"):
             next(it)
         else:
             raise ValueError(f"option {a} not handled")
@@ -88,13 +91,40 @@ class GoldenCase:
 
 
 def golden_cases():
+    """PLINK fixtures (packed genotypes)."""
     out = []
     for path in sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz"))):
         z = np.load(path)
+        if "packed" not in z.files:
+            continue
         opts = parse_options(json.loads(str(z["options"])))
         ref = {k: z[k] for k in z.files if k not in ("packed", "options")}
         meta = ref["meta"]
         out.append(GoldenCase(os.path.basename(path)[:-4], z["packed"], int(meta[0]), int(meta[1]), opts, ref))
+    return out
+
+
+@dataclass
+class BinaryCase:
+    name: str
+    dense: np.ndarray        # M x N float16 values (read by the reference as float32)
+    nsamples: int
+    nsnps: int
+    opts: RunOptions
+    ref: dict
+
+
+def binary_cases():
+    """FileBinary fixtures (dense float16 dosages, -B ... -C 0)."""
+    out = []
+    for path in sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz"))):
+        z = np.load(path)
+        if "dense" not in z.files:
+            continue
+        opts = parse_options(json.loads(str(z["options"])))
+        ref = {k: z[k] for k in z.files if k not in ("dense", "options")}
+        meta = ref["meta"]
+        out.append(BinaryCase(os.path.basename(path)[:-4], z["dense"], int(meta[0]), int(meta[1]), opts, ref))
     return out
 
 

@@ -55,6 +55,15 @@ CASES = {
                 ["-d", "1", "--emu", "--maxiter", "5", "--maxp", "3", "-k", "2"]),
 }
 
+# FileBinary input (-B; per-SNP mean centring only, -C 0): continuous dosages
+# stored as float16 (synthetic.sample_dosages), written as the float32 matrix
+BINARY_CASES = {
+    "bin_wsvd_n301": (dict(nsamples=301, nsnps=2400, npop=3, fst=0.1, seed=21),
+                      ["-d", "2", "-C", "0", "-k", "4", "--maxp", "6", "-w", "16"]),
+    "bin_ssvd_n256": (dict(nsamples=256, nsnps=1800, npop=4, fst=0.08, seed=22),
+                      ["-d", "1", "-C", "0", "-k", "3", "--maxp", "4"]),
+}
+
 
 def run_case(name: str, model_kw: dict, opts: list) -> dict:
     kw = dict(model_kw)
@@ -79,11 +88,36 @@ def run_case(name: str, model_kw: dict, opts: list) -> dict:
     return res
 
 
+def run_binary_case(name: str, model_kw: dict, opts: list) -> dict:
+    model = synthetic.draw_population_model(**model_kw)
+    dense = synthetic.sample_dosages(model)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, name + ".bin")
+        synthetic.write_binary(path, dense)
+        out = os.path.join(td, "out")
+        os.makedirs(out)
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        subprocess.check_call([DRIVER, out, "--dump-g0", "-B", path] + opts, env=env)
+        res = {k: np.load(os.path.join(out, k + ".npy")) for k in ("U", "S", "V", "Omg0", "meta")}
+        g0 = np.load(os.path.join(out, "G0.npy"))
+        res["G0_sha256"] = np.frombuffer(hashlib.sha256(np.asfortranarray(g0).tobytes(order="F")).digest(),
+                                         dtype=np.uint8)
+        if os.path.exists(os.path.join(out, "perm.npy")):
+            res["perm"] = np.load(os.path.join(out, "perm.npy"))
+    res["dense"] = dense
+    res["options"] = np.array(json.dumps(opts))
+    return res
+
+
 def main() -> None:
     if not os.path.exists(DRIVER):
         sys.exit("build the reference driver first: make -C oracle ref")
     for name, (mkw, opts) in CASES.items():
         res = run_case(name, mkw, opts)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+        print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"])
+    for name, (mkw, opts) in BINARY_CASES.items():
+        res = run_binary_case(name, mkw, opts)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
         print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"])
 

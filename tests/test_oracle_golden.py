@@ -80,3 +80,39 @@ def test_bed_counts_edge_cases():
     assert F.tolist() == [0.0, 1.0, 0.0, (1 + 0.5) / 3]
     one = pack_codes(np.array([[2]], dtype=np.uint8))
     assert H.allele_freq(H.bed_counts(one, 1)).tolist() == [0.5]
+
+
+# ---- FileBinary input (-B, -C 0): the oracle against the reference ----
+from tests.cases import binary_cases  # noqa: E402
+
+BIN_CASES = binary_cases()
+BIN_IDS = [c.name for c in BIN_CASES]
+
+
+def _oracle_dense(case, omega0=None):
+    o = case.opts
+    assert o.scale == 0
+    d = H.OracleData.from_dense(case.dense, perm=o.perm, seed=o.seed, bands=o.bands, rand=o.rand, svd_t=o.svd,
+                                omega0=omega0)
+    op = H.run_pca_with_halko(d, o.k, o.oversamples, maxp=o.maxp, tol=o.tol, maxiter=0)
+    return d, op
+
+
+@pytest.mark.parametrize("case", BIN_CASES, ids=BIN_IDS)
+def test_binary_centring_bit_exact(case):
+    """FileBin::read_all (src/FileBinary.cpp:54-64): float32 values, each SNP
+    centred by its float64 mean."""
+    d = H.OracleData.from_dense(case.dense)
+    digest = hashlib.sha256(np.asfortranarray(d.G).tobytes(order="F")).digest()
+    assert digest == bytes(case.ref["G0_sha256"])
+
+
+@pytest.mark.parametrize("case", BIN_CASES, ids=BIN_IDS)
+def test_binary_rsvd_matches_reference(case):
+    d, op = _oracle_dense(case, omega0=case.ref["Omg0"])
+    S = case.ref["S"]
+    assert np.max(np.abs(op.S ** 2 - S ** 2) / S ** 2) < 1e-9
+    assert np.max(np.abs(align_signs(op.U, case.ref["U"]) - case.ref["U"])) < 1e-8
+    assert np.max(np.abs(align_signs(op.V, case.ref["V"]) - case.ref["V"])) < 1e-8
+    if case.opts.perm:
+        assert np.array_equal(H.shuffle_columns(case.nsnps), case.ref["perm"])
