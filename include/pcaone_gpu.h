@@ -201,6 +201,19 @@ int pcaone_gpu_run_halko(pcaone_gpu_ctx* ctx, const pcaone_gpu_params* params, d
  * src/Data.hpp:49); identity when no shuffle was applied. */
 int pcaone_gpu_get_perm(pcaone_gpu_ctx* ctx, int32_t* perm);
 
+/* Projection of the loaded samples (a PLINK fileset with the fit's SNPs) onto
+ * a fit: run_projection --project 1 / 2 (src/Projection.cpp:236-247,
+ * solve_projection_scores :159-178).  The genotypes are decoded, centred and
+ * standardised (ploidy 2) with the fit's allele frequencies F (nsnps; the
+ * reference reads them from the .mbim, src/Data.cpp:17-32); V is the fit's
+ * loadings (nsnps x k, column-major, file order, as in .loadings) and S its
+ * singular values.  mode 1: U = X V S^-1 (missing genotypes at the mean);
+ * mode 2: per sample the least-squares solution of (V S) x = g over its
+ * observed SNPs (NaN for a sample whose system is singular).  U: nsamples x k
+ * column-major.  k <= 32. */
+int pcaone_gpu_project(pcaone_gpu_ctx* ctx, const double* F, const double* V, const double* S, int k, int mode,
+                       double* U);
+
 /* Learned warm start for the next pcaone_gpu_run_halko calls with emu set
  * (NULL or enable = 0: plain mean-fill EM). */
 int pcaone_gpu_set_warm_start(pcaone_gpu_ctx* ctx, const pcaone_gpu_mlp_params* p);

@@ -420,6 +420,28 @@ def run_pca_with_halko(data: OracleData, k: int, oversamples: int, maxp: int = 2
     return op
 
 
+def project(packed_new: np.ndarray, nsamples: int, F: np.ndarray, V: np.ndarray, S: np.ndarray, mode: int,
+            ploidy: int = 2) -> np.ndarray:
+    """Scores of new samples on a fit (run_projection, src/Projection.cpp:236-247).
+
+    The new genotypes are decoded and centred with the fit's allele
+    frequencies F (read from the .mbim, src/Data.cpp:17-32) and standardised
+    with them; V (M x k, file order) and S are the fit's loadings and
+    singular values.  mode 1: U = G V S^-1 (missing genotypes at the mean);
+    mode 2: per sample the least-squares solution of (V S) x = g over its
+    observed SNPs (solve_projection_scores, src/Projection.cpp:159-178)."""
+    G, C = decode_centered(packed_new, nsamples, F)
+    G = G * standardize_scale(F, ploidy)[None, :]
+    if mode == 1:
+        return G @ (V / S[None, :])
+    VS = V * S[None, :]
+    U = np.zeros((nsamples, V.shape[1]))
+    for i in range(nsamples):
+        obs = ~C[:, i]
+        U[i] = np.linalg.lstsq(VS[obs], G[i, obs], rcond=None)[0]
+    return U
+
+
 def arnoldi_matvec(data: OracleData, x: np.ndarray) -> np.ndarray:
     """y = X (X^T x) summed over SNP blocks (ArnoldiOpData::perform_op,
     src/Arnoldi.cpp:18-46)."""

@@ -14,6 +14,13 @@
 //   Omg0.npy      the initial random test matrix (src/Halko.cpp:15-23)
 //   G0.npy        optional (--dump-g0 as first option): the decoded, centred
 //                 matrix before standardisation (N x M), small inputs only
+//   P1.npy P2.npy optional (--project-new PREFIX): scores of the samples of a
+//                 second PLINK fileset (same SNPs) projected onto the fit, by
+//                 --project 1 (U = G V S^-1) and 2 (per-sample least squares
+//                 over observed SNPs, solve_projection_scores), with the new
+//                 genotypes decoded and standardised with the fit's F as
+//                 run_projection does (src/Projection.cpp:236-247,
+//                 src/Data.cpp:17-32)
 #define _DECLARE_TOOLBOX_HERE
 #include <cstdint>
 #include <cstdio>
@@ -24,6 +31,7 @@
 #include "FileBinary.hpp"
 #include "FilePlink.hpp"
 #include "Halko.hpp"
+#include "Projection.hpp"
 #include "Utils.hpp"
 
 namespace {
@@ -67,11 +75,16 @@ int main(int argc, char** argv) {
   }
   std::string outdir = argv[1];
   bool dump_g0 = false;
+  std::string project_new;
   std::vector<char*> args;
   args.push_back(argv[0]);
   for (int i = 2; i < argc; ++i) {
     if (std::strcmp(argv[i], "--dump-g0") == 0) {
       dump_g0 = true;
+      continue;
+    }
+    if (std::strcmp(argv[i], "--project-new") == 0 && i + 1 < argc) {
+      project_new = argv[++i];
       continue;
     }
     args.push_back(argv[i]);
@@ -125,6 +138,33 @@ int main(int argc, char** argv) {
     std::vector<long long> p(data->perm.indices().size());
     for (size_t i = 0; i < p.size(); ++i) p[i] = data->perm.indices()[i];
     write_npy(outdir + "/perm.npy", "<i8", p.data(), 8, {(long long)p.size()}, false);
+  }
+  if (!project_new.empty()) {
+    // loadings in file order (the un-permutation of Data::write_eigs_files)
+    Mat2D Vf = rsvd->V;
+    if (params.perm && data->perm.indices().size() == (Eigen::Index)data->nsnps)
+      for (Eigen::Index logical = 0; logical < (Eigen::Index)data->nsnps; ++logical)
+        Vf.row(data->perm.indices()[logical]) = rsvd->V.row(logical);
+    // the same options with the new fileset (Param is not copyable)
+    std::vector<char*> args2(args);
+    for (size_t i = 0; i + 1 < args2.size(); ++i)
+      if (std::strcmp(args2[i], "-b") == 0) args2[i + 1] = const_cast<char*>(project_new.c_str());
+    Param p2((int)args2.size(), args2.data());
+    p2.dopca = false;
+    p2.missme = true;
+    FileBed* nd = new FileBed(p2);
+    nd->F = data->F;  // the fit's allele frequencies (read from the .mbim in run_projection)
+    nd->read_all();
+    nd->standardize_E();
+    const int K = (int)rsvd->S.size() < (int)params.k ? (int)rsvd->S.size() : (int)params.k;
+    const Mat1D S = rsvd->S.head(K);
+    const Mat2D V = Vf.leftCols(K);
+    Mat2D P1 = nd->G * (V * S.array().inverse().matrix().asDiagonal());
+    Mat2D P2(nd->nsamples, K);
+    solve_projection_scores(V * S.asDiagonal(), nd->C, nd->G, P2);
+    dump(outdir, "P1", P1);
+    dump(outdir, "P2", P2);
+    delete nd;
   }
   std::vector<long long> meta = {(long long)data->nsamples, (long long)data->nsnps, em_iters};
   write_npy(outdir + "/meta.npy", "<i8", meta.data(), 8, {3}, false);

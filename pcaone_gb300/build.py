@@ -19,7 +19,7 @@ OBJDIR = os.path.join(LIBDIR, "obj")
 LIBNAME = "libpcaone_gb300.so"
 LIBPATH = os.path.join(LIBDIR, LIBNAME)
 
-CU_SOURCES = ["bed.cu", "prod_simt.cu", "prod_tc.cu", "dense64.cu", "util.cu", "halko.cu", "noalloc.cu", "mlp.cu"]
+CU_SOURCES = ["bed.cu", "prod_simt.cu", "prod_tc.cu", "dense64.cu", "util.cu", "halko.cu", "noalloc.cu", "mlp.cu", "project.cu"]
 CPP_SOURCES = ["rng.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

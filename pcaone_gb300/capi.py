@@ -32,7 +32,7 @@ EXPORTS = [
     "pcaone_gpu_set_profiling", "pcaone_gpu_kernel_stats", "pcaone_gpu_launch_count",
     "pcaone_gpu_matvec_static", "pcaone_gpu_mlp_default_params", "pcaone_gpu_set_warm_start",
     "pcaone_gpu_mlp_stats", "pcaone_gpu_mlp_forward_backward", "pcaone_gpu_load_dense",
-    "pcaone_gpu_load_binary_file_image", "pcaone_gpu_load_synthetic_dense",
+    "pcaone_gpu_load_binary_file_image", "pcaone_gpu_load_synthetic_dense", "pcaone_gpu_project",
 ]
 MLP_PARAMS, MLP_INPUTS = 82689, 64
 
@@ -101,6 +101,7 @@ def load(path: str = LIBPATH) -> ctypes.CDLL:
                                              c_void_p, c_void_p]
     lib.pcaone_gpu_load_dense.argtypes = [c_void_p, c_void_p, c_uint64, c_uint32]
     lib.pcaone_gpu_load_binary_file_image.argtypes = [c_void_p, c_void_p, c_uint64]
+    lib.pcaone_gpu_project.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]
     lib.pcaone_gpu_load_synthetic_dense.argtypes = [c_void_p, c_uint64, c_uint32, c_int, c_void_p, c_void_p,
                                                     c_double, c_uint64]
     lib.pcaone_gpu_mlp_default_params.argtypes = [P(MlpParams)]
@@ -289,6 +290,16 @@ class Context:
         v = np.ascontiguousarray(values, dtype=np.float32)
         self._check(self.lib.pcaone_gpu_load_dense(self.h, v.ctypes.data, v.shape[0], v.shape[1]))
         self.nsnps, self.nsamples = v.shape
+
+    def project(self, F: np.ndarray, V: np.ndarray, S: np.ndarray, mode: int = 1) -> np.ndarray:
+        """Scores of the loaded samples on a fit (F, V in file order, S)."""
+        F = np.ascontiguousarray(F, dtype=np.float64)
+        Vc = np.asfortranarray(V, dtype=np.float64)
+        S = np.ascontiguousarray(S, dtype=np.float64)
+        k = Vc.shape[1]
+        U = np.empty((self.nsamples, k), dtype=np.float64, order="F")
+        self._check(self.lib.pcaone_gpu_project(self.h, _ptr(F), Vc.ctypes.data, _ptr(S), k, mode, U.ctypes.data))
+        return U
 
     def load_synthetic_dense(self, model, sd: float = 0.1):
         """Continuous dosages of ``model`` generated on the device (FP16)."""

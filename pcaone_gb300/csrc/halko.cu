@@ -1174,6 +1174,65 @@ static int run_halko(Context& c, const pcaone_gpu_params& p) {
   return em_iters;
 }
 
+// Projection of the loaded samples onto a fit (project.cu; run_projection,
+// src/Projection.cpp:236-247).  F, V (M x k column-major, file order) and S
+// come from the fit; U (N x k column-major) receives the scores.
+static void project(Context& c, const double* F, const double* V, const double* S, int k, int mode, double* U) {
+  need_plink(c);
+  if (!F || !V || !S || !U) throw Error(PCAONE_E_ARG, "null projection argument");
+  if (mode != 1 && mode != 2) throw Error(PCAONE_E_ARG, "projection mode must be 1 or 2");
+  if (k <= 0 || k > project_max_k())
+    throw Error(PCAONE_E_LIMIT, "projection takes 1 to " + std::to_string(project_max_k()) + " PCs");
+  const int N = c.N;
+  const int64_t M = c.M;
+  std::vector<double> Bh((size_t)M * k);
+  for (int q = 0; q < k; ++q) {
+    if (!(S[q] > 0.0)) throw Error(PCAONE_E_ARG, "singular values must be positive");
+    const double f = mode == 1 ? 1.0 / S[q] : S[q];
+    for (int64_t j = 0; j < M; ++j) Bh[(size_t)j * k + q] = V[(size_t)q * M + j] * f;
+  }
+  DBuf<double> Fd, B, lut, sc, part, R, X, W, red;
+  Fd.ensure((size_t)M, c.stream, false);
+  B.ensure((size_t)M * k, c.stream, false);
+  lut.ensure((size_t)M * 4, c.stream, false);
+  sc.ensure((size_t)M, c.stream, false);
+  PCAONE_CUDA(cudaMemcpyAsync(Fd.p, F, (size_t)M * 8, cudaMemcpyHostToDevice, c.stream));
+  PCAONE_CUDA(cudaMemcpyAsync(B.p, Bh.data(), Bh.size() * 8, cudaMemcpyHostToDevice, c.stream));
+  launch_lut(Fd.p, M, 1, 2, nullptr, lut.p, sc.p, c.stream);  // standardize_E with the fit's F, ploidy 2
+  const int ctas = c.npad / 128;
+  const int nsplit = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(608, ctas), (M + 31) / 32));
+  part.ensure((size_t)nsplit * c.npad * k, c.stream, false);
+  R.ensure((size_t)N * k, c.stream, false);
+  launch_project_rhs(c.view(), lut.p, B.p, k, c.npad, part.p, nsplit, R.p, c.stream);
+  const double* out = R.p;
+  if (mode == 2) {
+    // K = B^T B, then per sample minus its missing SNPs' outer products
+    const int nb = cross_blocks(M);
+    W.ensure((size_t)k * k, c.stream, false);
+    red.ensure((size_t)nb * k * k, c.stream, false);
+    launch_cross(B.p, k, k, B.p, k, k, M, 1, W.p, k, red.p, nb, c.stream);
+    DBuf<int32_t> cnt, pos, smp;
+    DBuf<int64_t> ptr;
+    cnt.ensure(N, c.stream, false);
+    launch_bucket_count(c.view(), nullptr, M, 1, cnt.p, c.stream);
+    std::vector<int32_t> ch(N);
+    PCAONE_CUDA(cudaMemcpyAsync(ch.data(), cnt.p, (size_t)N * 4, cudaMemcpyDeviceToHost, c.stream));
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+    std::vector<int64_t> ph((size_t)N + 1, 0);
+    for (int i = 0; i < N; ++i) ph[i + 1] = ph[i] + ch[i];
+    ptr.ensure((size_t)N + 1, c.stream, false);
+    PCAONE_CUDA(cudaMemcpyAsync(ptr.p, ph.data(), ph.size() * 8, cudaMemcpyHostToDevice, c.stream));
+    pos.ensure((size_t)std::max<int64_t>(1, ph[N]), c.stream, false);
+    smp.ensure((size_t)std::max<int64_t>(1, ph[N]), c.stream, false);
+    launch_bucket_fill(c.view(), nullptr, M, 1, ptr.p, pos.p, smp.p, c.stream);
+    X.ensure((size_t)N * k, c.stream, false);
+    launch_project_solve(W.p, B.p, k, ptr.p, pos.p, R.p, N, X.p, c.stream);
+    out = X.p;
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));  // the local buffers are freed on return
+  }
+  copy_out(c, out, N, k, k, U);
+}
+
 static void matvec(Context& c, const double* x, double* y, int standardize) {
   need_plink(c);
   const int N = c.N;
@@ -1532,6 +1591,11 @@ int pcaone_gpu_get_perm(pcaone_gpu_ctx* ctx, int32_t* perm) {
     else
       for (int64_t i = 0; i < c.M; ++i) perm[i] = (int32_t)i;
   });
+}
+
+int pcaone_gpu_project(pcaone_gpu_ctx* ctx, const double* F, const double* V, const double* S, int k, int mode,
+                       double* U) {
+  return guarded(ctx, [&](Context& c) { pcaone::project(c, F, V, S, k, mode, U); });
 }
 
 int pcaone_gpu_matvec(pcaone_gpu_ctx* ctx, const double* x, double* y, int standardize) {

@@ -211,6 +211,12 @@ void launch_synth_dense(float* out, int64_t snp0, int64_t nsnps, int nsamples, i
                         const double* weights, double sd, uint64_t seed, cudaStream_t s);
 // dense rows: float32 -> FP16 rows of npad values (bytes at dst) and the exact row means
 void launch_dense_rows(const float* src, int64_t nrows, int N, int npad, uint8_t* dst, double* mean, cudaStream_t s);
+// projection of samples onto a fit (project.cu)
+int project_max_k();
+void launch_project_rhs(const BedView& v, const double* lut64, const double* B, int k, int npad, double* part,
+                        int nsplit, double* R, cudaStream_t s);
+void launch_project_solve(const double* K, const double* B, int k, const int64_t* ptr, const int32_t* pos,
+                          const double* R, int N, double* X, cudaStream_t s);
 void launch_flip_uv(double* U, int64_t nrows_u, double* V, int64_t nrows_v, int k, int* flag, cudaStream_t s);
 void launch_transpose_out(const double* A, int64_t rows, int lda, int cols, double* out, cudaStream_t s);
 

@@ -109,6 +109,40 @@ def run_binary_case(name: str, model_kw: dict, opts: list) -> dict:
     return res
 
 
+# projection of new samples (--project 1 and 2): the first n_base samples of
+# one model are fitted, the rest are projected (same SNPs, 2% missing)
+PROJECTION_CASES = {
+    "proj_wsvd_n400": (dict(nsamples=520, nsnps=3000, npop=3, fst=0.1, seed=41, mcar=0.02), 400,
+                       ["-d", "2", "-k", "4", "--maxp", "6", "-w", "16"]),
+}
+
+
+def run_projection_case(name: str, model_kw: dict, n_base: int, opts: list) -> dict:
+    model = synthetic.draw_population_model(**model_kw)
+    code = synthetic.sample_codes(model, 0, model.nsnps)
+    packed = synthetic.pack_codes(code[:, :n_base])
+    packed_new = synthetic.pack_codes(code[:, n_base:])
+    with tempfile.TemporaryDirectory() as td:
+        base, new = os.path.join(td, name), os.path.join(td, name + "_new")
+        synthetic.write_plink(base, packed, n_base)
+        synthetic.write_plink(new, packed_new, model.nsamples - n_base)
+        out = os.path.join(td, "out")
+        os.makedirs(out)
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        subprocess.check_call([DRIVER, out, "--dump-g0", "--project-new", new, "-b", base] + opts, env=env)
+        res = {k: np.load(os.path.join(out, k + ".npy")) for k in ("F", "U", "S", "V", "Omg0", "meta", "P1", "P2")}
+        g0 = np.load(os.path.join(out, "G0.npy"))
+        res["G0_sha256"] = np.frombuffer(hashlib.sha256(np.asfortranarray(g0).tobytes(order="F")).digest(),
+                                         dtype=np.uint8)
+        if os.path.exists(os.path.join(out, "perm.npy")):
+            res["perm"] = np.load(os.path.join(out, "perm.npy"))
+    res["packed"] = packed
+    res["packed_new"] = packed_new
+    res["n_new"] = np.array(model.nsamples - n_base)
+    res["options"] = np.array(json.dumps(opts))
+    return res
+
+
 def main() -> None:
     if not os.path.exists(DRIVER):
         sys.exit("build the reference driver first: make -C oracle ref")
@@ -120,6 +154,10 @@ def main() -> None:
         res = run_binary_case(name, mkw, opts)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
         print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"])
+    for name, (mkw, nb, opts) in PROJECTION_CASES.items():
+        res = run_projection_case(name, mkw, nb, opts)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+        print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"], "P2[0]=", res["P2"][0])
 
 
 if __name__ == "__main__":

@@ -116,3 +116,24 @@ def test_binary_rsvd_matches_reference(case):
     assert np.max(np.abs(align_signs(op.V, case.ref["V"]) - case.ref["V"])) < 1e-8
     if case.opts.perm:
         assert np.array_equal(H.shuffle_columns(case.nsnps), case.ref["perm"])
+
+
+# ---- projection of new samples (--project 1 and 2) ----
+PROJ_CASES = [c for c in CASES if "P2" in c.ref]
+
+
+@pytest.mark.parametrize("case", PROJ_CASES, ids=[c.name for c in PROJ_CASES])
+def test_projection_matches_reference(case):
+    """run_projection with the fit's F, V (file order) and S: mode 1 and the
+    per-sample least squares of mode 2 agree with the reference to rounding."""
+    k = case.opts.k
+    V = case.ref["V"][:, :k]
+    if case.opts.perm:
+        Vf = np.empty_like(V)
+        Vf[case.ref["perm"]] = V
+        V = Vf
+    S = case.ref["S"][:k]
+    n_new = int(case.ref["n_new"])
+    for mode, key in ((1, "P1"), (2, "P2")):
+        P = H.project(case.ref["packed_new"], n_new, case.ref["F"], V, S, mode)
+        assert np.max(np.abs(P - case.ref[key])) <= 1e-10 * max(1.0, np.max(np.abs(case.ref[key]))), mode
