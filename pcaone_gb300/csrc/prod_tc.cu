@@ -23,7 +23,8 @@
 // missing-entry terms use the same represented values as the products, so the
 // operator applied is exactly X times the sliced matrix.
 //
-// Kernels (one CTA = 384 threads in three roles, see role_wait below):
+// Kernels (one CTA = 320 threads in three roles, see role_wait below; two
+// CTAs share an SM when their TMEM plans fit in half of it, see pair_per_sm):
 //   k_tc_g : tile of 128 SNPs x one chunk of samples.  TMA brings the packed
 //            tile (128 rows x 16 bytes) and the W^T slice tiles (S*L rows x 64,
 //            128B swizzle, K-major B operand); decoder warps turn the packed
@@ -56,7 +57,7 @@ namespace tc {
 
 namespace {
 
-constexpr int kThreads = 384;          // 12 warps: TMA producer, MMA issuer, 8 decode / TMEM-epilogue warps
+constexpr int kThreads = 320;          // 10 warps: TMA producer, MMA issuer, 8 decode / TMEM-epilogue warps
 constexpr int kStepK = 64;              // K elements per pipeline stage (128 B of BF16 per row)
 constexpr int kMaxStages = 8;
 constexpr long long kTimeoutCycles = 4000000000ll;  // about 2 s at 2 GHz
@@ -242,16 +243,17 @@ __device__ __forceinline__ void mma_cat(uint32_t tmem_col0, uint32_t a_tmem, uin
   }
 }
 
-// Warp roles of both kernels (384 threads): warp 0 lane 0 issues the TMA
-// loads of each pipeline stage, warp 1 lane 0 issues the MMAs, warps 4-11
+// Warp roles of both kernels (320 threads): warp 0 lane 0 issues the TMA
+// loads of each pipeline stage, warp 1 lane 0 issues the MMAs, warps 2-9
 // decode the packed tile into the A operand(s) and finally read the
-// accumulators out of TMEM (warp w reads lanes 32*(w%4) .. +31, warps 4-7 the
-// first half of the columns and warps 8-11 the second).  Per stage s: full[s]
+// accumulators out of TMEM (warp w may only reach lanes 32*(w%4) .. +31;
+// warps 2-5 cover the four lane quarters for the first half of the columns
+// and warps 6-9 for the second).  Per stage s: full[s]
 // (TMA bytes landed), dec[s] (256 decoder arrivals), empty[s]
 // (tcgen05.commit of the stage's MMAs).  Every wait is bounded; a role that gives up sets the shared
 // abort flag, which makes every other wait return, so the CTA always reaches
 // its final barrier and frees its TMEM.
-constexpr int kDecodeWarp0 = 4;
+constexpr int kDecodeWarp0 = 2;
 constexpr int kDecoders = 256;
 
 __device__ __forceinline__ bool role_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
@@ -275,7 +277,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // G product
 // ---------------------------------------------------------------------------
 template <bool kDense>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, 2)
     k_tc_g(const __grid_constant__ CUtensorMap map_bed, const __grid_constant__ CUtensorMap map_w, GArgs a) {
   // A tile per stage: 128 SNP rows x 64 samples, packed (16 B per row) or FP16
   // (128 B per row, 128-byte swizzle)
@@ -430,7 +432,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 // H product
 // ---------------------------------------------------------------------------
 template <bool kDense>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, 2)
     k_tc_h(const __grid_constant__ CUtensorMap map_bed, const __grid_constant__ CUtensorMap map_g, HArgs a) {
   // A tile per stage: 64 SNP rows x 128 samples, packed (32 B per row) or FP16
   // (256 B per row, unswizzled)
@@ -812,20 +814,32 @@ void make_map_2d(CUtensorMap* map, const void* base, int dtype, uint64_t inner, 
   if (r != CUDA_SUCCESS) throw Error(-2, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
+// Two CTAs per SM when the slice accumulators leave room for two 32-column
+// operand stages within half of the SM's 512 TMEM columns.  The tensor core
+// then runs one CTA's MMAs while the other decodes and stores its next
+// operand into TMEM; on the 7,812 x 100,000 genotype window this cut both
+// products by a third against one CTA per SM with eight stages.
+bool pair_per_sm(int LP, int nslice) { return nslice * LP + 2 * 32 <= 256; }
+
 int stages_for(int LP, int nslice, int pbytes) {
   const SmemLayout l = layout_for(LP, nslice, pbytes);
-  const int budget = 212 * 1024;  // dynamic shared memory (static use is under 12 KB)
+  const bool pair = pair_per_sm(LP, nslice);
+  // dynamic shared memory (static use is under 12 KB); 228 KB per SM
+  const int budget = (pair ? 104 : 212) * 1024;
   const int by_smem = budget / (int)l.stage_bytes;
-  // TMEM: slice accumulators + 32 columns of A operand per stage, within the
-  // 512 columns of an SM
-  const int by_tmem = (512 - nslice * LP) / 32;
+  // TMEM: slice accumulators + 32 columns of A operand per stage
+  const int by_tmem = ((pair ? 256 : 512) - nslice * LP) / 32;
   return std::max(1, std::min(kMaxStages, std::min(by_smem, by_tmem)));
 }
 
 int tmem_cols_needed(int LP, int nslice, int nstages) { return nslice * LP + nstages * 32; }
 
-size_t smem_bytes(int LP, int nslice, int pbytes, int nstages) {
-  return (size_t)layout_for(LP, nslice, pbytes).stage_bytes * nstages + 1024;
+// A plan that takes more than half of the TMEM asks for more than half of the
+// shared memory too, so that a second CTA never shares its SM and waits in
+// tcgen05.alloc.
+size_t smem_bytes(int LP, int nslice, int pbytes, int nstages, int tmem_cols) {
+  const size_t b = (size_t)layout_for(LP, nslice, pbytes).stage_bytes * nstages + 1024;
+  return tmem_cols > 256 ? std::max(b, (size_t)120 * 1024) : b;
 }
 
 int tmem_cols_for(int ncols) {
@@ -860,7 +874,7 @@ void launch_g(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs&
   if (a.nstages < 1 || a.nstages > kMaxStages || a.tmem_cols > 512 ||
       a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.nstages))
     throw Error(-6, "tensor-core G product: pipeline plan exceeds TMEM or the stage limit");
-  const size_t smem = smem_bytes(a.LP, a.nslice, g_tile_bytes(a.dense != 0), a.nstages);
+  const size_t smem = smem_bytes(a.LP, a.nslice, g_tile_bytes(a.dense != 0), a.nstages, a.tmem_cols);
   if (smem > 214 * 1024) throw Error(-6, "tensor-core G product: pipeline plan exceeds shared memory");
   if (a.dense)
     launch_g_t<true>(map_bed, map_w, a, smem, s);
@@ -873,7 +887,7 @@ void launch_h(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs&
   if (a.nstages < 1 || a.nstages > kMaxStages || a.tmem_cols > 512 ||
       a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.nstages))
     throw Error(-6, "tensor-core H product: pipeline plan exceeds TMEM or the stage limit");
-  const size_t smem = smem_bytes(a.LP, a.nslice, h_tile_bytes(a.dense != 0), a.nstages);
+  const size_t smem = smem_bytes(a.LP, a.nslice, h_tile_bytes(a.dense != 0), a.nstages, a.tmem_cols);
   if (smem > 214 * 1024) throw Error(-6, "tensor-core H product: pipeline plan exceeds shared memory");
   if (a.dense)
     launch_h_t<true>(map_bed, map_g, a, smem, s);
