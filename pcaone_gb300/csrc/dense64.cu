@@ -15,6 +15,7 @@
 // matrices are LP x LP row-major.
 #include <algorithm>
 
+#include "dd.cuh"
 #include "internal.cuh"
 
 namespace pcaone {
@@ -97,17 +98,24 @@ __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict_
   }
 }
 
-// W (ldw columns) = sum over blocks of part; sym mirrors the upper triangle.
+// W (ldw columns) = sum over blocks of part, one warp per entry: the lanes sum
+// blocks lane, lane+32, ... and a butterfly combines them (a fixed order, so
+// the result does not depend on scheduling); sym mirrors the upper triangle.
 __global__ void k_cross_reduce(const double* __restrict__ part, int nblocks, int na, int nb, int sym,
                                double* __restrict__ W, int ldw) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= na * nb) return;
-  const int i = e / nb, j = e % nb;
-  if (sym && j < i) return;
+  const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (e >= (int64_t)na * nb) return;  // warp-uniform
+  const int i = (int)(e / nb), j = (int)(e % nb);
+  if (sym && j < i) return;  // warp-uniform
   double s = 0.0;
-  for (int b = 0; b < nblocks; ++b) s += part[(size_t)b * na * nb + e];
-  W[i * ldw + j] = s;
-  if (sym) W[j * ldw + i] = s;
+  for (int b = lane; b < nblocks; b += 32) s += part[(size_t)b * na * nb + e];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    W[i * ldw + j] = s;
+    if (sym) W[j * ldw + i] = s;
+  }
 }
 
 __global__ void k_zero(double* p, int64_t n) {
@@ -115,97 +123,141 @@ __global__ void k_zero(double* p, int64_t n) {
   if (i < n) p[i] = 0.0;
 }
 
-// Cholesky W = R^T R of the leading L x L block (right-looking, in shared
-// memory) and R^{-1} by back substitution; the padding block of R and Rinv is
-// the identity.  status: 0 ok, 1 non-positive or non-finite pivot.
-__global__ void k_chol_inv(const double* __restrict__ W, int L, int LP, double shift, double* __restrict__ R,
-                           double* __restrict__ Rinv, int* __restrict__ status) {
-  extern __shared__ double a[];  // L x L
+// Cholesky W = R^T R of the leading L x L block and R^{-1}, both right-looking
+// in shared memory, in double-float arithmetic (dd.cuh, about 48 bits): FP64
+// runs at a small fraction of the FP32 rate on this GPU, and the dependent
+// chain of L pivots (a square root and a reciprocal each) sets the time.
+//   factor, step k: row k scaled by 1/d_k, then the trailing upper triangle
+//     a_ij -= a_ki a_kj; thread 0 updates a_(k+1)(k+1) first and takes the
+//     next pivot's root and reciprocal while the others update;
+//   inverse, step k = L-1 .. 0 of R X = I with X = I initially: row k of X
+//     times 1/d_k, then rows i < k updated x_ic -= r_ik x_kc.
+// The padding block of R and Rinv is the identity.  status: 0 ok, 1
+// non-positive or non-finite pivot.
+constexpr int kCholThreads = 512;
+__device__ __forceinline__ void chol_pivot(const dd* a, int L, int k, dd* dg, dd* rdg, int* fail) {
+  const dd d = a[k * L + k];
+  const bool ok = d.hi > 0.f && isfinite(d.hi);
+  if (!ok) *fail = 1;
+  const dd dk = ok ? dd_sqrt(d) : dd{1.f, 0.f};
+  dg[k] = dk;
+  rdg[k] = dd_div(dd{1.f, 0.f}, dk);
+}
+
+__global__ void __launch_bounds__(kCholThreads) k_chol_inv(const double* __restrict__ W, int L, int LP, double shift,
+                                                           double* __restrict__ R, double* __restrict__ Rinv,
+                                                           int* __restrict__ status) {
+  extern __shared__ dd sdd[];  // L x L factor, L x L inverse, L roots, L reciprocals
+  dd* a = sdd;
+  dd* x = a + L * L;
+  dd* dg = x + L * L;
+  dd* rdg = dg + L;
   __shared__ int fail;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, nt = blockDim.x;
   if (tid == 0) fail = 0;
-  for (int e = tid; e < L * L; e += blockDim.x) {
+  for (int e = tid; e < L * L; e += nt) {
     const int i = e / L, j = e % L;
-    a[e] = W[i * LP + j] + (i == j ? shift : 0.0);
+    a[e] = dd_from_double(W[i * LP + j] + (i == j ? shift : 0.0));
+    x[e] = dd{i == j ? 1.f : 0.f, 0.f};
   }
+  __syncthreads();
+  if (tid == 0) chol_pivot(a, L, 0, dg, rdg, &fail);
   __syncthreads();
   for (int k = 0; k < L; ++k) {
-    if (tid == 0) {
-      const double d = a[k * L + k];
-      if (!(d > 0.0) || !isfinite(d)) fail = 1;
-      a[k * L + k] = d > 0.0 ? sqrt(d) : 1.0;
-    }
-    __syncthreads();
-    const double dk = a[k * L + k];
-    for (int j = k + 1 + tid; j < L; j += blockDim.x) a[k * L + j] /= dk;
+    const dd rk = rdg[k];
+    for (int j = k + 1 + tid; j < L; j += nt) a[k * L + j] = dd_mul(a[k * L + j], rk);
     __syncthreads();
     const int m = L - k - 1;
-    for (int e = tid; e < m * m; e += blockDim.x) {
+    for (int e = tid; e < m * m; e += nt) {
       const int i = k + 1 + e / m, j = k + 1 + e % m;
-      if (j >= i) a[i * L + j] -= a[k * L + i] * a[k * L + j];
+      if (j >= i) a[i * L + j] = dd_fms(a[i * L + j], a[k * L + i], a[k * L + j]);
+      if (e == 0) chol_pivot(a, L, k + 1, dg, rdg, &fail);  // element (k+1, k+1) is final now
     }
     __syncthreads();
   }
-  for (int e = tid; e < LP * LP; e += blockDim.x) {
-    const int i = e / LP, j = e % LP;
-    double v;
-    if (i < L && j < L)
-      v = j >= i ? a[i * L + j] : 0.0;
-    else
-      v = i == j ? 1.0 : 0.0;
-    R[e] = v;
-  }
-  __syncthreads();
-  // Rinv column c: X[c][c] = 1/R[c][c]; X[i][c] = -(sum_{t=i+1..c} R[i][t] X[t][c]) / R[i][i]
-  for (int c = tid; c < LP; c += blockDim.x) {
-    for (int i = LP - 1; i >= 0; --i) {
-      double v;
-      if (i > c) {
-        v = 0.0;
-      } else if (i >= L) {
-        v = i == c ? 1.0 : 0.0;
-      } else if (i == c) {
-        v = 1.0 / a[i * L + i];
-      } else {
-        double s = 0.0;
-        for (int t = i + 1; t <= c && t < L; ++t) s += a[i * L + t] * Rinv[t * LP + c];
-        v = -s / a[i * L + i];
-      }
-      Rinv[i * LP + c] = v;
+  for (int k = L - 1; k >= 0; --k) {
+    const dd rk = rdg[k];
+    for (int c = k + tid; c < L; c += nt) x[k * L + c] = dd_mul(x[k * L + c], rk);
+    __syncthreads();
+    const int w = L - k;  // columns k .. L-1
+    for (int e = tid; e < k * w; e += nt) {
+      const int i = e / w, c = k + e % w;
+      x[i * L + c] = dd_fms(x[i * L + c], a[i * L + k], x[k * L + c]);
     }
+    __syncthreads();
+  }
+  for (int e = tid; e < LP * LP; e += nt) {
+    const int i = e / LP, j = e % LP;
+    double v, w;
+    if (i < L && j < L) {
+      v = j > i ? dd_to_double(a[i * L + j]) : (j == i ? dd_to_double(dg[i]) : 0.0);
+      w = j >= i ? dd_to_double(x[i * L + j]) : 0.0;
+    } else {
+      v = w = i == j ? 1.0 : 0.0;
+    }
+    R[e] = v;
+    Rinv[e] = w;
   }
   if (tid == 0) *status = fail;
 }
 
-// C[rows x n] = A[rows x LP] * B[LP x n]; B and a 32-row tile of A in shared
-// memory as float pairs; thread (row r, column group cg) forms columns cg,
-// cg+8, ... in FP32 pairs.  C may alias A (ldc == LP, n <= LP): each CTA reads
-// a row tile into shared memory before it writes the same rows.
+// C[rows x n] = A[rows x LP] * B[LP x n]; B (zero-padded to a multiple of 48
+// columns) and a 32-row tile of A in shared memory as float pairs.  Thread
+// (row pair rp, column lane cg) forms rows 2rp, 2rp+1 and columns cg, cg+16,
+// cg+32 of each 48-column chunk in FP32 pairs, so every pair of operands it
+// loads serves three or two products.  C may alias A (ldc == LP, n <= LP):
+// each CTA reads a row tile into shared memory before it writes the same rows.
+constexpr int kTallCols = 48;
 __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows, int LP,
                                                    const double* __restrict__ B, int ldb, int n, double* C,
                                                    int ldc) {
   extern __shared__ float smf[];
-  float* Bh = smf;              // LP x n
-  float* Bl = Bh + LP * n;
-  float* Ah = Bl + LP * n;      // 32 x LP
-  float* Al = Ah + kRowsTile * LP;
+  const int npd = (n + kTallCols - 1) / kTallCols * kTallCols;
+  float* Bh = smf;              // LP x npd
+  float* Bl = Bh + LP * npd;
+  const int las = LP + 1;       // row stride of the A tile (odd: no bank conflicts between row pairs)
+  float* Ah = Bl + LP * npd;    // 32 x las
+  float* Al = Ah + kRowsTile * las;
   const int tid = threadIdx.x;
-  for (int e = tid; e < LP * n; e += blockDim.x) fp_split(B[(e / n) * ldb + (e % n)], Bh[e], Bl[e]);
-  const int r = tid >> 3, cg = tid & 7;
+  for (int e = tid; e < LP * npd; e += blockDim.x) {
+    const int t = e / npd, c = e % npd;
+    fp_split(c < n ? B[t * ldb + c] : 0.0, Bh[e], Bl[e]);
+  }
+  const int r = 2 * (tid >> 4), cg = tid & 15;
   for (int64_t rt = (int64_t)blockIdx.x * kRowsTile; rt < rows; rt += (int64_t)gridDim.x * kRowsTile) {
     __syncthreads();
     for (int e = tid; e < kRowsTile * LP; e += blockDim.x) {
-      const int64_t row = rt + e / LP;
-      fp_split(row < rows ? A[row * LP + (e % LP)] : 0.0, Ah[e], Al[e]);
+      const int rr = e / LP, cc = e % LP;
+      const int64_t row = rt + rr;
+      fp_split(row < rows ? A[row * LP + cc] : 0.0, Ah[rr * las + cc], Al[rr * las + cc]);
     }
     __syncthreads();
-    const int64_t row = rt + r;
-    if (row < rows) {
-      for (int c = cg; c < n; c += 8) {
-        FloatPair s;
-#pragma unroll 8
-        for (int t = 0; t < LP; ++t) fp_add_prod2(s, Ah[r * LP + t], Al[r * LP + t], Bh[t * n + c], Bl[t * n + c]);
-        C[row * ldc + c] = fp_value(s);
+    const int64_t row0 = rt + r;
+    for (int c0 = 0; c0 < n; c0 += kTallCols) {
+      FloatPair s[2][3];
+      const float* a0h = Ah + r * las;
+      const float* a0l = Al + r * las;
+      const float* bh = Bh + c0 + cg;
+      const float* bl = Bl + c0 + cg;
+#pragma unroll 4
+      for (int t = 0; t < LP; ++t) {
+        const float x0h = a0h[t], x0l = a0l[t], x1h = a0h[las + t], x1l = a0l[las + t];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          const float yh = bh[t * npd + 16 * q], yl = bl[t * npd + 16 * q];
+          fp_add_prod2(s[0][q], x0h, x0l, yh, yl);
+          fp_add_prod2(s[1][q], x1h, x1l, yh, yl);
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (row0 + h < rows) {
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const int c = c0 + cg + 16 * q;
+            if (c < n) C[(row0 + h) * ldc + c] = fp_value(s[h][q]);
+          }
+        }
       }
     }
   }
@@ -218,7 +270,8 @@ __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows
 // then eliminate below the pivot.  Mirrors beta = -sign(c0)*norm of the
 // reflector (Eigen makeHouseholder; LAPACK dlarfg).
 __global__ void k_house_signs(const double* __restrict__ Q, int L, int LP, double* __restrict__ sgn) {
-  extern __shared__ double a[];  // L x L
+  extern __shared__ double a[];  // L x L, then L multipliers
+  double* mult = a + L * L;
   const int tid = threadIdx.x;
   for (int e = tid; e < L * L; e += blockDim.x) a[e] = Q[(e / L) * LP + (e % L)];
   __syncthreads();
@@ -231,9 +284,13 @@ __global__ void k_house_signs(const double* __restrict__ Q, int L, int LP, doubl
     __syncthreads();
     const int m = L - i - 1;
     const double piv = a[i * L + i];
+    // multipliers first (column i below the pivot, in its own buffer), then
+    // the trailing update with the same rounding as a[r][i] / piv * a[i][c]
+    for (int r = i + 1 + tid; r < L; r += blockDim.x) mult[r] = a[r * L + i] / piv;
+    __syncthreads();
     for (int e = tid; e < m * m; e += blockDim.x) {
       const int r = i + 1 + e / m, c = i + 1 + e % m;
-      a[r * L + c] -= a[r * L + i] / piv * a[i * L + c];
+      a[r * L + c] -= mult[r] * a[i * L + c];
     }
     __syncthreads();
   }
@@ -246,31 +303,53 @@ __global__ void k_scale_cols(double* __restrict__ Q, int64_t rows, int LP, const
   Q[idx] *= sgn[idx % LP];
 }
 
-// column sums of |o2 - o| and |o2 + o| over a slab of rows
-__global__ void k_flip_partial(const double* __restrict__ o2, const double* __restrict__ o, int64_t rows, int LP,
-                               int64_t rows_per_block, double* __restrict__ part) {
-  const int c = threadIdx.x;
-  if (c >= LP) return;
+// column sums of |o2 - o| and |o2 + o| over a slab of rows: coalesced loads
+// (thread t keeps column t % LP), then the threads of each column combined in
+// shared memory
+__global__ void __launch_bounds__(256) k_flip_partial(const double* __restrict__ o2, const double* __restrict__ o,
+                                                      int64_t rows, int LP, int64_t rows_per_block,
+                                                      double* __restrict__ part) {
+  __shared__ double rm[256], rp[256];
+  const int tid = threadIdx.x;
+  const int step = (256 / LP) * LP;
   const int64_t r0 = blockIdx.x * rows_per_block, r1 = min(r0 + rows_per_block, rows);
   double dm = 0.0, dp = 0.0;
-  for (int64_t r = r0; r < r1; ++r) {
-    const double a = o2[r * LP + c], b = o[r * LP + c];
-    dm += fabs(a - b);
-    dp += fabs(a + b);
+  if (tid < step) {
+    for (int64_t f = r0 * LP + tid; f < r1 * LP; f += step) {
+      const double a = o2[f], b = o[f];
+      dm += fabs(a - b);
+      dp += fabs(a + b);
+    }
   }
-  part[((size_t)blockIdx.x * 2 + 0) * LP + c] = dm;
-  part[((size_t)blockIdx.x * 2 + 1) * LP + c] = dp;
+  rm[tid] = dm;
+  rp[tid] = dp;
+  __syncthreads();
+  if (tid < LP) {
+    for (int q = tid + LP; q < step; q += LP) {
+      dm += rm[q];
+      dp += rp[q];
+    }
+    part[((size_t)blockIdx.x * 2 + 0) * LP + tid] = dm;
+    part[((size_t)blockIdx.x * 2 + 1) * LP + tid] = dp;
+  }
 }
 
+// one warp per column: the block partials summed by the lanes and a butterfly
 __global__ void k_flip_flags(const double* __restrict__ part, int nblocks, int L, int LP, double* __restrict__ sgn) {
-  const int c = threadIdx.x;
-  if (c >= LP) return;
+  const int c = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= LP) return;  // warp-uniform
   double dm = 0.0, dp = 0.0;
-  for (int b = 0; b < nblocks; ++b) {
+  for (int b = lane; b < nblocks; b += 32) {
     dm += part[((size_t)b * 2 + 0) * LP + c];
     dp += part[((size_t)b * 2 + 1) * LP + c];
   }
-  sgn[c] = (c < L && dm > 2.0 * dp) ? -1.0 : 1.0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    dm += __shfl_xor_sync(0xffffffffu, dm, o);
+    dp += __shfl_xor_sync(0xffffffffu, dp, o);
+  }
+  if (lane == 0) sgn[c] = (c < L && dm > 2.0 * dp) ? -1.0 : 1.0;
 }
 
 __global__ void k_flip_apply(double* __restrict__ o2, double* __restrict__ o, int64_t n, int LP,
@@ -292,13 +371,21 @@ __global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, in
   if (i < n) b[i] = (float)a[i];
 }
 
-// C = A * B for LP x LP row-major (single CTA)
-__global__ void k_mult_small(const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C,
-                             int LP) {
+// C = A * B for LP x LP row-major (single CTA, operands staged in shared memory)
+__global__ void __launch_bounds__(512) k_mult_small(const double* __restrict__ A, const double* __restrict__ B,
+                                                    double* __restrict__ C, int LP) {
+  extern __shared__ double sab[];
+  double* As = sab;
+  double* Bs = sab + LP * LP;
+  for (int e = threadIdx.x; e < LP * LP; e += blockDim.x) {
+    As[e] = A[e];
+    Bs[e] = B[e];
+  }
+  __syncthreads();
   for (int e = threadIdx.x; e < LP * LP; e += blockDim.x) {
     const int i = e / LP, j = e % LP;
     double s = 0.0;
-    for (int t = 0; t < LP; ++t) s = fma(A[i * LP + t], B[t * LP + j], s);
+    for (int t = 0; t < LP; ++t) s = fma(As[i * LP + t], Bs[t * LP + j], s);
     C[e] = s;
   }
 }
@@ -595,7 +682,7 @@ void launch_cross(const double* A, int lda, int na, const double* B, int ldb, in
   else
     launch_cross_q<64>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, s);
   PCAONE_LAUNCH_CHECK();
-  k_cross_reduce<<<ceil_div((int64_t)na * nb, 256), 256, 0, s>>>(part, nblocks, na, nb, sym, W, ldw);
+  k_cross_reduce<<<ceil_div((int64_t)na * nb * 32, 256), 256, 0, s>>>(part, nblocks, na, nb, sym, W, ldw);
   PCAONE_LAUNCH_CHECK();
 }
 
@@ -606,7 +693,7 @@ void launch_chol_inv_shift(const double* W, int L, int LP, double shift, double*
     PCAONE_CUDA(cudaFuncSetAttribute(k_chol_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_set = true;
   }
-  k_chol_inv<<<1, 256, sizeof(double) * L * L, s>>>(W, L, LP, shift, R, Rinv, status);
+  k_chol_inv<<<1, kCholThreads, sizeof(dd) * (2 * L * L + 2 * L), s>>>(W, L, LP, shift, R, Rinv, status);
   PCAONE_LAUNCH_CHECK();
 }
 
@@ -618,7 +705,8 @@ void launch_gemm_tall(const double* A, int64_t rows, int LP, const double* B, in
     PCAONE_CUDA(cudaFuncSetAttribute(k_gemm_tall, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_set = true;
   }
-  const size_t smem = 2 * sizeof(float) * ((size_t)LP * n + (size_t)kRowsTile * LP);
+  const size_t npd = (size_t)(n + kTallCols - 1) / kTallCols * kTallCols;
+  const size_t smem = 2 * sizeof(float) * ((size_t)LP * npd + (size_t)kRowsTile * (LP + 1));
   const int grid = (int)std::min<int64_t>((rows + kRowsTile - 1) / kRowsTile, 152 * 8);
   k_gemm_tall<<<grid, 256, smem, s>>>(A, rows, LP, B, ldb, n, C, ldc);
   PCAONE_LAUNCH_CHECK();
@@ -630,7 +718,7 @@ void launch_house_signs(double* Q, int64_t rows, int L, int LP, double* sgn, cud
     PCAONE_CUDA(cudaFuncSetAttribute(k_house_signs, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_set = true;
   }
-  k_house_signs<<<1, 256, sizeof(double) * L * L, s>>>(Q, L, LP, sgn);
+  k_house_signs<<<1, 256, sizeof(double) * (L * L + L), s>>>(Q, L, LP, sgn);
   PCAONE_LAUNCH_CHECK();
   k_scale_cols<<<ceil_div(rows * LP, 256), 256, 0, s>>>(Q, rows, LP, sgn);
   PCAONE_LAUNCH_CHECK();
@@ -643,9 +731,10 @@ void launch_flip_omg(double* omg2, double* omg, int64_t rows, int L, int LP, dou
   int nb = flip_blocks(rows);
   const int64_t per = (rows + nb - 1) / nb;
   nb = (int)((rows + per - 1) / per);
-  k_flip_partial<<<nb, 128, 0, s>>>(omg2, omg, rows, LP, per, part);
+  if (LP > 256) throw Error(-6, "flipOmg: sketch wider than 256 columns");
+  k_flip_partial<<<nb, 256, 0, s>>>(omg2, omg, rows, LP, per, part);
   PCAONE_LAUNCH_CHECK();
-  k_flip_flags<<<1, 128, 0, s>>>(part, nb, L, LP, sgn);
+  k_flip_flags<<<ceil_div((int64_t)LP * 32, 256), 256, 0, s>>>(part, nb, L, LP, sgn);
   PCAONE_LAUNCH_CHECK();
   k_flip_apply<<<ceil_div(rows * LP, 256), 256, 0, s>>>(omg2, omg, rows * LP, LP, sgn);
   PCAONE_LAUNCH_CHECK();
@@ -664,7 +753,12 @@ void launch_to_f32(const double* a, float* b, int64_t n, cudaStream_t s) {
 }
 
 void launch_mult_small(const double* A, const double* B, double* C, int LP, cudaStream_t s) {
-  k_mult_small<<<1, 256, 0, s>>>(A, B, C, LP);
+  static bool attr_set = false;
+  if (!attr_set) {
+    PCAONE_CUDA(cudaFuncSetAttribute(k_mult_small, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
+    attr_set = true;
+  }
+  k_mult_small<<<1, 512, sizeof(double) * 2 * LP * LP, s>>>(A, B, C, LP);
   PCAONE_LAUNCH_CHECK();
 }
 

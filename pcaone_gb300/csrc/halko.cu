@@ -147,6 +147,8 @@ struct Context {
   DBuf<unsigned long long> gisum, gesum, hisum, hesum;
   DBuf<int> wexp, hexp;
   DBuf<int> err;
+  DBuf<double> cr_part;    // column-reduction partials (tc::kColRedBlocks x LP)
+  DBuf<unsigned> cr_cnt;   // its completion counter, zero between launches
   CUtensorMap map_bed_g{}, map_bed_h{}, map_w{}, map_gt{};
   int ldg = 0, win_max = 0;
   int nslice_cur = 1, w_slices = 0;
@@ -403,6 +405,8 @@ static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
   c.wexp.ensure(LP, c.stream);
   c.hexp.ensure(LP, c.stream);
   c.err.ensure(1, c.stream);
+  c.cr_part.ensure((size_t)tc::kColRedBlocks * LP, c.stream, false);
+  c.cr_cnt.ensure(1, c.stream, true);
   c.part.ensure(std::max(need_part, c.part.n), c.stream, false);
   c.hpart.ensure(std::max(need_hpart, c.hpart.n), c.stream, false);
   c.bed_work = c.bed.p;
@@ -535,9 +539,10 @@ static int read_status(Context& c) {
 
 // Orthonormal factor of A (rows x LP, in place) by CholeskyQR2, or shifted
 // CholeskyQR3 when the first Gram is not numerically positive definite
-// (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa 2020).  On return Rt
-// holds R (upper, A_in = Q R) and Rti its inverse.
-static void cholqr(Context& c, double* A, int64_t rows) {
+// (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa 2020).  With need_r, Rt
+// holds R (upper, A_in = Q R) and Rti its inverse on return; the updates of
+// Omega only need Q.
+static void cholqr(Context& c, double* A, int64_t rows, bool need_r) {
   const int L = c.L, LP = c.LP;
   const int nb = cross_blocks(rows);
   launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream);
@@ -559,17 +564,21 @@ static void cholqr(Context& c, double* A, int64_t rows) {
   launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R2.p, c.R2i.p, c.status.p, c.stream);
   if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: second Gram not positive definite");
   launch_gemm_tall(A, rows, LP, c.R2i.p, LP, LP, A, LP, c.stream);
-  launch_mult_small(c.R2.p, c.R1.p, c.Rt.p, LP, c.stream);     // R = R2 R1
-  launch_mult_small(c.R1i.p, c.R2i.p, c.Rti.p, LP, c.stream);  // R^-1 = R1^-1 R2^-1
+  if (need_r) {
+    launch_mult_small(c.R2.p, c.R1.p, c.Rt.p, LP, c.stream);     // R = R2 R1
+    launch_mult_small(c.R1i.p, c.R2i.p, c.Rti.p, LP, c.stream);  // R^-1 = R1^-1 R2^-1
+  }
   if (shifted) {
     launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream);
     launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R3.p, c.R3i.p, c.status.p, c.stream);
     if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: third Gram not positive definite");
     launch_gemm_tall(A, rows, LP, c.R3i.p, LP, LP, A, LP, c.stream);
-    launch_mult_small(c.R3.p, c.Rt.p, c.R1.p, LP, c.stream);
-    launch_mult_small(c.Rti.p, c.R3i.p, c.R1i.p, LP, c.stream);
-    PCAONE_CUDA(cudaMemcpyAsync(c.Rt.p, c.R1.p, (size_t)LP * LP * 8, cudaMemcpyDeviceToDevice, c.stream));
-    PCAONE_CUDA(cudaMemcpyAsync(c.Rti.p, c.R1i.p, (size_t)LP * LP * 8, cudaMemcpyDeviceToDevice, c.stream));
+    if (need_r) {
+      launch_mult_small(c.R3.p, c.Rt.p, c.R1.p, LP, c.stream);
+      launch_mult_small(c.Rti.p, c.R3i.p, c.R1i.p, LP, c.stream);
+      PCAONE_CUDA(cudaMemcpyAsync(c.Rt.p, c.R1.p, (size_t)LP * LP * 8, cudaMemcpyDeviceToDevice, c.stream));
+      PCAONE_CUDA(cudaMemcpyAsync(c.Rti.p, c.R1i.p, (size_t)LP * LP * 8, cudaMemcpyDeviceToDevice, c.stream));
+    }
   }
 }
 
@@ -578,7 +587,7 @@ static void cholqr(Context& c, double* A, int64_t rows) {
 static void update_omega_from_h(Context& c) {
   const size_t nl = (size_t)c.npad * c.LP;
   PCAONE_CUDA(cudaMemcpyAsync(c.Omg.p, c.H.p, nl * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
-  cholqr(c, c.Omg.p, c.N);
+  cholqr(c, c.Omg.p, c.N, false);
   launch_house_signs(c.Omg.p, c.N, c.L, c.LP, c.sgn.p, c.stream);
   launch_flip_omg(c.Omg2.p, c.Omg.p, c.N, c.L, c.LP, c.red.p, c.sgn.p, c.stream);
   launch_to_f32(c.Omg.p, c.Omg32.p, (int64_t)nl, c.stream);
@@ -733,7 +742,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   const int LP = c.LP, S = c.nslice_cur;
   if (c.w_slices != S) {
     tc::launch_omega_slices(c.Omg.p, c.npad, c.N, LP, S, c.wsl.p, c.wunit.p, c.colsum.p, c.wexp.p, c.wrep.p,
-                            c.wint.p, c.dense, c.stream);
+                            c.wint.p, c.dense, tc::ColRedScratch{c.cr_part.p, c.cr_cnt.p}, c.stream);
     c.w_slices = S;
   }
   int chunk, nch, per, nsp;
@@ -766,8 +775,8 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ga.chunk = chunk;
   ga.npad = c.npad;
   ga.nchunks = nch;
-  ga.nstages = tc::stages_for(LP, S, tc::g_tile_bytes(c.dense));
-  ga.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ga.nstages));
+  ga.nstages = tc::stages_for(LP, S, tc::g_tile_bytes(c.dense), c.dense);
+  ga.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ga.nstages, c.dense));
   ga.wscale = c.wunit.p;
   ga.part = c.part.p;
   ga.err = c.err.p;
@@ -818,7 +827,8 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   fa.gmint = c.gmint.p;
   fa.gt = c.gt.p;
   fa.cpart = c.cpart.p;
-  tc::launch_g_finish(fa, c.hexp.p, c.hunit.p, c.gmunit.p, c.cvec.p, c.stream);
+  tc::launch_g_finish(fa, c.hexp.p, c.hunit.p, c.gmunit.p, c.cvec.p, tc::ColRedScratch{c.cr_part.p, c.cr_cnt.p},
+                      c.stream);
   tc::HArgs ha{};
   ha.pos0 = pos0;
   ha.nsnp = (int)n;
@@ -828,8 +838,8 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ha.per_split = per;
   ha.nsplit = nsp;
   ha.npad = c.npad;
-  ha.nstages = tc::stages_for(LP, S, tc::h_tile_bytes(c.dense));
-  ha.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ha.nstages));
+  ha.nstages = tc::stages_for(LP, S, tc::h_tile_bytes(c.dense), c.dense);
+  ha.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ha.nstages, c.dense));
   ha.hscale = c.hunit.p;
   ha.hpart = c.hpart.p;
   ha.err = c.err.p;
@@ -988,7 +998,7 @@ static int compute_usv(Context& c, int p, double tol) {
     auto t1 = clk::now();
     c.t_prod += secs(t0, t1);
     ++epochs;
-    cholqr(c, c.G.p, M);  // G <- Q2, Rt = R2 R1
+    cholqr(c, c.G.p, M, true);  // G <- Q2, Rt = R2 R1
     launch_cross(c.H.p, LP, L, c.H.p, LP, L, N, 1, c.W.p, LP, c.red.p, cross_blocks(N), c.stream);
     launch_usv_small(c.Rti.p, c.W.p, L, LP, k, c.UB.p, c.sigma.p, c.T.p, c.tmp.p, c.status.p + 1, c.stream);
     // Ucur = H T (right singular vectors of B = R^{-T} H^T)

@@ -31,15 +31,16 @@
 //            bytes into the BF16 dosage operand D, written straight into TMEM
 //            (tcgen05.st); tcgen05.mma (A from TMEM, B from shared memory, the
 //            S slices concatenated along N) accumulates D*W in TMEM; the
-//            epilogue (tcgen05.ld) writes FP32 partial sums, combined in FP64
-//            by k_tc_g_finish.
+//            epilogue (tcgen05.ld) writes FP32 partial sums, combined by
+//            k_tc_g_finish.
 //   k_tc_h : tile of 128 samples x one split of the window's SNPs.  TMA brings
 //            the packed tile (64 SNP rows x 32 bytes) and the Gh^T slice tiles;
 //            decoder warps transpose into the D^T A operand.
 //
 // Dense input (FileBinary values held as FP16, src/FileBinary.cpp:54-64): the
 // same kernels with kDense, where the A tile is FP16 values instead of packed
-// codes (copied, or transposed for H, into TMEM), the slices are FP16 integer
+// codes (copied, or transposed for H, into a 128B-swizzled A tile in shared
+// memory, so that both MMA operands come from shared memory), the slices are FP16 integer
 // digits (both operands of kind::f16 FP16), the centring is by the per-SNP
 // mean mu with no scale (x = v - mu), and the FP32 accumulation is ordinary
 // rounding arithmetic since the values are not integers.
@@ -146,6 +147,36 @@ __device__ __forceinline__ void mma_bf16_ta(uint32_t d_tmem, uint32_t a_tmem, ui
       : "memory");
 }
 
+// D[tmem] (+)= A[smem desc] * B[smem desc]^T, kind::f16 (both operands K-major
+// in shared memory)
+__device__ __forceinline__ void mma_bf16_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                            uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// generic-proxy shared-memory writes made visible to the async proxy (the
+// tensor core reads the decoded A operand)
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// one decoder thread's 64 bytes of an A row (K elements 32ch .. 32ch+31 of row
+// r) into the 128B-swizzled K-major tile: 16-byte chunk c of row r sits at
+// chunk position c ^ (r & 7)
+__device__ __forceinline__ void st_a_row(uint8_t* tile, int r, int ch, const uint32_t* wd) {
+  uint8_t* row = tile + r * 128;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int cpos = (ch * 4 + q) ^ (r & 7);
+    *reinterpret_cast<uint4*>(row + cpos * 16) = make_uint4(wd[4 * q], wd[4 * q + 1], wd[4 * q + 2], wd[4 * q + 3]);
+  }
+}
+
 // 32 lanes x 16 consecutive 32-bit columns from registers into TMEM
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* r) {
   asm volatile(
@@ -212,15 +243,26 @@ __device__ __forceinline__ uint32_t dosage_pair(uint32_t x) {
 
 
 struct SmemLayout {
-  uint32_t b, p, stage_bytes;
+  uint32_t b, a, p, stage_bytes;
 };
 
 // one pipeline stage in shared memory: the B slices (nslice * LP rows of 128
-// bytes, 128B-swizzled) and the packed tile; the A operand lives in TMEM
-__host__ __device__ inline SmemLayout layout_for(int LP, int nslice, int pbytes) {
+// bytes, 128B-swizzled), for dense input the A tile (128 rows of 64 FP16 K
+// elements, the same layout), and the packed (or FP16) input tile.  LP is a
+// multiple of 16, so every region starts on a 1024-byte swizzle atom.
+//
+// Where the A operand lives: genotype A tiles go to TMEM (tcgen05.st), dense
+// ones to shared memory.  With A in shared memory the MMAs read both operands
+// there, which on the 100,000 x 7,812 genotype window made the products 20%
+// (two CTAs per SM) to 50% (one CTA) slower than A in TMEM; for FP16 input,
+// whose A tile is a copy rather than a decode, shared memory was 18% faster
+// end to end (100,000 x 100,000).
+constexpr uint32_t kATileBytes = 128 * 128;
+__host__ __device__ inline SmemLayout layout_for(int LP, int nslice, int pbytes, bool a_smem) {
   SmemLayout s{};
   s.b = 0;
-  s.p = (uint32_t)(nslice * LP * 128);
+  s.a = (uint32_t)(nslice * LP * 128);
+  s.p = s.a + (a_smem ? kATileBytes : 0u);
   s.stage_bytes = (s.p + (uint32_t)pbytes + 1023u) & ~1023u;
   return s;
 }
@@ -233,13 +275,18 @@ __host__ __device__ inline SmemLayout layout_for(int LP, int nslice, int pbytes)
 // MMA shape limit for M = 128: N <= 256 columns.
 constexpr int kMaxNTmemA = 256;
 
-template <bool kF16>
-__device__ __forceinline__ void mma_cat(uint32_t tmem_col0, uint32_t a_tmem, uint32_t b_addr, int ncols,
+// a_addr: TMEM address of the A operand (!kASmem) or its shared-memory
+// address (kASmem)
+template <bool kF16, bool kASmem>
+__device__ __forceinline__ void mma_cat(uint32_t tmem_col0, uint32_t a_addr, uint32_t b_addr, int ncols,
                                         uint32_t accumulate) {
   for (int n0 = 0; n0 < ncols; n0 += kMaxNTmemA) {
     const int n = min(kMaxNTmemA, ncols - n0);
-    mma_bf16_ta(tmem_col0 + n0, a_tmem, desc_sw128(b_addr + n0 * 128), kF16 ? idesc_f16(128, n) : idesc_bf16(128, n),
-                accumulate);
+    const uint32_t id = kF16 ? idesc_f16(128, n) : idesc_bf16(128, n);
+    if constexpr (kASmem)
+      mma_bf16_ss(tmem_col0 + n0, desc_sw128(a_addr), desc_sw128(b_addr + n0 * 128), id, accumulate);
+    else
+      mma_bf16_ta(tmem_col0 + n0, a_addr, desc_sw128(b_addr + n0 * 128), id, accumulate);
   }
 }
 
@@ -282,6 +329,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   // A tile per stage: 128 SNP rows x 64 samples, packed (16 B per row) or FP16
   // (128 B per row, 128-byte swizzle)
   constexpr int kTileBytes = kDense ? 128 * 128 : 128 * 16;
+  constexpr bool kASmem = kDense;  // A operand in shared memory (else TMEM)
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   __shared__ uint64_t full_bar[kMaxStages], dec_bar[kMaxStages], empty_bar[kMaxStages], acc_bar;
@@ -290,7 +338,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   __shared__ float unit[3 * 112];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int LP = a.LP, S = a.nslice;
-  const SmemLayout lay = layout_for(LP, S, kTileBytes);
+  const SmemLayout lay = layout_for(LP, S, kTileBytes, kASmem);
   const int row0 = blockIdx.x * 128;                  // window-local first SNP of the tile
   const int kbeg = blockIdx.y * a.chunk;
   const int kend = min(kbeg + a.chunk, a.npad);
@@ -314,8 +362,8 @@ __global__ void __launch_bounds__(kThreads, 2)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_sh;
-  // TMEM columns: accumulators [0, ncat), then per stage the dosage operand
-  // (32 columns = 64 BF16 K elements)
+  // TMEM columns: accumulators [0, ncat), then (A in TMEM) per stage the dosage
+  // operand (32 columns = 64 BF16 K elements)
   const uint32_t a_col0 = (uint32_t)ncat;
 
   if (warp == 0) {
@@ -351,9 +399,17 @@ __global__ void __launch_bounds__(kThreads, 2)
         tc_fence_after();
         uint8_t* base = smem + st * lay.stage_bytes;
         const uint32_t bb = smem_u32(base + lay.b);
-        const uint32_t ad = tmem + a_col0 + st * 32;
+        if constexpr (kASmem) {
+          const uint32_t aa = smem_u32(base + lay.a);
 #pragma unroll
-        for (int kk = 0; kk < kStepK / 16; ++kk) mma_cat<kDense>(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
+          for (int kk = 0; kk < kStepK / 16; ++kk)
+            mma_cat<kDense, true>(tmem, aa + kk * 32, bb + kk * 32, ncat, (kb | kk) != 0);
+        } else {
+          const uint32_t ad = tmem + a_col0 + st * 32;
+#pragma unroll
+          for (int kk = 0; kk < kStepK / 16; ++kk)
+            mma_cat<kDense, false>(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
+        }
         mma_commit(&empty_bar[st]);
       }
       mma_commit(&acc_bar);  // arrives once every MMA above has completed
@@ -361,7 +417,8 @@ __global__ void __launch_bounds__(kThreads, 2)
   } else if (warp >= kDecodeWarp0) {
     // ---- decoders: TMEM lane quarter q4 = warp % 4 (row r = SNP 32*q4 + lane of
     // the tile), K half ch: samples 32ch .. 32ch+31 of the step (8 packed bytes)
-    // -> 16 columns of BF16 pairs into the stage's operand in TMEM ----
+    // -> 16 columns of BF16 pairs into the stage's operand in TMEM (or, for
+    // dense input, 32 FP16 values into the stage's A tile) ----
     const int q4 = warp & 3, ch = (warp - kDecodeWarp0) >> 2;
     const int r = q4 * 32 + lane;
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
@@ -392,9 +449,14 @@ __global__ void __launch_bounds__(kThreads, 2)
           wd[e] = dosage_pair(((w32 >> sh) & 3u) | (((w32 >> (sh + 2)) & 3u) << 16));
         }
       }
-      tmem_st16(tmem + lane_off + a_col0 + st * 32 + ch * 16, wd);
-      tmem_wait_st();
-      tc_fence_before();
+      if constexpr (kASmem) {
+        st_a_row(base + lay.a, r, ch, wd);
+        fence_proxy_async_smem();
+      } else {
+        tmem_st16(tmem + lane_off + a_col0 + st * 32 + ch * 16, wd);
+        tmem_wait_st();
+        tc_fence_before();
+      }
       mbar_arrive(&dec_bar[st]);
     }
     // ---- epilogue: exact integer slice sums times power-of-two units (FP32 FMAs) ----
@@ -438,6 +500,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   // (256 B per row, unswizzled)
   constexpr int kRowBytes = kDense ? 256 : 32;
   constexpr int kTileBytes = 64 * kRowBytes;
+  constexpr bool kASmem = kDense;  // A operand in shared memory (else TMEM)
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   __shared__ uint64_t full_bar[kMaxStages], dec_bar[kMaxStages], empty_bar[kMaxStages], acc_bar;
@@ -447,7 +510,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   __shared__ float munit[2 * 112];  // units of the missing-entry sums (Gm integers, EM products)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int LP = a.LP, S = a.nslice;
-  const SmemLayout lay = layout_for(LP, S, kTileBytes);
+  const SmemLayout lay = layout_for(LP, S, kTileBytes, kASmem);
   const int samp0 = blockIdx.x * 128;
   const int jb = blockIdx.y * a.per_split;
   const int je = min(jb + a.per_split, a.nsnp);
@@ -475,6 +538,8 @@ __global__ void __launch_bounds__(kThreads, 2)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_sh;
+  // TMEM columns: accumulators [0, ncat), then (A in TMEM) per stage the dosage
+  // operand (32 columns = 64 BF16 K elements)
   const uint32_t a_col0 = (uint32_t)ncat;
 
   if (warp == 0) {
@@ -508,9 +573,17 @@ __global__ void __launch_bounds__(kThreads, 2)
         tc_fence_after();
         uint8_t* base = smem + st * lay.stage_bytes;
         const uint32_t bb = smem_u32(base + lay.b);
-        const uint32_t ad = tmem + a_col0 + st * 32;
+        if constexpr (kASmem) {
+          const uint32_t aa = smem_u32(base + lay.a);
 #pragma unroll
-        for (int kk = 0; kk < kStepK / 16; ++kk) mma_cat<kDense>(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
+          for (int kk = 0; kk < kStepK / 16; ++kk)
+            mma_cat<kDense, true>(tmem, aa + kk * 32, bb + kk * 32, ncat, (kb | kk) != 0);
+        } else {
+          const uint32_t ad = tmem + a_col0 + st * 32;
+#pragma unroll
+          for (int kk = 0; kk < kStepK / 16; ++kk)
+            mma_cat<kDense, false>(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
+        }
         mma_commit(&empty_bar[st]);
       }
       mma_commit(&acc_bar);
@@ -518,7 +591,8 @@ __global__ void __launch_bounds__(kThreads, 2)
   } else if (warp >= kDecodeWarp0) {
     // ---- decoders: TMEM lane quarter q4 (row r = sample 32*q4 + lane of the
     // tile), K half ch: SNPs 32ch .. 32ch+31 of the step, one packed byte each
-    // (column r/4 of the SNP row) -> 16 columns of BF16 pairs in TMEM ----
+    // (column r/4 of the SNP row) -> 16 columns of BF16 pairs in TMEM (or, for
+    // dense input, 32 FP16 values into the stage's A tile) ----
     const int q4 = warp & 3, ch = (warp - kDecodeWarp0) >> 2;
     const int r = q4 * 32 + lane;
     const int sh = 2 * (r & 3);
@@ -526,6 +600,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     for (int kb = 0; kb < nk; ++kb) {
       const int st = kb % nst;
       if (!role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
+      uint8_t* base = smem + st * lay.stage_bytes;
       uint32_t wd[16];
       if (kDense) {
         // value of SNP row j, sample r at j*256 + 2r: lanes read neighbouring
@@ -544,9 +619,14 @@ __global__ void __launch_bounds__(kThreads, 2)
           wd[e] = dosage_pair(((b0 >> sh) & 3u) | (((b1 >> sh) & 3u) << 16));
         }
       }
-      tmem_st16(tmem + lane_off + a_col0 + st * 32 + ch * 16, wd);
-      tmem_wait_st();
-      tc_fence_before();
+      if constexpr (kASmem) {
+        st_a_row(base + lay.a, r, ch, wd);
+        fence_proxy_async_smem();
+      } else {
+        tmem_st16(tmem + lane_off + a_col0 + st * 32 + ch * 16, wd);
+        tmem_wait_st();
+        tc_fence_before();
+      }
       mbar_arrive(&dec_bar[st]);
     }
     const bool ok = nk > 0 && role_wait(&acc_bar, 0u, &abort_sh);
@@ -604,24 +684,68 @@ __global__ void __launch_bounds__(kThreads, 2)
 // FP64 epilogues and operand preparation
 // ---------------------------------------------------------------------------
 
-// Per-column exponent E_l with max_r |A_rl| < 2^E_l over rows [0, rows) of a
-// row-major FP64 matrix (ld LP); one block per column.
-__global__ void k_col_exponent(const double* __restrict__ A, int64_t rows, int LP, int* __restrict__ E) {
-  const int l = blockIdx.x;
-  double m = 0.0;
-  for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) m = fmax(m, fabs(A[r * LP + l]));
+// Column reductions of a row-major FP64 matrix (rows x LP): the maximum of
+// |A| (kMax; the result is the exponent E_l with max_r |A_rl| < 2^E_l) or the
+// sum.  Block b reduces rows [b*per, (b+1)*per) with coalesced loads (thread t
+// keeps column t % LP) and writes one partial per column; the last block to
+// finish combines the partials in block order, so the result does not depend
+// on the order in which blocks run.  cnt is zero on entry and again on exit.
+template <bool kMax>
+__global__ void __launch_bounds__(256) k_colred(const double* __restrict__ A, int64_t rows, int LP, int64_t per,
+                                               double* __restrict__ part, unsigned* __restrict__ cnt,
+                                               double* __restrict__ sum_out, int* __restrict__ exp_out) {
   __shared__ double red[256];
-  red[threadIdx.x] = m;
+  __shared__ bool last;
+  const int tid = threadIdx.x;
+  const int step = (256 / LP) * LP;
+  const int64_t r0 = (int64_t)blockIdx.x * per;
+  const int64_t r1 = r0 + per < rows ? r0 + per : rows;
+  double v = 0.0;
+  if (tid < step) {
+    const int64_t f1 = r1 * LP;
+    for (int64_t f = r0 * LP + tid; f < f1; f += step) {
+      const double x = A[f];
+      v = kMax ? fmax(v, fabs(x)) : v + x;
+    }
+  }
+  red[tid] = v;
   __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
-    __syncthreads();
+  if (tid < LP) {
+    double t = red[tid];
+    for (int q = tid + LP; q < step; q += LP) t = kMax ? fmax(t, red[q]) : t + red[q];
+    part[(size_t)blockIdx.x * LP + tid] = t;
   }
-  if (threadIdx.x == 0) {
-    int e = 0;
-    if (red[0] > 0.0) frexp(red[0], &e);  // red = m * 2^e, 0.5 <= m < 1, so |A| < 2^e
-    E[l] = e;
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // one warp per column: the lanes combine blocks lane, lane+32, ..., then a
+  // butterfly (a fixed order)
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int l = warp; l < LP; l += 8) {
+    double t = 0.0;
+    for (unsigned b = lane; b < gridDim.x; b += 32) {
+      const double x = __ldcg(part + (size_t)b * LP + l);
+      t = kMax ? fmax(t, x) : t + x;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double y = __shfl_xor_sync(0xffffffffu, t, o);
+      t = kMax ? fmax(t, y) : t + y;
+    }
+    if (lane == 0) {
+      if (kMax) {
+        int e = 0;
+        if (t > 0.0) frexp(t, &e);  // t = m * 2^e, 0.5 <= m < 1, so |A| < 2^e
+        exp_out[l] = e;
+      } else {
+        sum_out[l] = t;
+      }
+    }
   }
+  if (tid == 0) *cnt = 0u;
 }
 
 // Split v (|v| < 2^E) into S integer slices: m = rint(v * 2^(8S-1-E)) has
@@ -650,17 +774,30 @@ __device__ __forceinline__ double split_store(double v, int E, int S, uint16_t* 
 
 // W slices of Omega (S*LP rows x npad, K-major) and the represented W, in FP64
 // and as the integer m (|m| <= 2^23; the value is m times the last slice unit).
-__global__ void k_omega_slices(const double* __restrict__ omg, int npad, int N, int LP, int S,
-                               const int* __restrict__ E, uint16_t* __restrict__ w, double* __restrict__ rep,
-                               int32_t* __restrict__ wint, int f16) {
-  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (idx >= (int64_t)npad * LP) return;
-  const int i = (int)(idx / LP), l = (int)(idx % LP);
-  const double v = i < N ? omg[idx] : 0.0;
-  int m = 0;
-  const double r = split_store(v, E[l], S, w + (size_t)l * npad + i, (size_t)LP * npad, f16 != 0, &m);
-  rep[idx] = r;
-  wint[idx] = m;
+// A block takes 64 rows of Omega (coalesced reads, and coalesced writes of the
+// represented values), keeps their digits in shared memory and writes each
+// slice row's 64 digits as one 128-byte run.  npad is a multiple of 64.
+constexpr int kOmgRows = 64;
+__global__ void __launch_bounds__(256) k_omega_slices(const double* __restrict__ omg, int npad, int N, int LP, int S,
+                                                      const int* __restrict__ E, uint16_t* __restrict__ w,
+                                                      double* __restrict__ rep, int32_t* __restrict__ wint, int f16) {
+  __shared__ uint16_t dg[3 * 112 * kOmgRows];  // [s][l][row]
+  const int i0 = blockIdx.x * kOmgRows;
+  for (int e = threadIdx.x; e < kOmgRows * LP; e += blockDim.x) {
+    const int il = e / LP, l = e % LP;
+    const int i = i0 + il;
+    const size_t idx = (size_t)i * LP + l;
+    const double v = i < N ? omg[idx] : 0.0;
+    int m = 0;
+    const double r = split_store(v, E[l], S, dg + l * kOmgRows + il, (size_t)LP * kOmgRows, f16 != 0, &m);
+    rep[idx] = r;
+    wint[idx] = m;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < S * LP * kOmgRows; e += blockDim.x) {
+    const int row = e / kOmgRows, il = e % kOmgRows;  // row = s * LP + l
+    w[(size_t)row * npad + i0 + il] = dg[e];
+  }
 }
 
 __global__ void k_units(const int* __restrict__ E, int LP, int S, int eoff, double* __restrict__ unit) {
@@ -686,8 +823,17 @@ __global__ void k_tc_g_finish(GFinishArgs a) {
     const int64_t pos = a.pos0 + j;
     const int64_t snp = a.perm ? (int64_t)a.perm[pos] : pos;
     const double f = a.F[snp], s = a.scale[snp];
-    double pd = 0.0;
-    for (int c = 0; c < a.nchunks; ++c) pd += (double)a.part[((size_t)c * a.nsnp + j) * LP + l];
+    // chunk partials summed as an FP32 pair (TwoSum, about 48 bits: far below
+    // the FP32 rounding of each partial) rather than on the FP64 pipe
+    float ph = 0.f, pl = 0.f;
+    for (int c = 0; c < a.nchunks; ++c) {
+      const float v = a.part[((size_t)c * a.nsnp + j) * LP + l];
+      const float t = __fadd_rn(ph, v);
+      const float bv = __fsub_rn(t, ph);
+      pl = __fadd_rn(pl, __fadd_rn(__fsub_rn(ph, __fsub_rn(t, bv)), __fsub_rn(v, bv)));
+      ph = t;
+    }
+    const double pd = (double)ph + (double)pl;
     double miss = 0.0;
     if (a.gisum) {
       miss = f * a.wunit_m[l] * (double)(long long)a.gisum[idx];
@@ -742,20 +888,6 @@ __global__ void k_tc_gh_slices(GFinishArgs a, const int* __restrict__ Eh) {
       a.cpart[(size_t)j * LP + l] = 0.0;
     }
   }
-}
-
-__global__ void k_colreduce(const double* __restrict__ part, int rows, int LP, double* __restrict__ out) {
-  const int l = blockIdx.x;
-  double acc = 0.0;
-  for (int r = threadIdx.x; r < rows; r += blockDim.x) acc += part[(size_t)r * LP + l];
-  __shared__ double red[256];
-  red[threadIdx.x] = acc;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) out[l] = red[0];
 }
 
 // H rows: FP64 sum of the split partials (the first carries the
@@ -814,32 +946,34 @@ void make_map_2d(CUtensorMap* map, const void* base, int dtype, uint64_t inner, 
   if (r != CUDA_SUCCESS) throw Error(-2, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-// Two CTAs per SM when the slice accumulators leave room for two 32-column
-// operand stages within half of the SM's 512 TMEM columns.  The tensor core
-// then runs one CTA's MMAs while the other decodes and stores its next
-// operand into TMEM; on the 7,812 x 100,000 genotype window this cut both
-// products by a third against one CTA per SM with eight stages.
-bool pair_per_sm(int LP, int nslice) { return nslice * LP + 2 * 32 <= 256; }
+// Genotype input (A in TMEM): two CTAs per SM when the slice accumulators
+// leave room for two 32-column operand stages within half of the SM's 512
+// TMEM columns.  The tensor core then runs one CTA's MMAs while the other
+// decodes and stores its next operand into TMEM; on the 7,812 x 100,000
+// genotype window this cut both products by a third against one CTA per SM
+// with eight stages.  Dense input (A in shared memory): one CTA per SM.
+bool pair_per_sm(int LP, int nslice, bool dense) { return !dense && nslice * LP + 2 * 32 <= 256; }
 
-int stages_for(int LP, int nslice, int pbytes) {
-  const SmemLayout l = layout_for(LP, nslice, pbytes);
-  const bool pair = pair_per_sm(LP, nslice);
+int stages_for(int LP, int nslice, int pbytes, bool dense) {
+  const SmemLayout l = layout_for(LP, nslice, pbytes, dense);
+  const bool pair = pair_per_sm(LP, nslice, dense);
   // dynamic shared memory (static use is under 12 KB); 228 KB per SM
   const int budget = (pair ? 104 : 212) * 1024;
   const int by_smem = budget / (int)l.stage_bytes;
-  // TMEM: slice accumulators + 32 columns of A operand per stage
-  const int by_tmem = ((pair ? 256 : 512) - nslice * LP) / 32;
+  // TMEM: slice accumulators + (A in TMEM) 32 columns of A operand per stage
+  const int by_tmem = dense ? kMaxStages : ((pair ? 256 : 512) - nslice * LP) / 32;
   return std::max(1, std::min(kMaxStages, std::min(by_smem, by_tmem)));
 }
 
-int tmem_cols_needed(int LP, int nslice, int nstages) { return nslice * LP + nstages * 32; }
+int tmem_cols_needed(int LP, int nslice, int nstages, bool dense) { return nslice * LP + (dense ? 0 : nstages * 32); }
 
-// A plan that takes more than half of the TMEM asks for more than half of the
-// shared memory too, so that a second CTA never shares its SM and waits in
-// tcgen05.alloc.
-size_t smem_bytes(int LP, int nslice, int pbytes, int nstages, int tmem_cols) {
-  const size_t b = (size_t)layout_for(LP, nslice, pbytes).stage_bytes * nstages + 1024;
-  return tmem_cols > 256 ? std::max(b, (size_t)120 * 1024) : b;
+// A plan that takes more than half of the TMEM, or that does not pair, asks
+// for more than half of the shared memory too, so that a second CTA never
+// shares its SM and waits in tcgen05.alloc.
+size_t smem_bytes(int LP, int nslice, int pbytes, int nstages, int tmem_cols, bool dense) {
+  const size_t b = (size_t)layout_for(LP, nslice, pbytes, dense).stage_bytes * nstages + 1024;
+  const bool pair = tmem_cols <= 256 && pair_per_sm(LP, nslice, dense);
+  return pair ? b : std::max(b, (size_t)120 * 1024);
 }
 
 int tmem_cols_for(int ncols) {
@@ -872,9 +1006,9 @@ void launch_h_t(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArg
 
 void launch_g(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs& a, cudaStream_t s) {
   if (a.nstages < 1 || a.nstages > kMaxStages || a.tmem_cols > 512 ||
-      a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.nstages))
+      a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.nstages, a.dense != 0))
     throw Error(-6, "tensor-core G product: pipeline plan exceeds TMEM or the stage limit");
-  const size_t smem = smem_bytes(a.LP, a.nslice, g_tile_bytes(a.dense != 0), a.nstages, a.tmem_cols);
+  const size_t smem = smem_bytes(a.LP, a.nslice, g_tile_bytes(a.dense != 0), a.nstages, a.tmem_cols, a.dense != 0);
   if (smem > 214 * 1024) throw Error(-6, "tensor-core G product: pipeline plan exceeds shared memory");
   if (a.dense)
     launch_g_t<true>(map_bed, map_w, a, smem, s);
@@ -885,9 +1019,9 @@ void launch_g(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs&
 
 void launch_h(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs& a, cudaStream_t s) {
   if (a.nstages < 1 || a.nstages > kMaxStages || a.tmem_cols > 512 ||
-      a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.nstages))
+      a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.nstages, a.dense != 0))
     throw Error(-6, "tensor-core H product: pipeline plan exceeds TMEM or the stage limit");
-  const size_t smem = smem_bytes(a.LP, a.nslice, h_tile_bytes(a.dense != 0), a.nstages, a.tmem_cols);
+  const size_t smem = smem_bytes(a.LP, a.nslice, h_tile_bytes(a.dense != 0), a.nstages, a.tmem_cols, a.dense != 0);
   if (smem > 214 * 1024) throw Error(-6, "tensor-core H product: pipeline plan exceeds shared memory");
   if (a.dense)
     launch_h_t<true>(map_bed, map_g, a, smem, s);
@@ -896,33 +1030,50 @@ void launch_h(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs&
   PCAONE_LAUNCH_CHECK();
 }
 
-void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv_bfloat16* w, double* wunit,
-                         double* colsum, int* E, double* rep, int32_t* wint, bool f16, cudaStream_t s) {
-  const int64_t n = (int64_t)npad * LP;
-  k_col_exponent<<<LP, 256, 0, s>>>(omg, N, LP, E);
-  PCAONE_LAUNCH_CHECK();
-  k_omega_slices<<<ceil_div(n, 256), 256, 0, s>>>(omg, npad, N, LP, S, E, reinterpret_cast<uint16_t*>(w), rep,
-                                                  wint, f16 ? 1 : 0);
-  PCAONE_LAUNCH_CHECK();
-  k_units<<<ceil_div(S * LP, 128), 128, 0, s>>>(E, LP, S, 0, wunit);
-  PCAONE_LAUNCH_CHECK();
-  k_colreduce<<<LP, 256, 0, s>>>(rep, N, LP, colsum);
+template <bool kMax>
+void launch_colred(const double* A, int64_t rows, int LP, const ColRedScratch& cr, double* sum_out, int* exp_out,
+                   cudaStream_t s) {
+  if (LP < 1 || LP > 256) throw Error(-6, "column reduction: row width out of range");
+  if (rows <= 0) {
+    // an empty column has sum 0 and exponent 0
+    if (kMax)
+      PCAONE_CUDA(cudaMemsetAsync(exp_out, 0, sizeof(int) * LP, s));
+    else
+      PCAONE_CUDA(cudaMemsetAsync(sum_out, 0, sizeof(double) * LP, s));
+    return;
+  }
+  const int64_t nb0 = std::min<int64_t>(kColRedBlocks, (rows + 31) / 32);
+  const int64_t per = (rows + nb0 - 1) / nb0;
+  const int nb = (int)((rows + per - 1) / per);
+  k_colred<kMax><<<nb, 256, 0, s>>>(A, rows, LP, per, cr.part, cr.cnt, sum_out, exp_out);
   PCAONE_LAUNCH_CHECK();
 }
 
-void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* gmunit, double* c_out, cudaStream_t s) {
+void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv_bfloat16* w, double* wunit,
+                         double* colsum, int* E, double* rep, int32_t* wint, bool f16, const ColRedScratch& cr,
+                         cudaStream_t s) {
+  launch_colred<true>(omg, N, LP, cr, nullptr, E, s);
+  if (npad % kOmgRows != 0 || S > 3 || LP > 112) throw Error(-6, "test-matrix slices: unsupported shape");
+  k_omega_slices<<<npad / kOmgRows, 256, 0, s>>>(omg, npad, N, LP, S, E, reinterpret_cast<uint16_t*>(w), rep, wint,
+                                                 f16 ? 1 : 0);
+  PCAONE_LAUNCH_CHECK();
+  k_units<<<ceil_div(S * LP, 128), 128, 0, s>>>(E, LP, S, 0, wunit);
+  PCAONE_LAUNCH_CHECK();
+  launch_colred<false>(rep, N, LP, cr, colsum, nullptr, s);
+}
+
+void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* gmunit, double* c_out,
+                     const ColRedScratch& cr, cudaStream_t s) {
   k_tc_g_finish<<<ceil_div((int64_t)a.nsnp * a.LP, 256), 256, 0, s>>>(a);
   PCAONE_LAUNCH_CHECK();
-  k_col_exponent<<<a.LP, 256, 0, s>>>(a.gh, a.nsnp, a.LP, Eh);
-  PCAONE_LAUNCH_CHECK();
+  launch_colred<true>(a.gh, a.nsnp, a.LP, cr, nullptr, Eh, s);
   k_tc_gh_slices<<<ceil_div((int64_t)a.ldg * a.LP, 256), 256, 0, s>>>(a, Eh);
   PCAONE_LAUNCH_CHECK();
   k_units<<<ceil_div(a.nslice * a.LP, 128), 128, 0, s>>>(Eh, a.LP, a.nslice, 0, hunit);
   PCAONE_LAUNCH_CHECK();
   k_units<<<ceil_div(a.nslice * a.LP, 128), 128, 0, s>>>(Eh, a.LP, a.nslice, 1, gmunit);
   PCAONE_LAUNCH_CHECK();
-  k_colreduce<<<a.LP, 256, 0, s>>>(a.cpart, a.nsnp, a.LP, c_out);
-  PCAONE_LAUNCH_CHECK();
+  launch_colred<false>(a.cpart, a.nsnp, a.LP, cr, c_out, nullptr, s);
 }
 
 void launch_h_finish(int nsamples, int npad, int L, int LP, const float* hpart, int nsplit, const double* c,

@@ -79,16 +79,25 @@ inline int g_tile_bytes(bool dense) { return dense ? 128 * 128 : 128 * 16; }
 inline int h_tile_bytes(bool dense) { return dense ? 64 * 256 : 64 * 32; }
 // pipeline stages within shared memory (B slices + packed tile per stage) and
 // TMEM (nslice * LP accumulator columns + 32 A columns per stage)
-int stages_for(int LP, int nslice, int pbytes);
+int stages_for(int LP, int nslice, int pbytes, bool dense);
 int tmem_cols_for(int ncols);
-int tmem_cols_needed(int LP, int nslice, int nstages);
+int tmem_cols_needed(int LP, int nslice, int nstages, bool dense);
 void launch_g(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs& a, cudaStream_t s);
 void launch_h(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs& a, cudaStream_t s);
+// scratch of the multi-block column reductions: kColRedBlocks x LP partials and
+// a completion counter that is zero between launches
+constexpr int kColRedBlocks = 304;
+struct ColRedScratch {
+  double* part;
+  unsigned* cnt;
+};
 void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv_bfloat16* w, double* wunit,
-                         double* colsum, int* E, double* rep, int32_t* wint, bool f16, cudaStream_t s);
+                         double* colsum, int* E, double* rep, int32_t* wint, bool f16, const ColRedScratch& cr,
+                         cudaStream_t s);
 // G finish, Gh slices and their units (hunit), Gm integers with their units
 // (gmunit: S x LP, the last slice row is the unit of gmint), c
-void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* gmunit, double* c_out, cudaStream_t s);
+void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* gmunit, double* c_out,
+                     const ColRedScratch& cr, cudaStream_t s);
 void launch_h_finish(int nsamples, int npad, int L, int LP, const float* hpart, int nsplit, const double* c,
                      double* Hx, cudaStream_t s);
 void launch_gather_rows(const uint8_t* src, uint8_t* dst, int64_t stride, const int32_t* perm, int64_t nrows,

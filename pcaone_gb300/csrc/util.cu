@@ -1,6 +1,8 @@
 // Small utility kernels: the missing-genotype lists (by position, and grouped
 // by window and sample), the missing-entry term of the H product, the sign
 // convention flip_UV, and the row-major -> column-major copy of outputs.
+#include <algorithm>
+
 #include "internal.cuh"
 
 namespace pcaone {
@@ -50,12 +52,17 @@ __global__ void k_missing_list(BedView v, const int32_t* __restrict__ perm, cons
 // position, the positions of window w at which sample i is missing (code 01).
 // One thread per 32-bit word of a row (16 samples), grid row = window; the
 // count pass writes cnt[w*N + i], the fill pass (after an exclusive scan of the
-// counts into ptr) writes the positions and samples.
+// counts into ptr) writes the positions and samples.  Each thread keeps its 16
+// counters or write offsets in its own column of shared memory, so a missing
+// entry costs one indexed update.
 template <bool kFill>
-__global__ void k_buckets(BedView v, const int32_t* __restrict__ perm, int64_t wsize, int32_t* __restrict__ cnt,
-                          const int64_t* __restrict__ ptr, int32_t* __restrict__ bpos,
-                          int32_t* __restrict__ bsample) {
-  const int wd = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(128) k_buckets(BedView v, const int32_t* __restrict__ perm, int64_t wsize,
+                                                 int32_t* __restrict__ cnt, const int64_t* __restrict__ ptr,
+                                                 int32_t* __restrict__ bpos, int32_t* __restrict__ bsample) {
+  __shared__ long long soff[kFill ? 16 : 1][128];
+  __shared__ int scnt[kFill ? 1 : 16][128];
+  const int tx = threadIdx.x;
+  const int wd = blockIdx.x * blockDim.x + tx;
   const int nwords = (v.nsamples + 15) >> 4;
   if (wd >= nwords) return;
   const int64_t win = blockIdx.y;
@@ -64,12 +71,12 @@ __global__ void k_buckets(BedView v, const int32_t* __restrict__ perm, int64_t w
   const int i0 = wd * 16;
   const int nloc = v.nsamples - i0 < 16 ? v.nsamples - i0 : 16;
   const uint32_t valid = nloc == 16 ? 0x55555555u : (((1u << (2 * nloc)) - 1u) & 0x55555555u);
-  int n[16];
-  int64_t off[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
-    n[q] = 0;
-    off[q] = (kFill && q < nloc) ? ptr[win * v.nsamples + i0 + q] : 0;
+    if (kFill)
+      soff[kFill ? q : 0][tx] = q < nloc ? ptr[win * v.nsamples + i0 + q] : 0;
+    else
+      scnt[kFill ? 0 : q][tx] = 0;
   }
 #pragma unroll 8
   for (int64_t p = p0; p < p1; ++p) {
@@ -79,25 +86,17 @@ __global__ void k_buckets(BedView v, const int32_t* __restrict__ perm, int64_t w
     while (miss) {
       const int q = (__ffs(miss) - 1) >> 1;
       if (kFill) {
-#pragma unroll
-        for (int t = 0; t < 16; ++t) {
-          if (t == q) {
-            bpos[off[t]] = (int32_t)p;
-            bsample[off[t]] = i0 + t;
-            ++off[t];
-          }
-        }
+        const long long e = soff[kFill ? q : 0][tx]++;
+        bpos[e] = (int32_t)p;
+        bsample[e] = i0 + q;
       } else {
-#pragma unroll
-        for (int t = 0; t < 16; ++t) n[t] += (t == q);
+        scnt[kFill ? 0 : q][tx] += 1;
       }
       miss &= miss - 1u;
     }
   }
   if (!kFill) {
-#pragma unroll
-    for (int q = 0; q < 16; ++q)
-      if (q < nloc) cnt[win * v.nsamples + i0 + q] = n[q];
+    for (int q = 0; q < nloc; ++q) cnt[win * v.nsamples + i0 + q] = scnt[kFill ? 0 : q][tx];
   }
 }
 
@@ -159,74 +158,92 @@ __global__ void k_h_buckets(int64_t win, int N, int L, int LP, const int64_t* __
   }
 }
 
-// One warp per chunk of 64 consecutive entries: the lanes fetch 32 entries'
-// keys, source rows and quantised values at once, load the broadcast source
-// rows 16 at a time (all loads independent), and sum them per key while the
-// key is unchanged; a key change (warp-uniform) flushes the running sums with
-// int64 atomics.
-template <int NQ, bool VALS>
-__global__ void k_seg_gather(SegGatherArgs a) {
-  constexpr int SB = VALS ? 8 : 16;  // entries whose rows are loaded together
-  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Lane groups: gsize = max(8, ceil(L/4)) lanes share one entry, lane c of a
+// group loading columns 4c .. 4c+3 of the entry's source row with one 16-byte
+// load, so a warp gathers 32/gsize rows per load instruction (three rows of
+// 40 columns).  Each group sums a run of kSegRun consecutive entries: lanes
+// c < 8 fetch the keys, source offsets and quantised values of 8 entries at
+// once (4 with EM values, to keep registers for two loads per entry), the
+// group loads their rows (all loads independent), then adds them
+// in entry order while the key is unchanged; a key change (group-uniform)
+// flushes the running sums into the int64 output with atomics.  The row sums
+// are int32: |R| <= 2^23, so a run of 64 entries stays below 2^29.
+constexpr int kSegRun = 64;
+constexpr int kSegFetch = 8;  // lanes per group that fetch entry indices (the minimum group size)
+
+template <bool VALS>
+__global__ void __launch_bounds__(256) k_seg_gather(SegGatherArgs a, int gsize, int ngroups) {
+  constexpr int kSegBatch = VALS ? 4 : 8;
   const int lane = threadIdx.x & 31;
-  const int64_t cb = a.e0 + w * 64;
-  if (cb >= a.e1) return;
-  const int64_t ce = cb + 64 < a.e1 ? cb + 64 : a.e1;
-  const int LP = a.LP, L = a.L;
-  long long acc[NQ], acc2[NQ];
-#pragma unroll
-  for (int q = 0; q < NQ; ++q) acc[q] = acc2[q] = 0;
+  const int grp = lane / gsize;
+  const bool active = grp < ngroups;
+  const int gbase = active ? grp * gsize : 0;
+  const int c = active ? lane - gbase : gsize;  // idle lanes fetch and sum nothing
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t wb = a.e0 + w * ngroups * kSegRun;
+  if (wb >= a.e1) return;  // warp-uniform
+  const int64_t rb = wb + (int64_t)(active ? grp : 0) * kSegRun;
+  const int64_t re = active ? (rb + kSegRun < a.e1 ? rb + kSegRun : a.e1) : rb;
+  const int col = 4 * c;
+  const bool cols = col < a.L;
+  int acc[4] = {0, 0, 0, 0};
+  long long acc2[4] = {0, 0, 0, 0};
   int cur = -1;
   auto flush = [&]() {
-    if (cur < 0) return;
+    if (cur >= 0 && cols) {
+      unsigned long long* o = a.out + (size_t)cur * a.LP + col;
+      unsigned long long* o2 = VALS ? a.out2 + (size_t)cur * a.LP + col : nullptr;
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      const int l = lane + 32 * q;
-      if (l < L) {
-        atomicAdd(a.out + (size_t)cur * LP + l, (unsigned long long)acc[q]);
-        if (VALS) atomicAdd(a.out2 + (size_t)cur * LP + l, (unsigned long long)acc2[q]);
-      }
-      acc[q] = acc2[q] = 0;
-    }
-  };
-  for (int64_t eb = cb; eb < ce; eb += 32) {
-    const int ne = (int)(ce - eb < 32 ? ce - eb : 32);
-    int krow = -1, soff = 0, vi = 0;
-    if (lane < ne) {
-      krow = (int)(a.key[eb + lane] - a.key_base);
-      soff = (int)(a.src[eb + lane] - a.src_base) * LP;
-      if (VALS) vi = __double2int_rn(a.val[eb + lane] * kSegValueScale);
-    }
-#pragma unroll 1
-    for (int h = 0; h < ne; h += SB) {
-      int m[SB][NQ], m2[VALS ? SB : 1][NQ];
-#pragma unroll
-      for (int u = 0; u < SB; ++u) {
-        const int t = h + u;
-        const int so = __shfl_sync(0xffffffffu, soff, t);
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-          const int l = lane + 32 * q;
-          const bool ok = t < ne && l < L;
-          m[u][q] = ok ? a.R[so + l] : 0;
-          if (VALS) m2[VALS ? u : 0][q] = ok ? a.R2[so + l] : 0;
+      for (int t = 0; t < 4; ++t) {
+        if (col + t < a.L) {
+          atomicAdd(o + t, (unsigned long long)(long long)acc[t]);
+          if (VALS) atomicAdd(o2 + t, (unsigned long long)acc2[t]);
         }
       }
+    }
 #pragma unroll
-      for (int u = 0; u < SB; ++u) {
-        const int t = h + u;
-        const int kr = __shfl_sync(0xffffffffu, krow, t);
-        const int vt = VALS ? __shfl_sync(0xffffffffu, vi, t) : 0;
-        if (t < ne) {
-          if (kr != cur) {
-            flush();
-            cur = kr;
-          }
+    for (int t = 0; t < 4; ++t) {
+      acc[t] = 0;
+      acc2[t] = 0;
+    }
+  };
+  for (int b = 0; b < kSegRun; b += kSegBatch) {
+    const int64_t ef = rb + b + c;
+    int krow = -1, soff = 0, vi = 0;
+    if (c < kSegBatch && ef < re) {
+      krow = (int)(a.key[ef] - a.key_base);
+      soff = (int)(a.src[ef] - a.src_base) * a.LP;
+      if (VALS) vi = __double2int_rn(a.val[ef] * kSegValueScale);
+    }
+    int kr[kSegBatch], vt[kSegBatch];
+    int4 r[kSegBatch], r2[VALS ? kSegBatch : 1];
 #pragma unroll
-          for (int q = 0; q < NQ; ++q) {
-            acc[q] += m[u][q];
-            if (VALS) acc2[q] += ((long long)vt * (long long)m2[VALS ? u : 0][q]) >> kSegValueShift;
-          }
+    for (int u = 0; u < kSegBatch; ++u) {
+      const int so = __shfl_sync(0xffffffffu, soff, gbase + u);
+      kr[u] = __shfl_sync(0xffffffffu, krow, gbase + u);
+      vt[u] = VALS ? __shfl_sync(0xffffffffu, vi, gbase + u) : 0;
+      const bool ok = kr[u] >= 0 && cols;
+      r[u] = ok ? __ldg(reinterpret_cast<const int4*>(a.R + so + col)) : make_int4(0, 0, 0, 0);
+      if (VALS) r2[VALS ? u : 0] = ok ? __ldg(reinterpret_cast<const int4*>(a.R2 + so + col)) : make_int4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int u = 0; u < kSegBatch; ++u) {
+      if (kr[u] >= 0) {
+        if (kr[u] != cur) {
+          flush();
+          cur = kr[u];
+        }
+        acc[0] += r[u].x;
+        acc[1] += r[u].y;
+        acc[2] += r[u].z;
+        acc[3] += r[u].w;
+        if (VALS) {
+          const int4 q = r2[VALS ? u : 0];
+          const long long v = vt[u];
+          acc2[0] += (v * (long long)q.x) >> kSegValueShift;
+          acc2[1] += (v * (long long)q.y) >> kSegValueShift;
+          acc2[2] += (v * (long long)q.z) >> kSegValueShift;
+          acc2[3] += (v * (long long)q.w) >> kSegValueShift;
         }
       }
     }
@@ -321,24 +338,18 @@ void launch_h_buckets(int64_t win, int N, int L, int LP, const int64_t* ptr, con
   PCAONE_LAUNCH_CHECK();
 }
 
-template <bool VALS>
-void launch_seg_gather_v(const SegGatherArgs& a, unsigned nb, cudaStream_t s) {
-  switch ((a.L + 31) / 32) {
-    case 1: k_seg_gather<1, VALS><<<nb, 256, 0, s>>>(a); break;
-    case 2: k_seg_gather<2, VALS><<<nb, 256, 0, s>>>(a); break;
-    case 3: k_seg_gather<3, VALS><<<nb, 256, 0, s>>>(a); break;
-    default: k_seg_gather<4, VALS><<<nb, 256, 0, s>>>(a); break;
-  }
-}
-
 void launch_seg_gather(const SegGatherArgs& a, cudaStream_t s) {
   if (a.e1 <= a.e0) return;
-  const int64_t warps = (a.e1 - a.e0 + 63) / 64;
+  if (a.LP % 4 != 0 || a.L > a.LP || a.L > 128)
+    throw Error(-6, "missing-entry gather: row width must be a multiple of 4 and at most 128");
+  const int gsize = std::max(kSegFetch, (a.L + 3) / 4);
+  const int ngroups = 32 / gsize;
+  const int64_t warps = (a.e1 - a.e0 + (int64_t)ngroups * kSegRun - 1) / ((int64_t)ngroups * kSegRun);
   const unsigned nb = ceil_div(warps * 32, 256);
   if (a.val)
-    launch_seg_gather_v<true>(a, nb, s);
+    k_seg_gather<true><<<nb, 256, 0, s>>>(a, gsize, ngroups);
   else
-    launch_seg_gather_v<false>(a, nb, s);
+    k_seg_gather<false><<<nb, 256, 0, s>>>(a, gsize, ngroups);
   PCAONE_LAUNCH_CHECK();
 }
 
