@@ -359,6 +359,7 @@ def run_ours(args):
         barrier(ws)
     launches = ctx.launch_count() - launches0
     kstats = ctx.kernel_stats()
+    host_phases = ctx.timings()  # host-clock phases of the last timed run_halko call
     ctx.set_profiling(False)
     t_dev = reduce_max(sum(times) / len(times), ws)
 
@@ -423,6 +424,7 @@ def run_ours(args):
             "roofline": roof,
             "cpu_baseline": cpu,
             "kernels": kstats,
+            "host_s": host_phases,
             "pcs": {"S_top": [float(x) for x in S[:5]]},
         }
         if wl.get("emu"):

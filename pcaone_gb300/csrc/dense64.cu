@@ -263,6 +263,60 @@ __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows
   }
 }
 
+// C = A * B in place (C == A, n == ldb == LP) for B upper triangular
+// (B[t][c] = 0 for t > c: the R^{-1} factors of CholeskyQR), so column c needs
+// only t <= c.  Lane = row of a 32-row tile; warp w takes the columns c whose
+// position r = c % 16 in its 16-column block is w or 15 - w, which gives
+// every warp the same number of products and warp-uniform loop bounds.  Each
+// output accumulates the same FP32-pair terms in the same order as
+// k_gemm_tall: the skipped terms are exact zeros there.
+constexpr int kUpperMaxQ = 14;  // columns per warp: LP / 8 with LP <= 112
+__global__ void __launch_bounds__(256) k_gemm_tall_upper(double* A, int64_t rows, int LP,
+                                                         const double* __restrict__ B) {
+  extern __shared__ float smf[];
+  const int las = LP + 1;  // odd row stride of the A tile: lanes hit distinct banks
+  float* Bh = smf;         // LP x LP
+  float* Bl = Bh + LP * LP;
+  float* Ah = Bl + LP * LP;  // 32 x las
+  float* Al = Ah + kRowsTile * las;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int e = tid; e < LP * LP; e += blockDim.x) fp_split(B[e], Bh[e], Bl[e]);
+  int cmax = -1;
+#pragma unroll
+  for (int q = 0; q < kUpperMaxQ; ++q) {
+    const int c = 16 * (q >> 1) + ((q & 1) ? 15 - warp : warp);
+    if (c < LP) cmax = max(cmax, c);
+  }
+  for (int64_t rt = (int64_t)blockIdx.x * kRowsTile; rt < rows; rt += (int64_t)gridDim.x * kRowsTile) {
+    __syncthreads();
+    for (int e = tid; e < kRowsTile * LP; e += blockDim.x) {
+      const int rr = e / LP, cc = e % LP;
+      const int64_t row = rt + rr;
+      fp_split(row < rows ? A[row * LP + cc] : 0.0, Ah[rr * las + cc], Al[rr * las + cc]);
+    }
+    __syncthreads();
+    FloatPair s[kUpperMaxQ];
+    const float* ah = Ah + lane * las;
+    const float* al = Al + lane * las;
+    for (int t = 0; t <= cmax; ++t) {
+      const float xh = ah[t], xl = al[t];
+#pragma unroll
+      for (int q = 0; q < kUpperMaxQ; ++q) {
+        const int c = 16 * (q >> 1) + ((q & 1) ? 15 - warp : warp);
+        if (c < LP && t <= c) fp_add_prod2(s[q], xh, xl, Bh[t * LP + c], Bl[t * LP + c]);
+      }
+    }
+    const int64_t row = rt + lane;
+    if (row < rows) {
+#pragma unroll
+      for (int q = 0; q < kUpperMaxQ; ++q) {
+        const int c = 16 * (q >> 1) + ((q & 1) ? 15 - warp : warp);
+        if (c < LP) A[row * LP + c] = fp_value(s[q]);
+      }
+    }
+  }
+}
+
 // Signs d_i an Eigen/LAPACK Householder QR gives its Q relative to the
 // positive-diagonal factor: the modified LU of the top L x L block of the
 // orthonormal Q (Ballard et al., "Reconstructing Householder vectors from
@@ -709,6 +763,20 @@ void launch_gemm_tall(const double* A, int64_t rows, int LP, const double* B, in
   const size_t smem = 2 * sizeof(float) * ((size_t)LP * npd + (size_t)kRowsTile * (LP + 1));
   const int grid = (int)std::min<int64_t>((rows + kRowsTile - 1) / kRowsTile, 152 * 8);
   k_gemm_tall<<<grid, 256, smem, s>>>(A, rows, LP, B, ldb, n, C, ldc);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_gemm_tall_upper(double* A, int64_t rows, int LP, const double* B, cudaStream_t s) {
+  if (rows == 0) return;
+  if (LP % 8 != 0 || LP > 8 * kUpperMaxQ) throw Error(-6, "triangular tall product: width must be a multiple of 8, at most 112");
+  static bool attr_set = false;
+  if (!attr_set) {
+    PCAONE_CUDA(cudaFuncSetAttribute(k_gemm_tall_upper, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set = true;
+  }
+  const size_t smem = 2 * sizeof(float) * ((size_t)LP * LP + (size_t)kRowsTile * (LP + 1));
+  const int grid = (int)std::min<int64_t>((rows + kRowsTile - 1) / kRowsTile, 152 * 8);
+  k_gemm_tall_upper<<<grid, 256, smem, s>>>(A, rows, LP, B);
   PCAONE_LAUNCH_CHECK();
 }
 

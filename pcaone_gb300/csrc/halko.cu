@@ -559,11 +559,11 @@ static void cholqr(Context& c, double* A, int64_t rows, bool need_r) {
     if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: Gram matrix not positive definite");
     shifted = true;
   }
-  launch_gemm_tall(A, rows, LP, c.R1i.p, LP, LP, A, LP, c.stream);
+  launch_gemm_tall_upper(A, rows, LP, c.R1i.p, c.stream);
   launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream);
   launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R2.p, c.R2i.p, c.status.p, c.stream);
   if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: second Gram not positive definite");
-  launch_gemm_tall(A, rows, LP, c.R2i.p, LP, LP, A, LP, c.stream);
+  launch_gemm_tall_upper(A, rows, LP, c.R2i.p, c.stream);
   if (need_r) {
     launch_mult_small(c.R2.p, c.R1.p, c.Rt.p, LP, c.stream);     // R = R2 R1
     launch_mult_small(c.R1i.p, c.R2i.p, c.Rti.p, LP, c.stream);  // R^-1 = R1^-1 R2^-1
@@ -572,7 +572,7 @@ static void cholqr(Context& c, double* A, int64_t rows, bool need_r) {
     launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream);
     launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R3.p, c.R3i.p, c.status.p, c.stream);
     if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: third Gram not positive definite");
-    launch_gemm_tall(A, rows, LP, c.R3i.p, LP, LP, A, LP, c.stream);
+    launch_gemm_tall_upper(A, rows, LP, c.R3i.p, c.stream);
     if (need_r) {
       launch_mult_small(c.R3.p, c.Rt.p, c.R1.p, LP, c.stream);
       launch_mult_small(c.Rti.p, c.R3i.p, c.R1i.p, LP, c.stream);

@@ -173,6 +173,8 @@ void launch_chol_inv_shift(const double* W, int L, int LP, double shift, double*
 // C (rows x n, ld ldc) = A (rows x LP) * B (LP x n, ld ldb); C may alias A
 void launch_gemm_tall(const double* A, int64_t rows, int LP, const double* B, int ldb, int n, double* C, int ldc,
                       cudaStream_t s);
+// A <- A * B in place for B upper triangular (LP x LP, LP a multiple of 8)
+void launch_gemm_tall_upper(double* A, int64_t rows, int LP, const double* B, cudaStream_t s);
 // Q columns times the signs an Eigen / LAPACK Householder QR gives
 void launch_house_signs(double* Q, int64_t rows, int L, int LP, double* sgn, cudaStream_t s);
 int flip_blocks(int64_t rows);

@@ -242,6 +242,48 @@ __device__ __forceinline__ uint32_t dosage_pair(uint32_t x) {
 }
 
 
+// Decode table: the two BF16 dosages of a 4-bit pair of codes (two samples or
+// two SNPs; the first code in bits 0-1 gives the low half-word), from
+// dosage_pair.  32 copies, entry n of copy c at word n * 32 + c, so that lane c
+// always reads bank c: a lookup is conflict-free whatever the codes.  It
+// replaces the SWAR arithmetic (about eleven integer operations per word,
+// which kept the ALU pipe at two thirds of its peak) by two and a load.
+constexpr int kLutWords = 16 * 32;
+__device__ __forceinline__ void lut_init(uint32_t* lut, int tid, int nthreads) {
+  for (int i = tid; i < kLutWords; i += nthreads) {
+    const uint32_t n = (uint32_t)i >> 5;
+    lut[i] = dosage_pair((n & 3u) | (((n >> 2) & 3u) << 16));
+  }
+}
+
+// One stage of a warp transpose of a 32 x 32 matrix of 2-bit codes held as
+// 64 bits per lane (lo: positions 0-15, hi: 16-31): lanes exchange lane bit K
+// with position bit K (Hacker's Delight 7-3, across lanes with shuffles).
+// Stage 4 swaps whole words; stages 3..0 move the masked halves of each word.
+template <int K>
+__device__ __forceinline__ void xpose2_stage(uint32_t& lo, uint32_t& hi, int lane) {
+  constexpr uint32_t m = K == 3 ? 0x0000FFFFu : K == 2 ? 0x00FF00FFu : K == 1 ? 0x0F0F0F0Fu : 0x33333333u;
+  constexpr int sh = 2 << K;  // bits per block of 2^K positions
+  const bool up = (lane >> K) & 1;
+  const uint32_t sm = up ? m : ~m;
+  const uint32_t rl = __shfl_xor_sync(0xffffffffu, lo & sm, 1 << K);
+  const uint32_t rh = __shfl_xor_sync(0xffffffffu, hi & sm, 1 << K);
+  lo = up ? ((lo & ~m) | (rl >> sh)) : ((lo & m) | (rl << sh));
+  hi = up ? ((hi & ~m) | (rh >> sh)) : ((hi & m) | (rh << sh));
+}
+__device__ __forceinline__ void xpose2_warp(uint32_t& lo, uint32_t& hi, int lane) {
+  const bool up = (lane >> 4) & 1;
+  const uint32_t r = __shfl_xor_sync(0xffffffffu, up ? lo : hi, 16);
+  if (up)
+    lo = r;
+  else
+    hi = r;
+  xpose2_stage<3>(lo, hi, lane);
+  xpose2_stage<2>(lo, hi, lane);
+  xpose2_stage<1>(lo, hi, lane);
+  xpose2_stage<0>(lo, hi, lane);
+}
+
 struct SmemLayout {
   uint32_t b, a, p, stage_bytes;
 };
@@ -336,10 +378,12 @@ __global__ void __launch_bounds__(kThreads, 2)
   __shared__ uint32_t tmem_sh;
   __shared__ volatile int abort_sh;
   __shared__ float unit[3 * 112];
+  __shared__ uint32_t lut[kDense ? 1 : kLutWords];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int LP = a.LP, S = a.nslice;
   const SmemLayout lay = layout_for(LP, S, kTileBytes, kASmem);
-  const int row0 = blockIdx.x * 128;                  // window-local first SNP of the tile
+  const int row0 = blockIdx.x * 128;
+  if (!kDense) lut_init(lut, tid, kThreads);                  // window-local first SNP of the tile
   const int kbeg = blockIdx.y * a.chunk;
   const int kend = min(kbeg + a.chunk, a.npad);
   const int nk = (kend - kbeg + kStepK - 1) / kStepK;
@@ -442,11 +486,12 @@ __global__ void __launch_bounds__(kThreads, 2)
         }
       } else {
         const uint2 pk = *reinterpret_cast<const uint2*>(base + lay.p + r * 16 + ch * 8);
+        const uint32_t* lut_l = lut + lane;
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
           const uint32_t w32 = e < 8 ? pk.x : pk.y;
           const int sh = 4 * (e & 7);
-          wd[e] = dosage_pair(((w32 >> sh) & 3u) | (((w32 >> (sh + 2)) & 3u) << 16));
+          wd[e] = lut_l[((w32 >> sh) & 15u) << 5];
         }
       }
       if constexpr (kASmem) {
@@ -508,7 +553,9 @@ __global__ void __launch_bounds__(kThreads, 2)
   __shared__ volatile int abort_sh;
   __shared__ float unit[3 * 112];
   __shared__ float munit[2 * 112];  // units of the missing-entry sums (Gm integers, EM products)
+  __shared__ uint32_t lut[kDense ? 1 : kLutWords];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (!kDense) lut_init(lut, tid, kThreads);
   const int LP = a.LP, S = a.nslice;
   const SmemLayout lay = layout_for(LP, S, kTileBytes, kASmem);
   const int samp0 = blockIdx.x * 128;
@@ -595,11 +642,11 @@ __global__ void __launch_bounds__(kThreads, 2)
     // dense input, 32 FP16 values into the stage's A tile) ----
     const int q4 = warp & 3, ch = (warp - kDecodeWarp0) >> 2;
     const int r = q4 * 32 + lane;
-    const int sh = 2 * (r & 3);
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
     for (int kb = 0; kb < nk; ++kb) {
       const int st = kb % nst;
-      if (!role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
+      // warp-uniform outcome: the genotype decode below shuffles across the warp
+      if (!__all_sync(0xffffffffu, role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh))) break;
       uint8_t* base = smem + st * lay.stage_bytes;
       uint32_t wd[16];
       if (kDense) {
@@ -612,11 +659,17 @@ __global__ void __launch_bounds__(kThreads, 2)
           wd[e] = v0 | (v1 << 16);
         }
       } else {
-        const uint8_t* pt = smem + st * lay.stage_bytes + lay.p + (ch * 32) * 32 + (r >> 2);
+        // lane l loads SNP row 32ch + l of the warp's 32 samples (8 bytes); the
+        // warp transpose leaves lane r with sample r's codes of those 32 rows,
+        // row j in bits 2j .. 2j+1 (lo: rows 0-15, hi: rows 16-31)
+        const uint2 rowv = *reinterpret_cast<const uint2*>(base + lay.p + (ch * 32 + lane) * 32 + q4 * 8);
+        uint32_t lo = rowv.x, hi = rowv.y;
+        xpose2_warp(lo, hi, lane);
+        const uint32_t* lut_l = lut + lane;
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
-          const uint32_t b0 = pt[(2 * e) * 32], b1 = pt[(2 * e + 1) * 32];
-          wd[e] = dosage_pair(((b0 >> sh) & 3u) | (((b1 >> sh) & 3u) << 16));
+          const uint32_t w32 = e < 8 ? lo : hi;
+          wd[e] = lut_l[((w32 >> (4 * (e & 7))) & 15u) << 5];
         }
       }
       if constexpr (kASmem) {
