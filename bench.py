@@ -122,9 +122,11 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-# DRAM bytes per launch of the tensor-core window products on the c2 window
-# shape (ncu, workload c2p; profiles/k_tc_window_c2p.md)
-NCU_TRAFFIC_C2_WINDOW = {"g": 255.3e6, "h": 227.2e6}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# tensor-core window products on the c2 window shape (ncu capture B of
+# profiles/k_tc_window_c2p.md, workload c2p); the H launch includes reading and
+# clearing the int64 missing-entry sums
+NCU_TRAFFIC_C2_WINDOW = {"g": 253.4e6, "h": 296.9e6}
 
 
 def workload_params(name: str, precision: str):
