@@ -94,8 +94,9 @@ struct Context {
   int bk_nwin = 0;
   bool bk_valid = false;
   DBuf<int64_t> bk_ptr;
-  std::vector<int64_t> bk_ptr_host;
+  std::vector<int64_t> bk_ptr_host;  // offsets at the window boundaries: bucket w*N for w = 0..nwin
   DBuf<int32_t> bk_cnt, bk_pos, bk_sample;
+  DBuf<long long> bk_scan;  // tile sums of the offsets' prefix sum
   DBuf<double> bk_value;
   bool bk_stale = true;  // bk_value does not yet hold the current fill values
 
@@ -657,17 +658,18 @@ static void ensure_buckets(Context& c) {
   const int32_t* perm = c.permuted ? c.perm.p : nullptr;
   c.bk_cnt.ensure(nb, c.stream, false);
   launch_bucket_count(c.view(), perm, ws, (int)nwin, c.bk_cnt.p, c.stream);
-  std::vector<int32_t> cnt(nb);
-  PCAONE_CUDA(cudaMemcpyAsync(cnt.data(), c.bk_cnt.p, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
+  // offsets by a prefix sum on the device; the host keeps those at the window
+  // boundaries (bucket w*N), one strided copy
+  c.bk_ptr.ensure(nb + 1, c.stream, false);
+  c.bk_scan.ensure((size_t)std::max<int64_t>(1, scan_tiles_needed((int64_t)nb)), c.stream, false);
+  launch_exclusive_scan(c.bk_cnt.p, (int64_t)nb, c.bk_ptr.p, c.bk_scan.p, c.stream);
+  std::vector<int64_t> ptr((size_t)nwin + 1);
+  PCAONE_CUDA(cudaMemcpy2DAsync(ptr.data(), sizeof(int64_t), c.bk_ptr.p, (size_t)c.N * sizeof(int64_t),
+                                sizeof(int64_t), (size_t)nwin + 1, cudaMemcpyDeviceToHost, c.stream));
   PCAONE_CUDA(cudaStreamSynchronize(c.stream));
-  std::vector<int64_t> ptr(nb + 1);
-  ptr[0] = 0;
-  for (size_t b = 0; b < nb; ++b) ptr[b + 1] = ptr[b] + cnt[b];
-  const int64_t total = ptr[nb];
+  const int64_t total = ptr[(size_t)nwin];
   if (total != (int64_t)c.counts_total_missing)
     throw Error(PCAONE_E_CUDA, "internal: missing-entry index disagrees with the genotype counts");
-  c.bk_ptr.ensure(nb + 1, c.stream, false);
-  PCAONE_CUDA(cudaMemcpyAsync(c.bk_ptr.p, ptr.data(), (nb + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, c.stream));
   c.bk_pos.ensure((size_t)std::max<int64_t>(1, total), c.stream, false);
   c.bk_sample.ensure((size_t)std::max<int64_t>(1, total), c.stream, false);
   launch_bucket_fill(c.view(), perm, ws, (int)nwin, c.bk_ptr.p, c.bk_pos.p, c.bk_sample.p, c.stream);
@@ -851,8 +853,8 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   if (any_miss) {
     // sum_j Gm_j (and sum_j 2 e_j Gh_j) over each sample's missing SNPs of the window
     SegGatherArgs sg{};
-    sg.e0 = c.bk_ptr_host[(size_t)win * c.N];
-    sg.e1 = c.bk_ptr_host[(size_t)(win + 1) * c.N];
+    sg.e0 = c.bk_ptr_host[(size_t)win];
+    sg.e1 = c.bk_ptr_host[(size_t)win + 1];
     sg.key = c.bk_sample.p;
     sg.key_base = 0;
     sg.src = c.bk_pos.p;

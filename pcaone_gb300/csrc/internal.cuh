@@ -200,6 +200,10 @@ void launch_missing_list(const BedView& v, const int32_t* perm, const int64_t* r
 // positions / samples at the exclusive-scan offsets ptr (nwin * N + 1)
 void launch_bucket_count(const BedView& v, const int32_t* perm, int64_t wsize, int nwin, int32_t* cnt,
                          cudaStream_t s);
+// exclusive prefix sum of n int32 counts: out[0..n], out[n] = total;
+// tile_sums holds scan_tiles_needed(n) values of scratch
+void launch_exclusive_scan(const int32_t* in, int64_t n, int64_t* out, long long* tile_sums, cudaStream_t s);
+int64_t scan_tiles_needed(int64_t n);
 void launch_bucket_fill(const BedView& v, const int32_t* perm, int64_t wsize, int nwin, const int64_t* ptr,
                         int32_t* bpos, int32_t* bsample, cudaStream_t s);
 // Hx[i] += the FP32-form EM term of window win: sum over the sample's missing

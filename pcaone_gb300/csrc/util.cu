@@ -100,6 +100,94 @@ __global__ void __launch_bounds__(128) k_buckets(BedView v, const int32_t* __res
   }
 }
 
+// Exclusive prefix sum of n int32 counts into int64 offsets, out[0..n] with
+// out[n] the total, in three passes over tiles of kScanTile counts: tile sums,
+// an exclusive scan of the tile sums (one block, which also writes out[n]),
+// then each tile's own scan from its offset.  Integer sums, so the result does
+// not depend on the order of the passes' additions.
+constexpr int kScanThreads = 512;
+constexpr int kScanPerThread = 8;
+constexpr int kScanTile = kScanThreads * kScanPerThread;
+
+// exclusive scan of one value per thread over the block (blockDim.x = kScanThreads);
+// *total receives the block's sum
+__device__ __forceinline__ long long block_exclusive_scan(long long v, long long* total) {
+  __shared__ long long wsum[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  long long incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    long long w = lane < kScanThreads / 32 ? wsum[lane] : 0;
+    long long wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long t = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    if (lane < kScanThreads / 32) wsum[lane] = wi - w;  // exclusive warp offsets
+    if (lane == kScanThreads / 32 - 1) *total = wi;
+  }
+  __syncthreads();
+  const long long r = wsum[warp] + incl - v;
+  __syncthreads();  // wsum is reused by the next call
+  return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(const int32_t* __restrict__ in, int64_t n,
+                                                                 long long* __restrict__ tsum) {
+  __shared__ long long tot;
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPerThread;
+  long long v = 0;
+#pragma unroll
+  for (int q = 0; q < kScanPerThread; ++q)
+    if (base + q < n) v += in[base + q];
+  block_exclusive_scan(v, &tot);
+  if (threadIdx.x == 0) tsum[blockIdx.x] = tot;
+}
+
+// one block: tsum[0..ntiles) becomes exclusive; out_total = the sum of all
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(long long* __restrict__ tsum, int ntiles,
+                                                             int64_t* __restrict__ out_total) {
+  __shared__ long long tot;
+  long long carry = 0;
+  for (int c0 = 0; c0 < ntiles; c0 += kScanThreads) {
+    const int i = c0 + threadIdx.x;
+    const long long v = i < ntiles ? tsum[i] : 0;
+    const long long ex = block_exclusive_scan(v, &tot);
+    __syncthreads();
+    if (i < ntiles) tsum[i] = carry + ex;
+    carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out_total = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int32_t* __restrict__ in, int64_t n,
+                                                             const long long* __restrict__ tsum,
+                                                             int64_t* __restrict__ out) {
+  __shared__ long long tot;
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPerThread;
+  int32_t c[kScanPerThread];
+  long long v = 0;
+#pragma unroll
+  for (int q = 0; q < kScanPerThread; ++q) {
+    c[q] = base + q < n ? in[base + q] : 0;
+    v += c[q];
+  }
+  long long run = tsum[blockIdx.x] + block_exclusive_scan(v, &tot);
+#pragma unroll
+  for (int q = 0; q < kScanPerThread; ++q) {
+    if (base + q < n) out[base + q] = run;
+    run += c[q];
+  }
+}
+
 // The EM term of H in the FP32 form for window `win` (positions
 // [pos0, pos0+nsnp)): for each sample i, over the entries e of bucket (win, i)
 // at positions p, Hx[i] += sum_e s_p v_e G32[p - pos0], with v_e the EM fill
@@ -186,6 +274,7 @@ __global__ void __launch_bounds__(256) k_seg_gather(SegGatherArgs a, int gsize, 
   const int64_t re = active ? (rb + kSegRun < a.e1 ? rb + kSegRun : a.e1) : rb;
   const int col = 4 * c;
   const bool cols = col < a.L;
+  const bool same = a.R2 == a.R;  // G side: the value products use the same integer rows
   int acc[4] = {0, 0, 0, 0};
   long long acc2[4] = {0, 0, 0, 0};
   int cur = -1;
@@ -224,7 +313,8 @@ __global__ void __launch_bounds__(256) k_seg_gather(SegGatherArgs a, int gsize, 
       vt[u] = VALS ? __shfl_sync(0xffffffffu, vi, gbase + u) : 0;
       const bool ok = kr[u] >= 0 && cols;
       r[u] = ok ? __ldg(reinterpret_cast<const int4*>(a.R + so + col)) : make_int4(0, 0, 0, 0);
-      if (VALS) r2[VALS ? u : 0] = ok ? __ldg(reinterpret_cast<const int4*>(a.R2 + so + col)) : make_int4(0, 0, 0, 0);
+      if (VALS)
+        r2[VALS ? u : 0] = same ? r[u] : (ok ? __ldg(reinterpret_cast<const int4*>(a.R2 + so + col)) : make_int4(0, 0, 0, 0));
     }
 #pragma unroll
     for (int u = 0; u < kSegBatch; ++u) {
@@ -321,6 +411,23 @@ void launch_bucket_fill(const BedView& v, const int32_t* perm, int64_t wsize, in
   k_buckets<true><<<grid, 128, 0, s>>>(v, perm, wsize, nullptr, ptr, bpos, bsample);
   PCAONE_LAUNCH_CHECK();
 }
+
+void launch_exclusive_scan(const int32_t* in, int64_t n, int64_t* out, long long* tile_sums, cudaStream_t s) {
+  if (n <= 0) {
+    PCAONE_CUDA(cudaMemsetAsync(out, 0, sizeof(int64_t), s));
+    return;
+  }
+  const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+  if (ntiles > 0x7fffffff) throw Error(-6, "prefix sum: too many counts");
+  k_scan_tile_sums<<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, tile_sums);
+  PCAONE_LAUNCH_CHECK();
+  k_scan_tiles<<<1, kScanThreads, 0, s>>>(tile_sums, (int)ntiles, out + n);
+  PCAONE_LAUNCH_CHECK();
+  k_scan_apply<<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, tile_sums, out);
+  PCAONE_LAUNCH_CHECK();
+}
+
+int64_t scan_tiles_needed(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
 
 void launch_h_buckets(int64_t win, int N, int L, int LP, const int64_t* ptr, const int32_t* bpos, const double* bval,
                       const int32_t* perm, const double* scale, const float* Rf, int64_t rbase, double* Hx,
