@@ -7,8 +7,10 @@
 // of the FP32 rate on this GPU, so the two O(rows * L^2) kernels (the Gram /
 // cross product and the tall x small product) compute in FP32 pairs
 // (double-float: error-free TwoProduct / TwoSum, about 44 significand bits),
-// which is far below the 24-bit integer slices the window products use; the
-// small L x L kernels stay in FP64.
+// which is far below the 24-bit integer slices the window products use.  The
+// (k+p)^2 Cholesky and inverse are latency-bound chains of square roots and
+// reciprocals and run in double-float too (dd.cuh); the Jacobi eigensolver,
+// the Householder sign rule and the small products stay in FP64.
 //
 // Tall matrices (N x L, M x L) are row-major with leading dimension LP (the
 // sketch width padded to a multiple of 8; padding columns are zero).  Small

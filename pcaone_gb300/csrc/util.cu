@@ -1,6 +1,8 @@
 // Small utility kernels: the missing-genotype lists (by position, and grouped
-// by window and sample), the missing-entry term of the H product, the sign
-// convention flip_UV, and the row-major -> column-major copy of outputs.
+// by window and sample, with the device prefix sum of the group offsets), the
+// segmented gather of the missing-entry terms, the EM term of H in the FP32
+// form, the sign convention flip_UV, and the row-major -> column-major copy of
+// outputs.
 #include <algorithm>
 
 #include "internal.cuh"
