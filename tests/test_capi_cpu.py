@@ -43,3 +43,40 @@ def test_abi_version_and_defaults(lib):
 def test_null_context_is_an_argument_error(lib):
     assert lib.pcaone_gpu_load_bed(None, None, 0, 0) == -1
     assert lib.pcaone_gpu_close(None) == 0
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include "pcaone_gpu.h"
+
+int main(void) {
+  pcaone_gpu_params p;
+  pcaone_gpu_default_params(&p);
+  if (pcaone_gpu_abi_version() != 1) return 1;
+  if (p.k != 10 || p.oversamples != 10 || p.bands != 64) return 2;
+  /* a null context is an argument error, reported without a GPU */
+  if (pcaone_gpu_load_bed(NULL, NULL, 0, 0) != PCAONE_E_ARG) return 3;
+  if (pcaone_gpu_close(NULL) != 0) return 4;
+  puts("c caller ok");
+  return 0;
+}
+"""
+
+
+def test_header_is_plain_c_and_links_from_c(tmp_path, lib):
+    """The header compiles as strict C99 and a C program links against the
+    library and calls its GPU-free entry points."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(capi.LIBPATH)
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.dirname(HEADER),
+                    str(src), "-o", str(exe), "-L", libdir, "-lpcaone_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, (out.returncode, out.stdout, out.stderr)
+    assert "c caller ok" in out.stdout
