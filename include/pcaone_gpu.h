@@ -37,8 +37,9 @@ extern "C" {
 #define PCAONE_PREC_FP32 0    /* FP32 SIMT products, FP64 window sums */
 #define PCAONE_PREC_BF16 1    /* tcgen05 tensor-core products: exact BF16 dosages; the test
                                  matrix and G split per column into three integer BF16 slices
-                                 (24 bits), exact integer accumulation in TMEM, FP32/FP64
-                                 epilogue; missing genotypes as an exact sparse term */
+                                 (27 bits), exact integer accumulation in TMEM, slices combined
+                                 exactly in int64, FP64 epilogue; missing genotypes as an exact
+                                 sparse term */
 #define PCAONE_PREC_FP8 2     /* reserved: FP8 e4m3 operands (not built yet) */
 #define PCAONE_PREC_BF16X3 3  /* same as PCAONE_PREC_BF16 */
 

@@ -128,6 +128,9 @@ struct Context {
   int64_t blocksize = 0;
   // window scratch
   DBuf<float> part, hpart, g32;
+  // tensor-core form: chunk and split partials (int64 slice combinations for
+  // genotypes, FP32 for dense input)
+  DBuf<long long> tpart, thpart;
   // small matrices and reductions
   DBuf<double> W, R1, R1i, R2, R2i, R3, R3i, Rt, Rti, UB, sigma, T, tmp, sgn, red, mevv;
   DBuf<int> status, flag;
@@ -361,16 +364,24 @@ static void tc_make_bed_maps(Context& c) {
                   64, false);
 }
 
-static void tc_shapes(int win, int npad, int& chunk, int& nchunks, int& per_split, int& nsplit) {
-  const int xt = ceil_div(win, 128);
-  int nch = std::max(1, ceil_div(304, xt));
-  chunk = round_up(ceil_div(npad, nch), 64);
-  chunk = std::min(chunk, 4096);
-  nchunks = ceil_div(npad, chunk);
-  const int xh = npad / 128;
-  int ns = std::max(1, ceil_div(304, xh));
-  per_split = round_up(ceil_div(win, ns), 64);
-  per_split = std::min(per_split, 4096);
+// launch shapes of one window's tensor-core products: G tiles of 128 SNPs x
+// chunks of samples, H tiles of 128 samples x splits of the window's SNPs.
+// Genotypes (exact integer accumulation, K per CTA <= kMaxKExact): the fewest
+// waves of long CTAs (tc::k_parts).  Dense FP16 input accumulates in FP32, so
+// its error grows with K per CTA: at least 304 CTAs of at most 4096.
+static void tc_shapes(const Context& c, int win, int S, int& chunk, int& nchunks, int& per_split, int& nsplit) {
+  if (c.dense) {
+    const int xt = ceil_div(win, 128), xh = c.npad / 128;
+    chunk = std::min(round_up(ceil_div(c.npad, std::max(1, ceil_div(304, xt))), 64), tc::kMaxKDense);
+    per_split = std::min(round_up(ceil_div(win, std::max(1, ceil_div(304, xh))), 64), tc::kMaxKDense);
+  } else {
+    const int slots = tc::cta_slots(c.LP, S, false);
+    const int nch = tc::k_parts(ceil_div(win, 128), c.npad, tc::kMaxKExact, slots);
+    chunk = round_up(ceil_div(c.npad, nch), 64);
+    const int nsp = tc::k_parts(c.npad / 128, win, tc::kMaxKExact, slots);
+    per_split = round_up(ceil_div(win, nsp), 64);
+  }
+  nchunks = ceil_div(c.npad, chunk);
   nsplit = ceil_div(win, per_split);
 }
 
@@ -381,10 +392,12 @@ static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
   size_t need_part = 1, need_hpart = 1;
   for (int64_t n : lens) {
     if (n <= 0) continue;
-    int ch, nch, per, nsp;
-    tc_shapes((int)n, c.npad, ch, nch, per, nsp);
-    need_part = std::max(need_part, (size_t)nch * n * LP);
-    need_hpart = std::max(need_hpart, (size_t)nsp * c.npad * LP);
+    for (int S = 1; S <= 3; ++S) {
+      int ch, nch, per, nsp;
+      tc_shapes(c, (int)n, S, ch, nch, per, nsp);
+      need_part = std::max(need_part, (size_t)nch * n * LP);
+      need_hpart = std::max(need_hpart, (size_t)nsp * c.npad * LP);
+    }
   }
   c.wsl.ensure((size_t)3 * LP * c.npad, c.stream);
   c.gt.ensure((size_t)3 * LP * c.ldg, c.stream);
@@ -408,8 +421,8 @@ static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
   c.err.ensure(1, c.stream);
   c.cr_part.ensure((size_t)tc::kColRedBlocks * LP, c.stream, false);
   c.cr_cnt.ensure(1, c.stream, true);
-  c.part.ensure(std::max(need_part, c.part.n), c.stream, false);
-  c.hpart.ensure(std::max(need_hpart, c.hpart.n), c.stream, false);
+  c.tpart.ensure(need_part, c.stream, false);
+  c.thpart.ensure(need_hpart, c.stream, false);
   c.bed_work = c.bed.p;
   tc_make_bed_maps(c);
   const int sl = c.dense ? tc::kMapF16 : tc::kMapBF16;  // slice digits: FP16 for dense input, else BF16
@@ -748,8 +761,8 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
     c.w_slices = S;
   }
   int chunk, nch, per, nsp;
-  tc_shapes((int)n, c.npad, chunk, nch, per, nsp);
-  if ((size_t)nch * n * LP > c.part.n || (size_t)nsp * c.npad * LP > c.hpart.n || n > c.win_max)
+  tc_shapes(c, (int)n, S, chunk, nch, per, nsp);
+  if ((size_t)nch * n * LP > c.tpart.n || (size_t)nsp * c.npad * LP > c.thpart.n || n > c.win_max)
     throw Error(PCAONE_E_ARG, "internal: tensor-core window scratch too small");
   const bool any_miss = c.counts_total_missing > 0;
   const bool em = c.fitted && c.P.emu && c.nnz > 0;
@@ -780,7 +793,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ga.nstages = tc::stages_for(LP, S, tc::g_tile_bytes(c.dense), c.dense);
   ga.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ga.nstages, c.dense));
   ga.wscale = c.wunit.p;
-  ga.part = c.part.p;
+  ga.part = c.tpart.p;
   ga.err = c.err.p;
   ga.dense = c.dense ? 1 : 0;
   mark(0);
@@ -815,7 +828,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   // the B operand tensor map spans ldg columns; windows shorter than the
   // longest one leave the tail zeroed by the slicing kernel
   fa.ldg = c.ldg;
-  fa.part = c.part.p;
+  fa.part = c.tpart.p;
   fa.colsum = c.colsum.p;
   fa.F = c.F.p;
   fa.scale = c.scale.p;
@@ -843,13 +856,9 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ha.nstages = tc::stages_for(LP, S, tc::h_tile_bytes(c.dense), c.dense);
   ha.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ha.nstages, c.dense));
   ha.hscale = c.hunit.p;
-  ha.hpart = c.hpart.p;
+  ha.hpart = c.thpart.p;
   ha.err = c.err.p;
   ha.dense = c.dense ? 1 : 0;
-  ha.hisum = any_miss ? c.hisum.p : nullptr;
-  ha.gmunit_m = c.gmunit.p + (size_t)(S - 1) * LP;
-  ha.hesum = (any_miss && em) ? c.hesum.p : nullptr;
-  ha.hunit_m = c.hunit.p + (size_t)(S - 1) * LP;
   if (any_miss) {
     // sum_j Gm_j (and sum_j 2 e_j Gh_j) over each sample's missing SNPs of the window
     SegGatherArgs sg{};
@@ -871,7 +880,20 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   mark(1);
   tc::launch_h(c.map_bed_h, c.map_gt, ha, c.stream);
   close_mark();
-  tc::launch_h_finish(c.N, c.npad, c.L, LP, c.hpart.p, nsp, c.cvec.p, Hx, c.stream);
+  tc::HFinishArgs hf{};
+  hf.nsamples = c.N;
+  hf.npad = c.npad;
+  hf.L = c.L;
+  hf.LP = LP;
+  hf.nsplit = nsp;
+  hf.dense = c.dense ? 1 : 0;
+  hf.hpart = c.thpart.p;
+  hf.c = c.cvec.p;
+  hf.Hx = Hx;
+  hf.hunit_m = c.hunit.p + (size_t)(S - 1) * LP;
+  hf.hisum = any_miss ? c.hisum.p : nullptr;
+  hf.hesum = (any_miss && em) ? c.hesum.p : nullptr;
+  tc::launch_h_finish(hf, c.stream);
 }
 
 // one window: G[pos0 .. pos0+n) = X_w Omega;  Hx += X_w^T G_w

@@ -12,16 +12,18 @@
 //   H_i += (D Gh)_i - c + sum_{j missing} 2 (f_j + e_ij) Gh_j,
 //          Gh_j = 1/2 s_j G_j,  c = sum_j 2 f_j Gh_j
 // where W is the test matrix Omega held as S integer slices (S = 1 or 3):
-// per column l a power-of-two unit u_ls = 2^(E_l - 7 - 8s) with
+// per column l a power-of-two unit u_ls = 2^(E_l - 8 - 9s) with
 // max_i |Omega_il| < 2^E_l, and W_il = sum_s u_ls * w_sil with integers
-// |w_sil| <= 128, exact in BF16 (Ozaki-style error-free splitting; three slices
-// carry 24 significand bits).  Each slice has its own TMEM accumulator: the
-// products d*w are integers of magnitude <= 256 and every partial sum of a CTA
-// (K <= 4096) stays below 2^24, so the tensor core accumulates exactly and no
-// rounding bias enters; the epilogue combines the slices with their units.  Gh
-// is split the same way (per-column units over the window).  The centring and
-// missing-entry terms use the same represented values as the products, so the
-// operator applied is exactly X times the sliced matrix.
+// |w_sil| <= 256, exact in BF16 (Ozaki-style error-free splitting with
+// balanced base-512 digits; three slices carry 27 significand bits).  Each
+// slice has its own TMEM accumulator: the products d*w are integers of
+// magnitude <= 512 and every partial sum of a CTA (K <= kMaxKExact = 16384)
+// stays below 2^23, so the tensor core accumulates exactly and no rounding
+// enters; the epilogue combines the slices exactly in int64, and one FP64
+// conversion per output follows.  Gh is split the same way (per-column units
+// over the window).  The centring and missing-entry terms use the same
+// represented values as the products, so the operator applied is exactly X
+// times the sliced matrix.
 //
 // Kernels (one CTA = 320 threads in three roles, see role_wait below; two
 // CTAs share an SM when their TMEM plans fit in half of it, see pair_per_sm):
@@ -362,6 +364,40 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// Epilogue helpers.  The accumulator of slice s for columns c0 .. c0+7 of a
+// lane sits at TMEM columns s*LP + c0 ...
+//
+// Genotype input: each slice sum is an exact integer (|v| <= 512 K <= 2^23),
+// so the slices combine exactly in int64, in units of the last slice:
+//   P = sum_s v_s 512^(S-1-s)   (|P| < 2^42 for S = 3)
+__device__ __forceinline__ void combine_slices_exact(uint32_t lane_base, int c0, int LP, int S, long long* acc) {
+  float v[8];
+  for (int s = 0; s < S; ++s) {
+    tmem_ld8(lane_base + s * LP + c0, v);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) acc[t] = acc[t] * (1 << kDigitBits) + __float2ll_rn(v[t]);
+  }
+}
+// Dense input: slice sums times their power-of-two units, smallest units first
+// so that the FP32 sum rounds as little as possible
+__device__ __forceinline__ void store_slice_sum(uint32_t lane_base, int c0, int LP, int S, const float* unit,
+                                                float* sum) {
+  float v[8];
+  for (int s = S - 1; s >= 0; --s) {
+    tmem_ld8(lane_base + s * LP + c0, v);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) sum[t] = fmaf(unit[s * LP + c0 + t], v[t], sum[t]);
+  }
+}
+__device__ __forceinline__ void store_f32x8(float* dst, const float* v) {
+  *reinterpret_cast<float4*>(dst) = make_float4(v[0], v[1], v[2], v[3]);
+  *reinterpret_cast<float4*>(dst + 4) = make_float4(v[4], v[5], v[6], v[7]);
+}
+__device__ __forceinline__ void store_i64x8(long long* dst, const long long* v) {
+#pragma unroll
+  for (int t = 0; t < 8; t += 2) *reinterpret_cast<longlong2*>(dst + t) = make_longlong2(v[t], v[t + 1]);
+}
+
 // ---------------------------------------------------------------------------
 // G product
 // ---------------------------------------------------------------------------
@@ -400,7 +436,8 @@ __global__ void __launch_bounds__(kThreads, 2)
     mbar_init(&acc_bar, 1);
     fence_mbar_init();
   }
-  for (int e = tid; e < S * LP; e += kThreads) unit[e] = (float)a.wscale[e];
+  if (kDense)
+    for (int e = tid; e < S * LP; e += kThreads) unit[e] = (float)a.wscale[e];
   if (warp == 0) tmem_alloc(&tmem_sh, (uint32_t)a.tmem_cols);
   tc_fence_before();
   __syncthreads();
@@ -504,27 +541,26 @@ __global__ void __launch_bounds__(kThreads, 2)
       }
       mbar_arrive(&dec_bar[st]);
     }
-    // ---- epilogue: exact integer slice sums times power-of-two units (FP32 FMAs) ----
+    // ---- epilogue ----
     const bool ok = nk > 0 && role_wait(&acc_bar, 0u, &abort_sh);
     tc_fence_after();
     const int quarter = warp & 3, chalf = (warp - kDecodeWarp0) >> 2;
     const int j = row0 + quarter * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
-    float v[8];
     if (!abort_sh) {
       for (int c0 = chalf * (LP / 2); c0 < (chalf + 1) * (LP / 2); c0 += 8) {
-        float sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        if (ok) {
-          for (int s = S - 1; s >= 0; --s) {
-            tmem_ld8(lane_base + s * LP + c0, v);
-#pragma unroll
-            for (int t = 0; t < 8; ++t) sum[t] = fmaf(unit[s * LP + c0 + t], v[t], sum[t]);
-          }
-        }
-        if (j < a.nsnp) {
-          float* dst = a.part + ((size_t)blockIdx.y * a.nsnp + j) * LP + c0;
-          *reinterpret_cast<float4*>(dst) = make_float4(sum[0], sum[1], sum[2], sum[3]);
-          *reinterpret_cast<float4*>(dst + 4) = make_float4(sum[4], sum[5], sum[6], sum[7]);
+        if constexpr (kDense) {
+          // FP16 values: slice sums times their power-of-two units (FP32 FMAs)
+          float sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          if (ok) store_slice_sum(lane_base, c0, LP, S, unit, sum);
+          if (j < a.nsnp) store_f32x8(reinterpret_cast<float*>(a.part) + ((size_t)blockIdx.y * a.nsnp + j) * LP + c0, sum);
+        } else {
+          // genotypes: every slice sum is an integer below 2^23, combined
+          // exactly in int64 in units of the last slice
+          long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          if (ok) combine_slices_exact(lane_base, c0, LP, S, acc);
+          if (j < a.nsnp)
+            store_i64x8(reinterpret_cast<long long*>(a.part) + ((size_t)blockIdx.y * a.nsnp + j) * LP + c0, acc);
         }
       }
     }
@@ -552,7 +588,6 @@ __global__ void __launch_bounds__(kThreads, 2)
   __shared__ uint32_t tmem_sh;
   __shared__ volatile int abort_sh;
   __shared__ float unit[3 * 112];
-  __shared__ float munit[2 * 112];  // units of the missing-entry sums (Gm integers, EM products)
   __shared__ uint32_t lut[kDense ? 1 : kLutWords];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (!kDense) lut_init(lut, tid, kThreads);
@@ -565,11 +600,8 @@ __global__ void __launch_bounds__(kThreads, 2)
   const int nst = a.nstages;
   const int ncat = S * LP;
 
-  for (int e = tid; e < ncat; e += kThreads) unit[e] = (float)a.hscale[e];
-  for (int e = tid; e < LP; e += kThreads) {
-    munit[e] = a.hisum ? (float)a.gmunit_m[e] : 0.f;
-    munit[LP + e] = a.hesum ? (float)(2.0 * exp2i(-24 + kSegValueShift) * a.hunit_m[e]) : 0.f;
-  }
+  if (kDense)
+    for (int e = tid; e < ncat; e += kThreads) unit[e] = (float)a.hscale[e];
   if (tid == 0) {
     abort_sh = 0;
     for (int s = 0; s < nst; ++s) {
@@ -687,43 +719,18 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int quarter = warp & 3, chalf = (warp - kDecodeWarp0) >> 2;
     const int i = samp0 + quarter * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
-    float v[8];
     if (!abort_sh) {
       for (int c0 = chalf * (LP / 2); c0 < (chalf + 1) * (LP / 2); c0 += 8) {
-        // smallest units first, so the FP32 sum rounds as little as possible
-        float sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        if (ok) {
-          for (int s = S - 1; s >= 0; --s) {
-            tmem_ld8(lane_base + s * LP + c0, v);
-#pragma unroll
-            for (int t = 0; t < 8; ++t) sum[t] = fmaf(unit[s * LP + c0 + t], v[t], sum[t]);
-          }
+        const size_t row = (size_t)blockIdx.y * a.npad + i;
+        if constexpr (kDense) {
+          float sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          if (ok) store_slice_sum(lane_base, c0, LP, S, unit, sum);
+          store_f32x8(reinterpret_cast<float*>(a.hpart) + row * LP + c0, sum);
+        } else {
+          long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          if (ok) combine_slices_exact(lane_base, c0, LP, S, acc);
+          store_i64x8(reinterpret_cast<long long*>(a.hpart) + row * LP + c0, acc);
         }
-        // the first split also adds the missing-entry terms of its samples
-        // (int64 sums from k_seg_gather, read and cleared here)
-        if (blockIdx.y == 0 && a.hisum) {
-          unsigned long long* hs = a.hisum + (size_t)i * LP + c0;
-#pragma unroll
-          for (int t = 0; t < 8; ++t) {
-            if (c0 + t < a.L) {
-              sum[t] = fmaf(__ll2float_rn((long long)hs[t]), munit[c0 + t], sum[t]);
-              hs[t] = 0ull;
-            }
-          }
-          if (a.hesum) {
-            unsigned long long* he = a.hesum + (size_t)i * LP + c0;
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-              if (c0 + t < a.L) {
-                sum[t] = fmaf(__ll2float_rn((long long)he[t]), munit[LP + c0 + t], sum[t]);
-                he[t] = 0ull;
-              }
-            }
-          }
-        }
-        float* dst = a.hpart + ((size_t)blockIdx.y * a.npad + i) * LP + c0;
-        *reinterpret_cast<float4*>(dst) = make_float4(sum[0], sum[1], sum[2], sum[3]);
-        *reinterpret_cast<float4*>(dst + 4) = make_float4(sum[4], sum[5], sum[6], sum[7]);
       }
     }
   }
@@ -801,10 +808,10 @@ __global__ void __launch_bounds__(256) k_colred(const double* __restrict__ A, in
   if (tid == 0) *cnt = 0u;
 }
 
-// Split v (|v| < 2^E) into S integer slices: m = rint(v * 2^(8S-1-E)) has
-// |m| <= 2^(8S-1), and its balanced base-256 digits w_s (m = sum_s w_s
-// 256^(S-1-s), |w_s| <= 128, exact in BF16) are the slices, with units
-// u_s = 2^(E-7-8s).  Returns the represented value m * u_(S-1).  Integer
+// Split v (|v| < 2^E) into S integer slices: m = rint(v * 2^(9S-1-E)) has
+// |m| <= 2^(9S-1), and its balanced base-512 digits w_s (m = sum_s w_s
+// 512^(S-1-s), |w_s| <= 256, exact in BF16) are the slices, with units
+// u_s = 2^(E-8-9s).  Returns the represented value m * u_(S-1).  Integer
 // digit arithmetic keeps the FP64 work to one multiply and one conversion.
 // The digits are stored as BF16 or (f16) FP16 bit patterns, exact in both.
 // *m_out (optional) receives m.
@@ -813,20 +820,21 @@ __device__ __forceinline__ uint16_t digit_bits(int w, bool f16) {
 }
 __device__ __forceinline__ double split_store(double v, int E, int S, uint16_t* dst, size_t slice_stride, bool f16,
                                               int* m_out = nullptr) {
-  const int m = __double2int_rn(v * exp2i(8 * S - 1 - E));
+  constexpr int kBase = 1 << kDigitBits, kHalf = kBase / 2;
+  const int m = __double2int_rn(v * exp2i(kDigitBits * S - 1 - E));
   if (m_out) *m_out = m;
   int rest = m;
   for (int s = S - 1; s > 0; --s) {
-    const int w = ((rest + 128) & 255) - 128;
+    const int w = ((rest + kHalf) & (kBase - 1)) - kHalf;
     dst[(size_t)s * slice_stride] = digit_bits(w, f16);
-    rest = (rest - w) >> 8;
+    rest = (rest - w) / kBase;  // exact: rest - w is a multiple of the base
   }
   dst[0] = digit_bits(rest, f16);
-  return (double)m * exp2i(E - 8 * S + 1);
+  return (double)m * exp2i(E - kDigitBits * S + 1);
 }
 
 // W slices of Omega (S*LP rows x npad, K-major) and the represented W, in FP64
-// and as the integer m (|m| <= 2^23; the value is m times the last slice unit).
+// and as the integer m (|m| <= 2^26; the value is m times the last slice unit).
 // A block takes 64 rows of Omega (coalesced reads, and coalesced writes of the
 // represented values), keeps their digits in shared memory and writes each
 // slice row's 64 digits as one 128-byte run.  npad is a multiple of 64.
@@ -857,7 +865,7 @@ __global__ void k_units(const int* __restrict__ E, int LP, int S, int eoff, doub
   const int idx = threadIdx.x + blockIdx.x * blockDim.x;
   if (idx >= S * LP) return;
   const int s = idx / LP, l = idx % LP;
-  unit[idx] = ldexp(1.0, E[l] + eoff - 7 - 8 * s);
+  unit[idx] = ldexp(1.0, E[l] + eoff - (kDigitBits - 1) - kDigitBits * s);
 }
 
 // G rows of the window: FP64 sum of the chunk partials, the centring term, and
@@ -876,17 +884,28 @@ __global__ void k_tc_g_finish(GFinishArgs a) {
     const int64_t pos = a.pos0 + j;
     const int64_t snp = a.perm ? (int64_t)a.perm[pos] : pos;
     const double f = a.F[snp], s = a.scale[snp];
-    // chunk partials summed as an FP32 pair (TwoSum, about 48 bits: far below
-    // the FP32 rounding of each partial) rather than on the FP64 pipe
-    float ph = 0.f, pl = 0.f;
-    for (int c = 0; c < a.nchunks; ++c) {
-      const float v = a.part[((size_t)c * a.nsnp + j) * LP + l];
-      const float t = __fadd_rn(ph, v);
-      const float bv = __fsub_rn(t, ph);
-      pl = __fadd_rn(pl, __fadd_rn(__fsub_rn(ph, __fsub_rn(t, bv)), __fsub_rn(v, bv)));
-      ph = t;
+    double pd;
+    if (a.vfac == 1.0) {
+      // dense input: FP32 chunk partials summed as an FP32 pair (TwoSum, about
+      // 48 bits: far below the FP32 rounding of each partial)
+      const float* part = reinterpret_cast<const float*>(a.part);
+      float ph = 0.f, pl = 0.f;
+      for (int c = 0; c < a.nchunks; ++c) {
+        const float v = part[((size_t)c * a.nsnp + j) * LP + l];
+        const float t = __fadd_rn(ph, v);
+        const float bv = __fsub_rn(t, ph);
+        pl = __fadd_rn(pl, __fadd_rn(__fsub_rn(ph, __fsub_rn(t, bv)), __fsub_rn(v, bv)));
+        ph = t;
+      }
+      pd = (double)ph + (double)pl;
+    } else {
+      // genotypes: exact int64 sum of the chunks' slice combinations (below
+      // 2^53), one conversion, scaled by the last slice unit (a power of two)
+      const long long* part = reinterpret_cast<const long long*>(a.part);
+      long long ps = 0;
+      for (int c = 0; c < a.nchunks; ++c) ps += part[((size_t)c * a.nsnp + j) * LP + l];
+      pd = (double)ps * a.wunit_m[l];
     }
-    const double pd = (double)ph + (double)pl;
     double miss = 0.0;
     if (a.gisum) {
       miss = f * a.wunit_m[l] * (double)(long long)a.gisum[idx];
@@ -929,9 +948,9 @@ __global__ void k_tc_gh_slices(GFinishArgs a, const int* __restrict__ Eh) {
       a.cpart[(size_t)j * LP + l] = a.F[snp] * ghq;
     } else {
       const int e = Eh[l] + 1;
-      const int m = __double2int_rn(2.0 * a.F[snp] * ghq * exp2i(8 * S - 1 - e));
+      const int m = __double2int_rn(2.0 * a.F[snp] * ghq * exp2i(kDigitBits * S - 1 - e));
       a.gmint[(size_t)j * LP + l] = m;
-      a.cpart[(size_t)j * LP + l] = (double)m * exp2i(e - 8 * S + 1);
+      a.cpart[(size_t)j * LP + l] = (double)m * exp2i(e - kDigitBits * S + 1);
     }
   } else {
     for (int s = 0; s < S; ++s) dh[s * sstride] = 0;
@@ -943,18 +962,40 @@ __global__ void k_tc_gh_slices(GFinishArgs a, const int* __restrict__ Eh) {
   }
 }
 
-// H rows: FP64 sum of the split partials (the first carries the
-// missing-entry terms) minus c.
-__global__ void k_tc_h_finish(int nsamples, int npad, int L, int LP, const float* __restrict__ hpart, int nsplit,
-                              const double* __restrict__ c, double* __restrict__ Hx) {
+// H rows: the split partials, the missing-entry terms and the centring term.
+// Genotypes: the dosage part P (units u = the last Gh slice unit), the Gm sums
+// (units 2u) and the EM products (units 2^-15 u) are combined exactly in int64
+// in units of 2^-15 u (below 2^56 in magnitude), converted once and scaled;
+// the int64 missing-entry sums are cleared for the next window.  Dense input:
+// FP64 sum of the FP32 split partials.
+__global__ void k_tc_h_finish(HFinishArgs a) {
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (idx >= (int64_t)nsamples * LP) return;
+  const int LP = a.LP;
+  if (idx >= (int64_t)a.nsamples * LP) return;
   const int64_t i = idx / LP;
   const int l = (int)(idx - i * LP);
-  if (l >= L) return;
-  double acc = 0.0;
-  for (int s = 0; s < nsplit; ++s) acc += (double)hpart[((size_t)s * npad + i) * LP + l];
-  Hx[idx] += acc - c[l];
+  if (l >= a.L) return;
+  double h;
+  if (a.dense) {
+    const float* hp = reinterpret_cast<const float*>(a.hpart);
+    h = 0.0;
+    for (int s = 0; s < a.nsplit; ++s) h += (double)hp[((size_t)s * a.npad + i) * LP + l];
+  } else {
+    const long long* hp = reinterpret_cast<const long long*>(a.hpart);
+    long long t = 0;
+    for (int s = 0; s < a.nsplit; ++s) t += hp[((size_t)s * a.npad + i) * LP + l];
+    t *= 32768;
+    if (a.hisum) {
+      t += (long long)a.hisum[idx] * 65536;
+      a.hisum[idx] = 0ull;
+      if (a.hesum) {
+        t += (long long)a.hesum[idx];
+        a.hesum[idx] = 0ull;
+      }
+    }
+    h = (double)t * (a.hunit_m[l] * (1.0 / 32768.0));
+  }
+  a.Hx[idx] += h - a.c[l];
 }
 
 __global__ void k_gather_rows(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, int64_t stride,
@@ -1006,6 +1047,40 @@ void make_map_2d(CUtensorMap* map, const void* base, int dtype, uint64_t inner, 
 // genotype window this cut both products by a third against one CTA per SM
 // with eight stages.  Dense input (A in shared memory): one CTA per SM.
 bool pair_per_sm(int LP, int nslice, bool dense) { return !dense && nslice * LP + 2 * 32 <= 256; }
+
+int cta_slots(int LP, int nslice, bool dense) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    PCAONE_CUDA(cudaGetDevice(&dev));
+    PCAONE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return sms * (pair_per_sm(LP, nslice, dense) ? 2 : 1);
+}
+
+// A CTA's fixed cost (TMEM allocation, barrier and table set-up, pipeline
+// fill, epilogue) in K elements: about the time of 12 pipeline steps of 64.
+constexpr int kCtaCostK = 768;
+
+int k_parts(int tiles, int K, int kmax, int slots) {
+  if (K <= 0) return 1;
+  const int lo = std::max(1, ceil_div(K, kmax));
+  const int hi = std::max(lo, std::min(ceil_div(K, 1024), lo + 128));
+  int best = lo;
+  double best_cost = 1e300;
+  for (int p = lo; p <= hi; ++p) {
+    const int kp = round_up(ceil_div(K, p), 64);
+    const int parts = ceil_div(K, kp);
+    const int64_t ctas = (int64_t)tiles * parts;
+    const int64_t waves = (ctas + slots - 1) / slots;
+    const double cost = (double)waves * (kp + kCtaCostK);
+    if (cost < best_cost * 0.999) {
+      best_cost = cost;
+      best = parts;
+    }
+  }
+  return best;
+}
 
 int stages_for(int LP, int nslice, int pbytes, bool dense) {
   const SmemLayout l = layout_for(LP, nslice, pbytes, dense);
@@ -1129,10 +1204,9 @@ void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* gmuni
   launch_colred<false>(a.cpart, a.nsnp, a.LP, cr, c_out, nullptr, s);
 }
 
-void launch_h_finish(int nsamples, int npad, int L, int LP, const float* hpart, int nsplit, const double* c,
-                     double* Hx, cudaStream_t s) {
-  const int64_t n = (int64_t)nsamples * LP;
-  k_tc_h_finish<<<ceil_div(n, 256), 256, 0, s>>>(nsamples, npad, L, LP, hpart, nsplit, c, Hx);
+void launch_h_finish(const HFinishArgs& a, cudaStream_t s) {
+  const int64_t n = (int64_t)a.nsamples * a.LP;
+  k_tc_h_finish<<<ceil_div(n, 256), 256, 0, s>>>(a);
   PCAONE_LAUNCH_CHECK();
 }
 

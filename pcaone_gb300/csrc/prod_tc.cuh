@@ -20,14 +20,14 @@ struct GArgs {
   int nchunks;            // gridDim.y
   int nstages;            // pipeline depth
   int tmem_cols;          // TMEM columns allocated per CTA
-  const double* wscale;   // S x LP units of the W slices
-  float* part;            // [nchunks][nsnp][LP]
+  const double* wscale;   // S x LP units of the W slices (dense input)
+  void* part;             // [nchunks][nsnp][LP]: int64 slice combinations (genotypes) or FP32 sums (dense)
   int* err;               // set to 1 when a bounded wait gave up
   int dense;              // 1: FP16 values (FileBinary input) instead of packed codes
 };
 
-// H += X_w^T * Gh for one SNP window (dosage part; the first split's
-// epilogue adds the missing-entry sums gathered by k_seg_gather)
+// H += X_w^T * Gh for one SNP window (dosage part; k_tc_h_finish adds the
+// missing-entry sums gathered by k_seg_gather)
 struct HArgs {
   int64_t pos0;
   int nsnp;
@@ -39,14 +39,21 @@ struct HArgs {
   int npad;               // gridDim.x * 128
   int nstages;
   int tmem_cols;
-  const double* hscale;   // S x LP units of the Gh slices
-  float* hpart;           // [nsplit][npad][LP]
+  const double* hscale;   // S x LP units of the Gh slices (dense input)
+  void* hpart;            // [nsplit][npad][LP]: int64 slice combinations (genotypes) or FP32 sums (dense)
   int* err;
+  int dense;              // 1: FP16 values instead of packed codes
+};
+
+// H rows of one window: Hx += sum of the split partials + missing-entry terms - c
+struct HFinishArgs {
+  int nsamples, npad, L, LP, nsplit, dense;
+  const void* hpart;          // as HArgs::hpart
+  const double* c;            // LP centring terms
+  double* Hx;
+  const double* hunit_m;      // per column unit of the Gh integers (the last slice unit)
   unsigned long long* hisum;  // npad x LP int64 sums of Gm over missing entries (nullptr: none), cleared
-  const double* gmunit_m;     // per column unit of the Gm integers
   unsigned long long* hesum;  // npad x LP int64 EM product sums (nullptr: no EM), cleared
-  const double* hunit_m;      // per column unit of the Gh integers
-  int dense;                  // 1: FP16 values instead of packed codes
 };
 
 struct GFinishArgs {
@@ -55,7 +62,7 @@ struct GFinishArgs {
   int nsnp;
   int L, LP, nslice, nchunks;
   int ldg;                       // columns of the Gh operand (window length rounded up to 64)
-  const float* part;             // chunk partials of D W
+  const void* part;              // chunk partials of D W (int64 for genotypes, FP32 for dense input)
   const double* colsum;          // column sums of the sliced W
   const double* F;
   const double* scale;
@@ -82,6 +89,20 @@ inline int h_tile_bytes(bool dense) { return dense ? 64 * 256 : 64 * 32; }
 int stages_for(int LP, int nslice, int pbytes, bool dense);
 int tmem_cols_for(int ncols);
 int tmem_cols_needed(int LP, int nslice, int nstages, bool dense);
+// Slice digits: balanced base-512 integers, |w| <= 256, exact in BF16 and FP16.
+constexpr int kDigitBits = 9;
+// Exact accumulation: a product d*w of a genotype dosage (<= 2) and a slice
+// digit is at most 512 in magnitude, so a CTA that sums at most 2^14 K elements
+// keeps every FP32 accumulator an exactly represented integer (|v| <= 2^23).
+// Dense FP16 input rounds in FP32; its K per CTA stays at 4096.
+constexpr int kMaxKExact = 16384;
+constexpr int kMaxKDense = 4096;
+// CTAs that run at once: two per SM when the TMEM plan pairs, else one
+int cta_slots(int LP, int nslice, bool dense);
+// number of parts to cut a K extent into (tiles CTAs per part): the fewest
+// waves of `slots` CTAs times the per-CTA length plus a fixed cost, each part
+// at most kmax long and a multiple of 64
+int k_parts(int tiles, int K, int kmax, int slots);
 void launch_g(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs& a, cudaStream_t s);
 void launch_h(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs& a, cudaStream_t s);
 // scratch of the multi-block column reductions: kColRedBlocks x LP partials and
@@ -98,8 +119,7 @@ void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv
 // (gmunit: S x LP, the last slice row is the unit of gmint), c
 void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* gmunit, double* c_out,
                      const ColRedScratch& cr, cudaStream_t s);
-void launch_h_finish(int nsamples, int npad, int L, int LP, const float* hpart, int nsplit, const double* c,
-                     double* Hx, cudaStream_t s);
+void launch_h_finish(const HFinishArgs& a, cudaStream_t s);
 void launch_gather_rows(const uint8_t* src, uint8_t* dst, int64_t stride, const int32_t* perm, int64_t nrows,
                         cudaStream_t s);
 

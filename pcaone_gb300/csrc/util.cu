@@ -257,7 +257,7 @@ __global__ void k_h_buckets(int64_t win, int N, int L, int LP, const int64_t* __
 // group loads their rows (all loads independent), then adds them
 // in entry order while the key is unchanged; a key change (group-uniform)
 // flushes the running sums into the int64 output with atomics.  The row sums
-// are int32: |R| <= 2^23, so a run of 64 entries stays below 2^29.
+// are int64 (|R| <= 2^26: a run of 64 entries reaches 2^32).
 constexpr int kSegRun = 64;
 constexpr int kSegFetch = 8;  // lanes per group that fetch entry indices (the minimum group size)
 
@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(256) k_seg_gather(SegGatherArgs a, int gsize, 
   const int col = 4 * c;
   const bool cols = col < a.L;
   const bool same = a.R2 == a.R;  // G side: the value products use the same integer rows
-  int acc[4] = {0, 0, 0, 0};
+  long long acc[4] = {0, 0, 0, 0};
   long long acc2[4] = {0, 0, 0, 0};
   int cur = -1;
   auto flush = [&]() {
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(256) k_seg_gather(SegGatherArgs a, int gsize, 
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
         if (col + t < a.L) {
-          atomicAdd(o + t, (unsigned long long)(long long)acc[t]);
+          atomicAdd(o + t, (unsigned long long)acc[t]);
           if (VALS) atomicAdd(o2 + t, (unsigned long long)acc2[t]);
         }
       }

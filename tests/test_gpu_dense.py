@@ -4,8 +4,10 @@ file-image loader, and the errors of the dense path.
 
 The dense values are FP16 numbers (the storage of imputed dosages), which the
 reference reads as float32 exactly.  Unlike 2-bit genotypes they are not
-integers, so the tensor core's FP32 accumulation rounds; the tolerance on the
-well-separated PCs is the same as for the genotype path (1e-6).
+integers, so the tensor core's FP32 accumulation rounds like any FP32 GEMM.
+The 1e-8 eigenvalue bar of the genotype path does not apply; on the
+well-separated PCs the tolerance is 1e-6 for both the principal angle and the
+relative eigenvalue error.
 """
 import numpy as np
 import pytest
@@ -16,6 +18,9 @@ from tests.cases import binary_cases
 from tests.test_gpu_parity import compare
 
 pytestmark = pytest.mark.gpu
+
+DENSE_ANGLE_TOL = 1e-6
+DENSE_EIG_TOL = 1e-6
 
 CASES = binary_cases()
 IDS = [c.name for c in CASES]
@@ -36,7 +41,8 @@ def test_dense_rsvd_vs_reference_outputs(case):
         U, S, V, _ = c.run_halko(d_params(o))
         if o.perm:
             assert np.array_equal(c.perm(), case.ref["perm"])
-    compare(U, S, V, case.ref["U"], case.ref["S"], case.ref["V"], f"{case.name}[dense]")
+    compare(U, S, V, case.ref["U"], case.ref["S"], case.ref["V"], f"{case.name}[dense]", angle_tol=DENSE_ANGLE_TOL,
+            eig_tol=DENSE_EIG_TOL)
 
 
 def test_dense_vs_oracle_at_larger_size():
@@ -51,7 +57,7 @@ def test_dense_vs_oracle_at_larger_size():
         c.load_dense(dense.astype(np.float32))
         U, S, V, _ = c.run_halko(capi.default_params(svd=2, k=10, oversamples=10, maxp=6, bands=16, perm=1,
                                                      standardize=0, precision=capi.PREC_BF16))
-    compare(U, S, V, op.U, op.S, op.V, "dense 3000x20000")
+    compare(U, S, V, op.U, op.S, op.V, "dense 3000x20000", angle_tol=DENSE_ANGLE_TOL, eig_tol=DENSE_EIG_TOL)
 
 
 def test_binary_file_image_matches_dense_load(tmp_path):

@@ -2,13 +2,20 @@
 reference's own outputs (tests/golden/).
 
 Tolerances (floating point):
-  * decode, counts, allele frequencies: bit-exact.
-  * FP32 block products vs the FP64 oracle, same Omega, same schedule:
+  * decode, counts, allele frequencies: bit-exact (the decode and the products
+    themselves are checked bit for bit in test_gpu_exact.py).
+  * U, S, V of both forms vs the reference's FP64 outputs or the FP64 oracle,
+    same Omega, same schedule (the benchmark spec's bar):
       - largest principal angle (sin) over the well-separated leading PCs
         (relative eigen-gap > 5%): <= 1e-6
-      - relative eigenvalue error of those PCs: <= 1e-6
+      - relative eigenvalue error of those PCs: <= 1e-8
     Near-degenerate noise PCs are not determined by a few power iterations (the
     reference's own FP64 methods disagree on them); they are not compared.
+  * first-epoch G and H vs the oracle's FP64 products: relative error <= 1e-7
+    for the tensor-core form (the test matrix and G enter as 27-bit integer
+    slices; rounding them to 27 bits relative to the column maximum is the
+    only error left, since the integer products are exact) and <= 1e-6 for the
+    FP32 CUDA-core form.
 """
 import os
 
@@ -23,8 +30,9 @@ from tests.cases import align_signs, golden_case, golden_cases
 pytestmark = pytest.mark.gpu
 
 ANGLE_TOL = 1e-6
-EIG_TOL = 1e-6
-# tensor-core form: three integer BF16 slices per column (24 bits, exact integer
+EIG_TOL = 1e-8
+PROD_TOL = {"bf16": 1e-7, "fp32": 1e-6}
+# tensor-core form: three integer BF16 slices per column (27 bits, exact integer
 # accumulation in TMEM) in every epoch
 PRECISIONS = {"fp32": capi.PREC_FP32, "bf16": capi.PREC_BF16}
 
@@ -112,7 +120,7 @@ def test_first_epoch_products_vs_oracle(prec):
     eg = np.linalg.norm(G - Gr) / np.linalg.norm(Gr)
     eh = np.linalg.norm(Hg - Hr) / np.linalg.norm(Hr)
     print(f"epoch-0 products [{prec}]: rel err G {eg:.2e} H {eh:.2e}")
-    assert eg < 1e-5 and eh < 1e-5
+    assert eg <= PROD_TOL[prec] and eh <= PROD_TOL[prec]
 
 
 @pytest.mark.parametrize("prec", list(PRECISIONS))
@@ -132,6 +140,29 @@ def test_wide_sketch_with_missing(prec):
         c.set_omega(omega)
         U, S, V, _ = c.run_halko(p)
     compare(U, S, V, ref.U, ref.S, ref.V, f"wide[{prec}]")
+
+
+@pytest.mark.parametrize("prec", list(PRECISIONS))
+def test_precision_form_shape(prec):
+    """The shapes of the 200,000 x 1,000,000 precision-form workload at a small
+    size: k=40, p=10 (L=50, padded to 64: the three slices take 192 TMEM
+    columns), 64 windows, N not a multiple of 128, eight Balding-Nichols
+    populations plus 2% admixed samples (Dirichlet ancestry), allele
+    frequencies from Beta(0.5, 0.5) truncated to [0.01, 0.99], and 0.5%
+    missing genotypes."""
+    model = synthetic.model_for("c3", seed=3, nsamples=3001, nsnps=19200, mcar=0.005)
+    packed = synthetic.sample_packed_bed(model)
+    k, os_ = 40, 10
+    omega = H.random_omega(112, model.nsamples, k + os_)
+    d = H.OracleData(packed, model.nsamples, perm=True, bands=64, omega0=omega)
+    ref = H.run_pca_with_halko(d, k, os_, maxp=6)
+    p = capi.default_params(k=k, oversamples=os_, maxp=6, bands=64, precision=PRECISIONS[prec])
+    with capi.Context() as c:
+        c.load_bed(packed, model.nsamples)
+        c.set_omega(omega)
+        U, S, V, _ = c.run_halko(p)
+    n, *_ = compare(U, S, V, ref.U, ref.S, ref.V, f"c3-shape[{prec}]")
+    assert n >= 7  # the seven population PCs are compared
 
 
 def test_matvec_vs_oracle():
