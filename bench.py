@@ -1,7 +1,7 @@
 """Benchmark: seconds to the top-k PCs of a PLINK genotype matrix on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload c2] [--precision fp32]
+                    [--workload c3] [--precision bf16|fp32|fp64]
 
 One step = the whole hot path on one synthetic workload: packed genotypes ->
 counts and allele frequencies -> window-based RSVD (winSVD, 7 epochs for the
@@ -9,7 +9,7 @@ counts and allele frequencies -> window-based RSVD (winSVD, 7 epochs for the
 
 * ``value``: steps timed with CUDA events (synchronised on both sides), the
   packed matrix already resident in HBM (device-to-device load into the
-  operator, then run_halko).  The packed matrix (12.5 GB for c2) is far larger
+  operator, then run_halko).  The packed matrix (50 GB for c3) is far larger
   than L2, so no flush is needed between steps.
 * ``e2e``: the same through the C-ABI with host buffers: pinned host .bed body
   -> pcaone_gpu_load_bed (H2D inside the timed region) -> run_halko -> U, S, V
@@ -19,8 +19,13 @@ counts and allele frequencies -> window-based RSVD (winSVD, 7 epochs for the
   stream; ``executed_tflops`` counts the MMA work actually issued (three
   integer BF16 slices of the sketch, padded to a multiple of 16 columns).
   ``traffic`` is the DRAM bytes per launch of that kernel from an ncu capture
-  of a window of the same shape (workload c2p: the c2 window, 7,812 SNPs x
-  100,000 samples).
+  of a window of the same shape, where one exists.
+* ``accuracy`` (PLINK workloads): after the timed steps, the same workload
+  runs once in the FP64-grade form (six 9-bit slices: 54-bit operands, exact
+  integer accumulation; the GPU oracle) and once in the plain FP32 CUDA-core
+  form; the line reports each form's largest principal angle (sin) and
+  relative eigenvalue error against the oracle on the well-separated leading
+  PCs, and the FP32 form's time over ``value``.
 * EM workloads (``c4``: ``--emu``) report the EM iterations and, with
   ``--warm-start``, the learned start's statistics.
 * ``cpu_baseline`` / ``--impl reference``: the oracle (numpy/LAPACK restatement
@@ -123,17 +128,16 @@ class ClockSampler:
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# tensor-core window products on the c2 window shape (ncu capture B of
-# profiles/k_tc_window_c2p.md, workload c2p); the H launch includes reading and
-# clearing the int64 missing-entry sums
-NCU_TRAFFIC_C2_WINDOW = {"g": 253.4e6, "h": 296.9e6}
+# tensor-core window products, from one ncu capture of a window of the
+# workload's shape, keyed by (workload, product)
+NCU_TRAFFIC = {}
 
 
 def workload_params(name: str, precision: str):
     from pcaone_gb300 import capi, synthetic
     wl = synthetic.WORKLOADS[name]
     prec = {"fp32": capi.PREC_FP32, "bf16": capi.PREC_BF16, "bf16x3": capi.PREC_BF16X3,
-            "fp8": capi.PREC_FP8}[precision]
+            "fp8": capi.PREC_FP8, "fp64": capi.PREC_FP64}[precision]
     p = capi.default_params(svd=wl.get("svd", 2), k=wl["k"], oversamples=wl["p"], maxp=wl["maxp"],
                             bands=wl["bands"], perm=wl.get("perm", 1), standardize=0 if wl.get("dense") else 1,
                             precision=prec)
@@ -184,6 +188,45 @@ def cpu_sample_run(name: str):
     if wl.get("emu"):
         desc += "; one RSVD pass (EM iterations not included)"
     return t, t * scale, desc, cores
+
+
+def timed_call(fn):
+    """(seconds by CUDA events, result) of one call, synchronised on both sides."""
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    out = fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3, out
+
+
+def accuracy_block(args, params, step_with, outputs, t_dev):
+    """The measured form's errors, and the FP32 form's, against one run of the
+    FP64-grade form on the same resident matrix (same seed, same Omega, same
+    schedule); the FP32 form's time over the measured one."""
+    from pcaone_gb300 import accuracy as A
+    from pcaone_gb300 import capi
+    p64 = capi.Params.from_buffer_copy(params)
+    p64.precision = capi.PREC_FP64
+    t64, (Uo, So, Vo, _) = timed_call(lambda: step_with(p64))
+    U, S, V = outputs
+    errors = {args.precision: A.compare_pcs(U, S, V, Uo, So, Vo)}
+    out = {"oracle": "FP64-grade form: six 9-bit integer slices of the test matrix and of G (54 bits per column), "
+                     "exact integer accumulation in TMEM, FP64 slice combination and epilogues; same Omega and "
+                     "schedule", "oracle_s": t64,
+           "bars": {"sin_angle": 1e-6, "eig_relerr": 1e-8}, "errors": errors,
+           "S_oracle_top": [float(x) for x in So[:8]]}
+    if args.precision != "fp32":
+        p32 = capi.Params.from_buffer_copy(params)
+        p32.precision = capi.PREC_FP32
+        t32, (U32, S32, V32, _) = timed_call(lambda: step_with(p32))
+        errors["fp32"] = A.compare_pcs(U32, S32, V32, Uo, So, Vo)
+        out["fp32_form_s"] = t32
+        out["speedup_vs_fp32_form"] = t32 / t_dev
+    return out
 
 
 def dist_init():
@@ -328,9 +371,12 @@ def run_ours(args):
 
     em_iters = []
 
-    def step_device():
+    def step_device_with(p):
         ctx.load_bed_device(dev_src.data_ptr(), bps, M, N)
-        out = ctx.run_halko(params)
+        return ctx.run_halko(p)
+
+    def step_device():
+        out = step_device_with(params)
         em_iters.append(out[3])
         return out
 
@@ -389,10 +435,10 @@ def run_ours(args):
     peak = peaks.get("bf16_tflops", PEAKS_FALLBACK["bf16_tflops"])
     tc = args.precision != "fp32"
     LPtc = (L + 15) // 16 * 16
-    executed = achieved * (3 * LPtc / L) if tc else achieved
+    nslices = 6 if args.precision == "fp64" else 3
+    executed = achieved * (nslices * LPtc / L) if tc else achieved
     per_launch_s = ks["ms"] / 1e3 / max(1, ks["launches"])
-    c2_shape = args.workload in ("c2", "c2p")
-    traffic = NCU_TRAFFIC_C2_WINDOW[dom[0]] if (tc and c2_shape) else None
+    traffic = NCU_TRAFFIC.get((args.workload, dom[0])) if tc else None
     roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": traffic,
             "kernel": f"k_tc_{dom[0]}" if tc else f"k_window_{dom[0]}",
@@ -400,9 +446,14 @@ def run_ours(args):
             "hbm_gbs": (traffic / per_launch_s / 1e9) if traffic else None,
             "note": (f"{args.precision} form; {ks['launches']} launches, {ks['ms']:.1f} ms of "
                      f"{sum(times) * 1e3:.1f} ms; achieved = algorithmic 2*N*SNPs*L per launch / event time; "
-                     f"peak = {peak_kind} bf16 dense; traffic per launch from ncu (c2 window shape)")}
+                     f"peak = {peak_kind} bf16 dense; traffic per launch from ncu of the same window shape")}
     if not tc:
         roof["note"] += "; the FP32 form runs on CUDA cores, not the tensor pipe"
+
+    # ---- accuracy against the FP64-grade form; the FP32 CUDA-core form ----
+    accuracy = None
+    if rank == 0 and not args.no_accuracy and not wl.get("emu"):
+        accuracy = accuracy_block(args, params, step_device_with, (U, S, V), t_dev)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -428,6 +479,7 @@ def run_ours(args):
             "kernels": kstats,
             "host_s": host_phases,
             "pcs": {"S_top": [float(x) for x in S[:5]]},
+            "accuracy": accuracy,
         }
         if wl.get("emu"):
             line["em"] = {"iterations": em_iters[-1] if em_iters else None, "tolem": params.tolem,
@@ -444,9 +496,10 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2")
-    ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16", "bf16x3", "fp8"])
+    ap.add_argument("--workload", default="c3")
+    ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16", "bf16x3", "fp8", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64-grade and FP32 reference runs")
     ap.add_argument("--warm-start", action="store_true", help="learned EM warm start (EM workloads)")
     ap.add_argument("--maxiter", type=int, default=None, help="EM iteration cap (EM workloads)")
     args = ap.parse_args()

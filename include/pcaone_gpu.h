@@ -42,6 +42,12 @@ extern "C" {
                                  sparse term */
 #define PCAONE_PREC_FP8 2     /* reserved: FP8 e4m3 operands (not built yet) */
 #define PCAONE_PREC_BF16X3 3  /* same as PCAONE_PREC_BF16 */
+#define PCAONE_PREC_FP64 4    /* FP64-grade form for checking the other forms (no counterpart in the
+                                 reference): the tensor-core form with six slices (54 bits per column:
+                                 at least the FP64 significand relative to each column's maximum),
+                                 slices combined in FP64, CholeskyQR and the small SVD in plain FP64;
+                                 the missing-genotype terms keep 27-bit integers.  PLINK input,
+                                 k + oversamples <= 80 */
 
 /* SVD method (Param::svd_t, src/Cmd.hpp:14) */
 #define PCAONE_SVD_SINGLE 1   /* NormalRsvdOpData: single-pass RSVD, -d 1 */

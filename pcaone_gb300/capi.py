@@ -18,7 +18,7 @@ LIBPATH = os.path.join(HERE, "lib", "libpcaone_gb300.so")
 PCAONE_OK = 0
 ERRORS = {-1: "PCAONE_E_ARG", -2: "PCAONE_E_CUDA", -3: "PCAONE_E_NOMEM", -4: "PCAONE_E_FORMAT",
           -5: "PCAONE_E_NUMERIC", -6: "PCAONE_E_LIMIT"}
-PREC_FP32, PREC_BF16, PREC_FP8, PREC_BF16X3 = 0, 1, 2, 3
+PREC_FP32, PREC_BF16, PREC_FP8, PREC_BF16X3, PREC_FP64 = 0, 1, 2, 3, 4
 SVD_SINGLE, SVD_WINDOW = 1, 2
 MAX_L = 112
 

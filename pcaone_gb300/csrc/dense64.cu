@@ -10,7 +10,10 @@
 // which is far below the 24-bit integer slices the window products use.  The
 // (k+p)^2 Cholesky and inverse are latency-bound chains of square roots and
 // reciprocals and run in double-float too (dd.cuh); the Jacobi eigensolver,
-// the Householder sign rule and the small products stay in FP64.
+// the Householder sign rule and the small products stay in FP64.  The
+// FP64-grade form (the GPU oracle) runs these four kernels in plain FP64
+// arithmetic instead (template flag F64; the same shared-memory bytes hold one
+// double where the FP32-pair form keeps a float pair).
 //
 // Tall matrices (N x L, M x L) are row-major with leading dimension LP (the
 // sketch width padded to a multiple of 8; padding columns are zero).  Small
@@ -30,7 +33,7 @@ constexpr int kRowsTile = 32;
 // na x nb).  sym: A == B and only the upper triangle is formed (mirrored by the
 // reduction).  Row tiles are staged in shared memory as float pairs; each
 // thread accumulates Q entries in FP32 pairs.
-template <int Q>
+template <int Q, bool F64>
 __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict__ A, int lda, int na,
                                                        const double* __restrict__ B, int ldb, int nb, int64_t rows,
                                                        int64_t rows_per_block, int sym, double* __restrict__ part) {
@@ -39,6 +42,8 @@ __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict_
   float* Al = Ah + kRowsTile * na;
   float* Bh = Al + kRowsTile * na;       // kRowsTile x nb (not used when sym)
   float* Bl = Bh + kRowsTile * nb;
+  double* Ad = reinterpret_cast<double*>(smf);  // F64: the same bytes as doubles
+  double* Bd = Ad + kRowsTile * na;
   uint16_t* pi = reinterpret_cast<uint16_t*>(Bl + kRowsTile * nb);
   uint16_t* pj = pi + na * nb;
   const int tid = threadIdx.x;
@@ -62,32 +67,51 @@ __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict_
   const int64_t r0 = blockIdx.x * rows_per_block;
   const int64_t r1 = min(r0 + rows_per_block, rows);
   FloatPair acc[Q];
+  double accd[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) accd[q] = 0.0;
   __syncthreads();
   for (int64_t rt = r0; rt < r1; rt += kRowsTile) {
     const int nr = (int)min((int64_t)kRowsTile, r1 - rt);
     for (int e = tid; e < kRowsTile * na; e += blockDim.x) {
       const int r = e / na, c = e % na;
-      fp_split(r < nr ? A[(rt + r) * lda + c] : 0.0, Ah[e], Al[e]);
+      const double v = r < nr ? A[(rt + r) * lda + c] : 0.0;
+      if constexpr (F64)
+        Ad[e] = v;
+      else
+        fp_split(v, Ah[e], Al[e]);
     }
     if (!sym)
       for (int e = tid; e < kRowsTile * nb; e += blockDim.x) {
         const int r = e / nb, c = e % nb;
-        fp_split(r < nr ? B[(rt + r) * ldb + c] : 0.0, Bh[e], Bl[e]);
+        const double v = r < nr ? B[(rt + r) * ldb + c] : 0.0;
+        if constexpr (F64)
+          Bd[e] = v;
+        else
+          fp_split(v, Bh[e], Bl[e]);
       }
     __syncthreads();
-    const float* Th = sym ? Ah : Bh;
-    const float* Tl = sym ? Al : Bl;
     const int ldt = sym ? na : nb;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int e = tid + q * 256;
       if (e < nent) {
         const int i = pi[e], j = pj[e];
-        FloatPair s = acc[q];
+        if constexpr (F64) {
+          const double* Td = sym ? Ad : Bd;
+          double s = accd[q];
 #pragma unroll 8
-        for (int r = 0; r < kRowsTile; ++r)
-          fp_add_prod2(s, Ah[r * na + i], Al[r * na + i], Th[r * ldt + j], Tl[r * ldt + j]);
-        acc[q] = s;
+          for (int r = 0; r < kRowsTile; ++r) s = fma(Ad[r * na + i], Td[r * ldt + j], s);
+          accd[q] = s;
+        } else {
+          const float* Th = sym ? Ah : Bh;
+          const float* Tl = sym ? Al : Bl;
+          FloatPair s = acc[q];
+#pragma unroll 8
+          for (int r = 0; r < kRowsTile; ++r)
+            fp_add_prod2(s, Ah[r * na + i], Al[r * na + i], Th[r * ldt + j], Tl[r * ldt + j]);
+          acc[q] = s;
+        }
       }
     }
     __syncthreads();
@@ -96,7 +120,7 @@ __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict_
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int e = tid + q * 256;
-    if (e < nent) out[pi[e] * nb + pj[e]] = fp_value(acc[q]);
+    if (e < nent) out[pi[e] * nb + pj[e]] = F64 ? accd[q] : fp_value(acc[q]);
   }
 }
 
@@ -137,54 +161,73 @@ __global__ void k_zero(double* p, int64_t n) {
 // The padding block of R and Rinv is the identity.  status: 0 ok, 1
 // non-positive or non-finite pivot.
 constexpr int kCholThreads = 512;
-__device__ __forceinline__ void chol_pivot(const dd* a, int L, int k, dd* dg, dd* rdg, int* fail) {
-  const dd d = a[k * L + k];
-  const bool ok = d.hi > 0.f && isfinite(d.hi);
+// the arithmetic of the factor: double-float (dd) or, in the FP64-grade form,
+// FP64 (sqrt and division as CUDA provides them)
+__device__ __forceinline__ dd num_from(double v, dd*) { return dd_from_double(v); }
+__device__ __forceinline__ double num_from(double v, double*) { return v; }
+__device__ __forceinline__ double num_to_double(dd a) { return dd_to_double(a); }
+__device__ __forceinline__ double num_to_double(double a) { return a; }
+__device__ __forceinline__ dd num_mul(dd a, dd b) { return dd_mul(a, b); }
+__device__ __forceinline__ double num_mul(double a, double b) { return a * b; }
+__device__ __forceinline__ dd num_fms(dd c, dd a, dd b) { return dd_fms(c, a, b); }
+__device__ __forceinline__ double num_fms(double c, double a, double b) { return fma(-a, b, c); }
+__device__ __forceinline__ bool num_pos(dd d) { return d.hi > 0.f && isfinite(d.hi); }
+__device__ __forceinline__ bool num_pos(double d) { return d > 0.0 && isfinite(d); }
+__device__ __forceinline__ dd num_sqrt(dd a) { return dd_sqrt(a); }
+__device__ __forceinline__ double num_sqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ dd num_recip(dd a) { return dd_div(dd{1.f, 0.f}, a); }
+__device__ __forceinline__ double num_recip(double a) { return 1.0 / a; }
+
+template <class T>
+__device__ __forceinline__ void chol_pivot(const T* a, int L, int k, T* dg, T* rdg, int* fail) {
+  const T d = a[k * L + k];
+  const bool ok = num_pos(d);
   if (!ok) *fail = 1;
-  const dd dk = ok ? dd_sqrt(d) : dd{1.f, 0.f};
+  const T dk = ok ? num_sqrt(d) : num_from(1.0, (T*)nullptr);
   dg[k] = dk;
-  rdg[k] = dd_div(dd{1.f, 0.f}, dk);
+  rdg[k] = num_recip(dk);
 }
 
+template <class T>
 __global__ void __launch_bounds__(kCholThreads) k_chol_inv(const double* __restrict__ W, int L, int LP, double shift,
                                                            double* __restrict__ R, double* __restrict__ Rinv,
                                                            int* __restrict__ status) {
   extern __shared__ dd sdd[];  // L x L factor, L x L inverse, L roots, L reciprocals
-  dd* a = sdd;
-  dd* x = a + L * L;
-  dd* dg = x + L * L;
-  dd* rdg = dg + L;
+  T* a = reinterpret_cast<T*>(sdd);
+  T* x = a + L * L;
+  T* dg = x + L * L;
+  T* rdg = dg + L;
   __shared__ int fail;
   const int tid = threadIdx.x, nt = blockDim.x;
   if (tid == 0) fail = 0;
   for (int e = tid; e < L * L; e += nt) {
     const int i = e / L, j = e % L;
-    a[e] = dd_from_double(W[i * LP + j] + (i == j ? shift : 0.0));
-    x[e] = dd{i == j ? 1.f : 0.f, 0.f};
+    a[e] = num_from(W[i * LP + j] + (i == j ? shift : 0.0), (T*)nullptr);
+    x[e] = num_from(i == j ? 1.0 : 0.0, (T*)nullptr);
   }
   __syncthreads();
   if (tid == 0) chol_pivot(a, L, 0, dg, rdg, &fail);
   __syncthreads();
   for (int k = 0; k < L; ++k) {
-    const dd rk = rdg[k];
-    for (int j = k + 1 + tid; j < L; j += nt) a[k * L + j] = dd_mul(a[k * L + j], rk);
+    const T rk = rdg[k];
+    for (int j = k + 1 + tid; j < L; j += nt) a[k * L + j] = num_mul(a[k * L + j], rk);
     __syncthreads();
     const int m = L - k - 1;
     for (int e = tid; e < m * m; e += nt) {
       const int i = k + 1 + e / m, j = k + 1 + e % m;
-      if (j >= i) a[i * L + j] = dd_fms(a[i * L + j], a[k * L + i], a[k * L + j]);
+      if (j >= i) a[i * L + j] = num_fms(a[i * L + j], a[k * L + i], a[k * L + j]);
       if (e == 0) chol_pivot(a, L, k + 1, dg, rdg, &fail);  // element (k+1, k+1) is final now
     }
     __syncthreads();
   }
   for (int k = L - 1; k >= 0; --k) {
-    const dd rk = rdg[k];
-    for (int c = k + tid; c < L; c += nt) x[k * L + c] = dd_mul(x[k * L + c], rk);
+    const T rk = rdg[k];
+    for (int c = k + tid; c < L; c += nt) x[k * L + c] = num_mul(x[k * L + c], rk);
     __syncthreads();
     const int w = L - k;  // columns k .. L-1
     for (int e = tid; e < k * w; e += nt) {
       const int i = e / w, c = k + e % w;
-      x[i * L + c] = dd_fms(x[i * L + c], a[i * L + k], x[k * L + c]);
+      x[i * L + c] = num_fms(x[i * L + c], a[i * L + k], x[k * L + c]);
     }
     __syncthreads();
   }
@@ -192,8 +235,8 @@ __global__ void __launch_bounds__(kCholThreads) k_chol_inv(const double* __restr
     const int i = e / LP, j = e % LP;
     double v, w;
     if (i < L && j < L) {
-      v = j > i ? dd_to_double(a[i * L + j]) : (j == i ? dd_to_double(dg[i]) : 0.0);
-      w = j >= i ? dd_to_double(x[i * L + j]) : 0.0;
+      v = j > i ? num_to_double(a[i * L + j]) : (j == i ? num_to_double(dg[i]) : 0.0);
+      w = j >= i ? num_to_double(x[i * L + j]) : 0.0;
     } else {
       v = w = i == j ? 1.0 : 0.0;
     }
@@ -210,6 +253,7 @@ __global__ void __launch_bounds__(kCholThreads) k_chol_inv(const double* __restr
 // loads serves three or two products.  C may alias A (ldc == LP, n <= LP):
 // each CTA reads a row tile into shared memory before it writes the same rows.
 constexpr int kTallCols = 48;
+template <bool F64>
 __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows, int LP,
                                                    const double* __restrict__ B, int ldb, int n, double* C,
                                                    int ldc) {
@@ -220,10 +264,16 @@ __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows
   const int las = LP + 1;       // row stride of the A tile (odd: no bank conflicts between row pairs)
   float* Ah = Bl + LP * npd;    // 32 x las
   float* Al = Ah + kRowsTile * las;
+  double* Bd = reinterpret_cast<double*>(smf);  // F64: the same bytes as doubles
+  double* Ad = Bd + LP * npd;
   const int tid = threadIdx.x;
   for (int e = tid; e < LP * npd; e += blockDim.x) {
     const int t = e / npd, c = e % npd;
-    fp_split(c < n ? B[t * ldb + c] : 0.0, Bh[e], Bl[e]);
+    const double v = c < n ? B[t * ldb + c] : 0.0;
+    if constexpr (F64)
+      Bd[e] = v;
+    else
+      fp_split(v, Bh[e], Bl[e]);
   }
   const int r = 2 * (tid >> 4), cg = tid & 15;
   for (int64_t rt = (int64_t)blockIdx.x * kRowsTile; rt < rows; rt += (int64_t)gridDim.x * kRowsTile) {
@@ -231,24 +281,44 @@ __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows
     for (int e = tid; e < kRowsTile * LP; e += blockDim.x) {
       const int rr = e / LP, cc = e % LP;
       const int64_t row = rt + rr;
-      fp_split(row < rows ? A[row * LP + cc] : 0.0, Ah[rr * las + cc], Al[rr * las + cc]);
+      const double v = row < rows ? A[row * LP + cc] : 0.0;
+      if constexpr (F64)
+        Ad[rr * las + cc] = v;
+      else
+        fp_split(v, Ah[rr * las + cc], Al[rr * las + cc]);
     }
     __syncthreads();
     const int64_t row0 = rt + r;
     for (int c0 = 0; c0 < n; c0 += kTallCols) {
       FloatPair s[2][3];
-      const float* a0h = Ah + r * las;
-      const float* a0l = Al + r * las;
-      const float* bh = Bh + c0 + cg;
-      const float* bl = Bl + c0 + cg;
+      double sd[2][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+      if constexpr (F64) {
+        const double* a0 = Ad + r * las;
+        const double* b = Bd + c0 + cg;
 #pragma unroll 4
-      for (int t = 0; t < LP; ++t) {
-        const float x0h = a0h[t], x0l = a0l[t], x1h = a0h[las + t], x1l = a0l[las + t];
+        for (int t = 0; t < LP; ++t) {
+          const double x0 = a0[t], x1 = a0[las + t];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          const float yh = bh[t * npd + 16 * q], yl = bl[t * npd + 16 * q];
-          fp_add_prod2(s[0][q], x0h, x0l, yh, yl);
-          fp_add_prod2(s[1][q], x1h, x1l, yh, yl);
+          for (int q = 0; q < 3; ++q) {
+            const double y = b[t * npd + 16 * q];
+            sd[0][q] = fma(x0, y, sd[0][q]);
+            sd[1][q] = fma(x1, y, sd[1][q]);
+          }
+        }
+      } else {
+        const float* a0h = Ah + r * las;
+        const float* a0l = Al + r * las;
+        const float* bh = Bh + c0 + cg;
+        const float* bl = Bl + c0 + cg;
+#pragma unroll 4
+        for (int t = 0; t < LP; ++t) {
+          const float x0h = a0h[t], x0l = a0l[t], x1h = a0h[las + t], x1l = a0l[las + t];
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const float yh = bh[t * npd + 16 * q], yl = bl[t * npd + 16 * q];
+            fp_add_prod2(s[0][q], x0h, x0l, yh, yl);
+            fp_add_prod2(s[1][q], x1h, x1l, yh, yl);
+          }
         }
       }
 #pragma unroll
@@ -257,7 +327,7 @@ __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows
 #pragma unroll
           for (int q = 0; q < 3; ++q) {
             const int c = c0 + cg + 16 * q;
-            if (c < n) C[(row0 + h) * ldc + c] = fp_value(s[h][q]);
+            if (c < n) C[(row0 + h) * ldc + c] = F64 ? sd[h][q] : fp_value(s[h][q]);
           }
         }
       }
@@ -273,6 +343,7 @@ __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows
 // output accumulates the same FP32-pair terms in the same order as
 // k_gemm_tall: the skipped terms are exact zeros there.
 constexpr int kUpperMaxQ = 14;  // columns per warp: LP / 8 with LP <= 112
+template <bool F64>
 __global__ void __launch_bounds__(256) k_gemm_tall_upper(double* A, int64_t rows, int LP,
                                                          const double* __restrict__ B) {
   extern __shared__ float smf[];
@@ -281,8 +352,15 @@ __global__ void __launch_bounds__(256) k_gemm_tall_upper(double* A, int64_t rows
   float* Bl = Bh + LP * LP;
   float* Ah = Bl + LP * LP;  // 32 x las
   float* Al = Ah + kRowsTile * las;
+  double* Bd = reinterpret_cast<double*>(smf);  // F64: the same bytes as doubles
+  double* Ad = Bd + LP * LP;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int e = tid; e < LP * LP; e += blockDim.x) fp_split(B[e], Bh[e], Bl[e]);
+  for (int e = tid; e < LP * LP; e += blockDim.x) {
+    if constexpr (F64)
+      Bd[e] = B[e];
+    else
+      fp_split(B[e], Bh[e], Bl[e]);
+  }
   int cmax = -1;
 #pragma unroll
   for (int q = 0; q < kUpperMaxQ; ++q) {
@@ -294,18 +372,37 @@ __global__ void __launch_bounds__(256) k_gemm_tall_upper(double* A, int64_t rows
     for (int e = tid; e < kRowsTile * LP; e += blockDim.x) {
       const int rr = e / LP, cc = e % LP;
       const int64_t row = rt + rr;
-      fp_split(row < rows ? A[row * LP + cc] : 0.0, Ah[rr * las + cc], Al[rr * las + cc]);
+      const double v = row < rows ? A[row * LP + cc] : 0.0;
+      if constexpr (F64)
+        Ad[rr * las + cc] = v;
+      else
+        fp_split(v, Ah[rr * las + cc], Al[rr * las + cc]);
     }
     __syncthreads();
     FloatPair s[kUpperMaxQ];
-    const float* ah = Ah + lane * las;
-    const float* al = Al + lane * las;
-    for (int t = 0; t <= cmax; ++t) {
-      const float xh = ah[t], xl = al[t];
+    double sd[kUpperMaxQ];
 #pragma unroll
-      for (int q = 0; q < kUpperMaxQ; ++q) {
-        const int c = 16 * (q >> 1) + ((q & 1) ? 15 - warp : warp);
-        if (c < LP && t <= c) fp_add_prod2(s[q], xh, xl, Bh[t * LP + c], Bl[t * LP + c]);
+    for (int q = 0; q < kUpperMaxQ; ++q) sd[q] = 0.0;
+    if constexpr (F64) {
+      const double* ad = Ad + lane * las;
+      for (int t = 0; t <= cmax; ++t) {
+        const double x = ad[t];
+#pragma unroll
+        for (int q = 0; q < kUpperMaxQ; ++q) {
+          const int c = 16 * (q >> 1) + ((q & 1) ? 15 - warp : warp);
+          if (c < LP && t <= c) sd[q] = fma(x, Bd[t * LP + c], sd[q]);
+        }
+      }
+    } else {
+      const float* ah = Ah + lane * las;
+      const float* al = Al + lane * las;
+      for (int t = 0; t <= cmax; ++t) {
+        const float xh = ah[t], xl = al[t];
+#pragma unroll
+        for (int q = 0; q < kUpperMaxQ; ++q) {
+          const int c = 16 * (q >> 1) + ((q & 1) ? 15 - warp : warp);
+          if (c < LP && t <= c) fp_add_prod2(s[q], xh, xl, Bh[t * LP + c], Bl[t * LP + c]);
+        }
       }
     }
     const int64_t row = rt + lane;
@@ -313,7 +410,7 @@ __global__ void __launch_bounds__(256) k_gemm_tall_upper(double* A, int64_t rows
 #pragma unroll
       for (int q = 0; q < kUpperMaxQ; ++q) {
         const int c = 16 * (q >> 1) + ((q & 1) ? 15 - warp : warp);
-        if (c < LP) A[row * LP + c] = fp_value(s[q]);
+        if (c < LP) A[row * LP + c] = F64 ? sd[q] : fp_value(s[q]);
       }
     }
   }
@@ -701,19 +798,28 @@ size_t cross_smem(int na, int nb, int sym) {
   return 2 * sizeof(float) * kRowsTile * (na + nb) + 2 * sizeof(uint16_t) * na * nb + 64;
 }
 
-template <int Q>
-void launch_cross_q(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int64_t per,
-                    int sym, double* part, int nblocks, size_t smem, cudaStream_t s) {
+template <int Q, bool F64>
+void launch_cross_qf(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int64_t per,
+                     int sym, double* part, int nblocks, size_t smem, cudaStream_t s) {
   static bool attr_set = false;
   if (!attr_set) {
-    PCAONE_CUDA(cudaFuncSetAttribute(k_cross_partial<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    PCAONE_CUDA(
+        cudaFuncSetAttribute(k_cross_partial<Q, F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_set = true;
   }
-  k_cross_partial<Q><<<nblocks, 256, smem, s>>>(A, lda, na, B, ldb, nb, rows, per, sym, part);
+  k_cross_partial<Q, F64><<<nblocks, 256, smem, s>>>(A, lda, na, B, ldb, nb, rows, per, sym, part);
+}
+template <int Q>
+void launch_cross_q(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int64_t per,
+                    int sym, double* part, int nblocks, size_t smem, bool f64, cudaStream_t s) {
+  if (f64)
+    launch_cross_qf<Q, true>(A, lda, na, B, ldb, nb, rows, per, sym, part, nblocks, smem, s);
+  else
+    launch_cross_qf<Q, false>(A, lda, na, B, ldb, nb, rows, per, sym, part, nblocks, smem, s);
 }
 
 void launch_cross(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int sym,
-                  double* W, int ldw, double* part, int nblocks, cudaStream_t s) {
+                  double* W, int ldw, double* part, int nblocks, cudaStream_t s, bool f64) {
   if (na * nb > 64 * 256 || na > 0xffff) throw Error(-6, "cross product wider than 128 x 128");
   if (rows == 0) {
     k_zero<<<ceil_div((int64_t)na * ldw, 256), 256, 0, s>>>(W, (int64_t)na * ldw);
@@ -728,57 +834,85 @@ void launch_cross(const double* A, int lda, int na, const double* B, int ldb, in
   const double* Bv = sym ? A : B;
   const int ldbv = sym ? lda : ldb;
   if (q <= 4)
-    launch_cross_q<4>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, s);
+    launch_cross_q<4>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s);
   else if (q <= 8)
-    launch_cross_q<8>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, s);
+    launch_cross_q<8>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s);
   else if (q <= 16)
-    launch_cross_q<16>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, s);
+    launch_cross_q<16>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s);
   else if (q <= 32)
-    launch_cross_q<32>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, s);
+    launch_cross_q<32>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s);
   else
-    launch_cross_q<64>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, s);
+    launch_cross_q<64>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s);
   PCAONE_LAUNCH_CHECK();
   k_cross_reduce<<<ceil_div((int64_t)na * nb * 32, 256), 256, 0, s>>>(part, nblocks, na, nb, sym, W, ldw);
   PCAONE_LAUNCH_CHECK();
 }
 
-void launch_chol_inv_shift(const double* W, int L, int LP, double shift, double* R, double* Rinv, int* status,
-                           cudaStream_t s) {
+template <class T>
+void launch_chol_t(const double* W, int L, int LP, double shift, double* R, double* Rinv, int* status,
+                   cudaStream_t s) {
   static bool attr_set = false;
   if (!attr_set) {
-    PCAONE_CUDA(cudaFuncSetAttribute(k_chol_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    PCAONE_CUDA(cudaFuncSetAttribute(k_chol_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_set = true;
   }
-  k_chol_inv<<<1, kCholThreads, sizeof(dd) * (2 * L * L + 2 * L), s>>>(W, L, LP, shift, R, Rinv, status);
+  static_assert(sizeof(T) == sizeof(dd), "factor element size");
+  k_chol_inv<T><<<1, kCholThreads, sizeof(T) * (2 * L * L + 2 * L), s>>>(W, L, LP, shift, R, Rinv, status);
+}
+
+void launch_chol_inv_shift(const double* W, int L, int LP, double shift, double* R, double* Rinv, int* status,
+                           cudaStream_t s, bool f64) {
+  if (f64)
+    launch_chol_t<double>(W, L, LP, shift, R, Rinv, status, s);
+  else
+    launch_chol_t<dd>(W, L, LP, shift, R, Rinv, status, s);
   PCAONE_LAUNCH_CHECK();
 }
 
-void launch_gemm_tall(const double* A, int64_t rows, int LP, const double* B, int ldb, int n, double* C, int ldc,
-                      cudaStream_t s) {
-  if (rows == 0) return;
+template <bool F64>
+void launch_gemm_tall_t(const double* A, int64_t rows, int LP, const double* B, int ldb, int n, double* C, int ldc,
+                        cudaStream_t s) {
   static bool attr_set = false;
   if (!attr_set) {
-    PCAONE_CUDA(cudaFuncSetAttribute(k_gemm_tall, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    PCAONE_CUDA(cudaFuncSetAttribute(k_gemm_tall<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_set = true;
   }
   const size_t npd = (size_t)(n + kTallCols - 1) / kTallCols * kTallCols;
   const size_t smem = 2 * sizeof(float) * ((size_t)LP * npd + (size_t)kRowsTile * (LP + 1));
   const int grid = (int)std::min<int64_t>((rows + kRowsTile - 1) / kRowsTile, 152 * 8);
-  k_gemm_tall<<<grid, 256, smem, s>>>(A, rows, LP, B, ldb, n, C, ldc);
+  k_gemm_tall<F64><<<grid, 256, smem, s>>>(A, rows, LP, B, ldb, n, C, ldc);
+}
+
+void launch_gemm_tall(const double* A, int64_t rows, int LP, const double* B, int ldb, int n, double* C, int ldc,
+                      cudaStream_t s, bool f64) {
+  if (rows == 0) return;
+  if (f64)
+    launch_gemm_tall_t<true>(A, rows, LP, B, ldb, n, C, ldc, s);
+  else
+    launch_gemm_tall_t<false>(A, rows, LP, B, ldb, n, C, ldc, s);
   PCAONE_LAUNCH_CHECK();
 }
 
-void launch_gemm_tall_upper(double* A, int64_t rows, int LP, const double* B, cudaStream_t s) {
-  if (rows == 0) return;
-  if (LP % 8 != 0 || LP > 8 * kUpperMaxQ) throw Error(-6, "triangular tall product: width must be a multiple of 8, at most 112");
+template <bool F64>
+void launch_gemm_tall_upper_t(double* A, int64_t rows, int LP, const double* B, cudaStream_t s) {
   static bool attr_set = false;
   if (!attr_set) {
-    PCAONE_CUDA(cudaFuncSetAttribute(k_gemm_tall_upper, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    PCAONE_CUDA(
+        cudaFuncSetAttribute(k_gemm_tall_upper<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_set = true;
   }
   const size_t smem = 2 * sizeof(float) * ((size_t)LP * LP + (size_t)kRowsTile * (LP + 1));
   const int grid = (int)std::min<int64_t>((rows + kRowsTile - 1) / kRowsTile, 152 * 8);
-  k_gemm_tall_upper<<<grid, 256, smem, s>>>(A, rows, LP, B);
+  k_gemm_tall_upper<F64><<<grid, 256, smem, s>>>(A, rows, LP, B);
+}
+
+void launch_gemm_tall_upper(double* A, int64_t rows, int LP, const double* B, cudaStream_t s, bool f64) {
+  if (rows == 0) return;
+  if (LP % 8 != 0 || LP > 8 * kUpperMaxQ) throw Error(-6, "triangular tall product: width must be a multiple of 8, at most 112");
+  if (f64)
+    launch_gemm_tall_upper_t<true>(A, rows, LP, B, s);
+  else
+    launch_gemm_tall_upper_t<false>(A, rows, LP, B, s);
   PCAONE_LAUNCH_CHECK();
 }
 

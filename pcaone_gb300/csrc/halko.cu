@@ -156,6 +156,8 @@ struct Context {
   CUtensorMap map_bed_g{}, map_bed_h{}, map_w{}, map_gt{};
   int ldg = 0, win_max = 0;
   int nslice_cur = 1, w_slices = 0;
+  int max_slices = 3;  // slices of the chosen form: 3, or 6 in the FP64-grade form
+  bool fp64 = false;   // FP64-grade form: the QR and small-SVD kernels in plain FP64 too
 
   // optional per-kernel CUDA-event timing of the window products
   // (pcaone_gpu_set_profiling): class 0 = G product, 1 = H product
@@ -399,8 +401,9 @@ static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
       need_hpart = std::max(need_hpart, (size_t)nsp * c.npad * LP);
     }
   }
-  c.wsl.ensure((size_t)3 * LP * c.npad, c.stream);
-  c.gt.ensure((size_t)3 * LP * c.ldg, c.stream);
+  const int smax = c.max_slices;
+  c.wsl.ensure((size_t)smax * LP * c.npad, c.stream);
+  c.gt.ensure((size_t)smax * LP * c.ldg, c.stream);
   c.colsum.ensure(LP, c.stream);
   c.cvec.ensure(LP, c.stream);
   c.cpart.ensure((size_t)win * LP, c.stream, false);
@@ -409,13 +412,13 @@ static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
   c.wint.ensure((size_t)c.npad * LP, c.stream, false);
   c.ghint.ensure((size_t)win * LP, c.stream, false);
   c.gmint.ensure((size_t)win * LP, c.stream, false);
-  c.gmunit.ensure((size_t)3 * LP, c.stream);
+  c.gmunit.ensure((size_t)smax * LP, c.stream);
   c.gisum.ensure((size_t)win * LP, c.stream, true);
   c.gesum.ensure((size_t)win * LP, c.stream, true);
   c.hisum.ensure((size_t)c.npad * LP, c.stream, true);
   c.hesum.ensure((size_t)c.npad * LP, c.stream, true);
-  c.wunit.ensure((size_t)3 * LP, c.stream);
-  c.hunit.ensure((size_t)3 * LP, c.stream);
+  c.wunit.ensure((size_t)smax * LP, c.stream);
+  c.hunit.ensure((size_t)smax * LP, c.stream);
   c.wexp.ensure(LP, c.stream);
   c.hexp.ensure(LP, c.stream);
   c.err.ensure(1, c.stream);
@@ -426,8 +429,8 @@ static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
   c.bed_work = c.bed.p;
   tc_make_bed_maps(c);
   const int sl = c.dense ? tc::kMapF16 : tc::kMapBF16;  // slice digits: FP16 for dense input, else BF16
-  tc::make_map_2d(&c.map_w, c.wsl.p, sl, (uint64_t)c.npad, (uint64_t)3 * LP, (uint64_t)c.npad * 2, 64, LP, true);
-  tc::make_map_2d(&c.map_gt, c.gt.p, sl, (uint64_t)c.ldg, (uint64_t)3 * LP, (uint64_t)c.ldg * 2, 64, LP, true);
+  tc::make_map_2d(&c.map_w, c.wsl.p, sl, (uint64_t)c.npad, (uint64_t)smax * LP, (uint64_t)c.npad * 2, 64, LP, true);
+  tc::make_map_2d(&c.map_gt, c.gt.p, sl, (uint64_t)c.ldg, (uint64_t)smax * LP, (uint64_t)c.ldg * 2, 64, LP, true);
   c.w_slices = 0;
 }
 
@@ -440,15 +443,20 @@ static void op_init(Context& c, const pcaone_gpu_params& p) {
   if (p.svd != PCAONE_SVD_SINGLE && p.svd != PCAONE_SVD_WINDOW) throw Error(PCAONE_E_ARG, "svd must be 1 or 2");
   if (p.svd == PCAONE_SVD_WINDOW && (p.bands < 4 || (p.bands & (p.bands - 1)) != 0))
     throw Error(PCAONE_E_ARG, "the -w/--batches must be a power of 2 and the minimun is 4.");
-  if (p.precision != PCAONE_PREC_FP32 && p.precision != PCAONE_PREC_BF16 && p.precision != PCAONE_PREC_BF16X3)
+  if (p.precision != PCAONE_PREC_FP32 && p.precision != PCAONE_PREC_BF16 && p.precision != PCAONE_PREC_BF16X3 &&
+      p.precision != PCAONE_PREC_FP64)
     throw Error(PCAONE_E_ARG, "precision form not available in this build of the operator");
   if (c.dense && p.precision == PCAONE_PREC_FP32)
     throw Error(PCAONE_E_ARG, "dense (FileBinary) input runs in the tensor-core form only");
+  if (c.dense && p.precision == PCAONE_PREC_FP64)
+    throw Error(PCAONE_E_ARG, "the FP64-grade form takes PLINK genotypes (its products are exact only for integer dosages)");
   if (c.dense && p.emu) throw Error(PCAONE_E_ARG, "EM imputation needs PLINK input (no missing genotypes in dense input)");
   c.P = p;
   c.k = p.k;
   c.L = L;
   c.tc = p.precision != PCAONE_PREC_FP32;
+  c.max_slices = p.precision == PCAONE_PREC_FP64 ? tc::kMaxSlices : tc::kIntSlices;
+  c.fp64 = p.precision == PCAONE_PREC_FP64;
   c.LP = c.tc ? round_up(L, 16) : round_up(L, 8);
   c.update = c.standardize = c.scaled = c.fitted = false;
   c.have_usv = false;
@@ -508,7 +516,9 @@ static void op_init(Context& c, const pcaone_gpu_params& p) {
     ensure_missing_total(c);
     // TMEM per CTA: one accumulator per slice (3 x LP columns) plus at least
     // one 32-column stage of the A operand (LP <= 112 always fits)
-    if (3 * c.LP + 32 > 512) throw Error(PCAONE_E_LIMIT, "tensor-core form: k + oversamples too large for TMEM");
+    if (c.max_slices * c.LP + 32 > 512)
+      throw Error(PCAONE_E_LIMIT, c.max_slices > 3 ? "FP64-grade form: k + oversamples above 80 do not fit in TMEM"
+                                                   : "tensor-core form: k + oversamples too large for TMEM");
     tc_setup(c, (int)std::max<int64_t>(1, win), lens);
   }
   upload_omega0(c);
@@ -559,8 +569,8 @@ static int read_status(Context& c) {
 static void cholqr(Context& c, double* A, int64_t rows, bool need_r) {
   const int L = c.L, LP = c.LP;
   const int nb = cross_blocks(rows);
-  launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream);
-  launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R1.p, c.R1i.p, c.status.p, c.stream);
+  launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream, c.fp64);
+  launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R1.p, c.R1i.p, c.status.p, c.stream, c.fp64);
   bool shifted = false;
   if (read_status(c) != 0) {
     // shift = 11 (m n + n (n + 1)) u ||A||_F^2
@@ -569,24 +579,24 @@ static void cholqr(Context& c, double* A, int64_t rows, bool need_r) {
     double tr = 0;
     for (int i = 0; i < L; ++i) tr += w[(size_t)i * LP + i];
     const double shift = 11.0 * ((double)rows * L + (double)L * (L + 1)) * 1.1102230246251565e-16 * tr;
-    launch_chol_inv_shift(c.W.p, L, LP, shift, c.R1.p, c.R1i.p, c.status.p, c.stream);
+    launch_chol_inv_shift(c.W.p, L, LP, shift, c.R1.p, c.R1i.p, c.status.p, c.stream, c.fp64);
     if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: Gram matrix not positive definite");
     shifted = true;
   }
-  launch_gemm_tall_upper(A, rows, LP, c.R1i.p, c.stream);
-  launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream);
-  launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R2.p, c.R2i.p, c.status.p, c.stream);
+  launch_gemm_tall_upper(A, rows, LP, c.R1i.p, c.stream, c.fp64);
+  launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream, c.fp64);
+  launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R2.p, c.R2i.p, c.status.p, c.stream, c.fp64);
   if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: second Gram not positive definite");
-  launch_gemm_tall_upper(A, rows, LP, c.R2i.p, c.stream);
+  launch_gemm_tall_upper(A, rows, LP, c.R2i.p, c.stream, c.fp64);
   if (need_r) {
     launch_mult_small(c.R2.p, c.R1.p, c.Rt.p, LP, c.stream);     // R = R2 R1
     launch_mult_small(c.R1i.p, c.R2i.p, c.Rti.p, LP, c.stream);  // R^-1 = R1^-1 R2^-1
   }
   if (shifted) {
-    launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream);
-    launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R3.p, c.R3i.p, c.status.p, c.stream);
+    launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream, c.fp64);
+    launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R3.p, c.R3i.p, c.status.p, c.stream, c.fp64);
     if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: third Gram not positive definite");
-    launch_gemm_tall_upper(A, rows, LP, c.R3i.p, c.stream);
+    launch_gemm_tall_upper(A, rows, LP, c.R3i.p, c.stream, c.fp64);
     if (need_r) {
       launch_mult_small(c.R3.p, c.Rt.p, c.R1.p, LP, c.stream);
       launch_mult_small(c.Rti.p, c.R3i.p, c.R1i.p, LP, c.stream);
@@ -833,7 +843,8 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   fa.F = c.F.p;
   fa.scale = c.scale.p;
   fa.perm = perm;
-  fa.wunit_m = c.wunit.p + (size_t)(S - 1) * LP;
+  fa.wunit_m = c.wunit.p + (size_t)(std::min(S, tc::kIntSlices) - 1) * LP;
+  fa.wunit_p = c.wunit.p + (size_t)(S - 1) * LP;
   fa.gisum = any_miss ? c.gisum.p : nullptr;
   fa.gesum = (any_miss && em) ? c.gesum.p : nullptr;
   fa.G = c.G.p;
@@ -890,7 +901,9 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   hf.hpart = c.thpart.p;
   hf.c = c.cvec.p;
   hf.Hx = Hx;
-  hf.hunit_m = c.hunit.p + (size_t)(S - 1) * LP;
+  hf.nslice = S;
+  hf.hunit_m = c.hunit.p + (size_t)(std::min(S, tc::kIntSlices) - 1) * LP;
+  hf.hunit_p = c.hunit.p + (size_t)(S - 1) * LP;
   hf.hisum = any_miss ? c.hisum.p : nullptr;
   hf.hesum = (any_miss && em) ? c.hesum.p : nullptr;
   tc::launch_h_finish(hf, c.stream);
@@ -982,13 +995,11 @@ static void compute_g_and_h_window(Context& c, int pi) {
   }
 }
 
-// integer slices of the tensor-core form: three (24 bits per column) in every
-// epoch.  Fewer slices in the range-finding epochs were measured to move the
-// converged PCs by up to 3e-4 (principal angle) on a five-population sample.
+// integer slices of the tensor-core forms in every epoch: three (27 bits per
+// column), or six (54 bits) in the FP64-grade form
 static int slices_for_epoch(const Context& c, int pi) {
-  (void)c;
   (void)pi;
-  return 3;
+  return c.max_slices;
 }
 
 static void check_tc_err(Context& c) {
@@ -1023,10 +1034,10 @@ static int compute_usv(Context& c, int p, double tol) {
     c.t_prod += secs(t0, t1);
     ++epochs;
     cholqr(c, c.G.p, M, true);  // G <- Q2, Rt = R2 R1
-    launch_cross(c.H.p, LP, L, c.H.p, LP, L, N, 1, c.W.p, LP, c.red.p, cross_blocks(N), c.stream);
+    launch_cross(c.H.p, LP, L, c.H.p, LP, L, N, 1, c.W.p, LP, c.red.p, cross_blocks(N), c.stream, c.fp64);
     launch_usv_small(c.Rti.p, c.W.p, L, LP, k, c.UB.p, c.sigma.p, c.T.p, c.tmp.p, c.status.p + 1, c.stream);
     // Ucur = H T (right singular vectors of B = R^{-T} H^T)
-    launch_gemm_tall(c.H.p, N, LP, c.T.p, k, k, c.U.p, k, c.stream);
+    launch_gemm_tall(c.H.p, N, LP, c.T.p, k, k, c.U.p, k, c.stream, c.fp64);
     // Upre <- Ucur only where the reference assigns it (Halko.cpp:84-94); the
     // winSVD minimum-epoch branch keeps the older Upre.
     bool set_upre = pi == 0;
@@ -1041,7 +1052,7 @@ static int compute_usv(Context& c, int p, double tol) {
         if (c.P.svd == PCAONE_SVD_WINDOW && std::ldexp(1.0, pi) < c.P.bands) {
           p = (int)std::log2((double)c.P.bands);
         } else {
-          launch_gemm_tall(c.G.p, M, LP, c.UB.p, LP, k, c.V.p, k, c.stream);  // V = Q2 U_B[:, :k]
+          launch_gemm_tall(c.G.p, M, LP, c.UB.p, LP, k, c.V.p, k, c.stream, c.fp64);  // V = Q2 U_B[:, :k]
           done = true;
         }
       } else {

@@ -165,16 +165,18 @@ void launch_window_h_finish(const WindowArgs& a, const float* hpart, int nsplit,
 int cross_blocks(int64_t rows);
 size_t cross_smem(int na, int nb, int sym);
 // W[i][j] (ld ldw) = sum_r A[r][i] * B[r][j], i < na, j < nb; sym: B = A
+// f64 (here and below): plain FP64 arithmetic instead of FP32 pairs (the
+// FP64-grade form)
 void launch_cross(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int sym,
-                  double* W, int ldw, double* part, int nblocks, cudaStream_t s);
+                  double* W, int ldw, double* part, int nblocks, cudaStream_t s, bool f64 = false);
 // Cholesky of W + shift*I (leading L block) -> R (upper), Rinv; padding = identity
 void launch_chol_inv_shift(const double* W, int L, int LP, double shift, double* R, double* Rinv, int* status,
-                           cudaStream_t s);
+                           cudaStream_t s, bool f64 = false);
 // C (rows x n, ld ldc) = A (rows x LP) * B (LP x n, ld ldb); C may alias A
 void launch_gemm_tall(const double* A, int64_t rows, int LP, const double* B, int ldb, int n, double* C, int ldc,
-                      cudaStream_t s);
+                      cudaStream_t s, bool f64 = false);
 // A <- A * B in place for B upper triangular (LP x LP, LP a multiple of 8)
-void launch_gemm_tall_upper(double* A, int64_t rows, int LP, const double* B, cudaStream_t s);
+void launch_gemm_tall_upper(double* A, int64_t rows, int LP, const double* B, cudaStream_t s, bool f64 = false);
 // Q columns times the signs an Eigen / LAPACK Householder QR gives
 void launch_house_signs(double* Q, int64_t rows, int L, int LP, double* sgn, cudaStream_t s);
 int flip_blocks(int64_t rows);

@@ -389,6 +389,30 @@ __device__ __forceinline__ void store_slice_sum(uint32_t lane_base, int c0, int 
     for (int t = 0; t < 8; ++t) sum[t] = fmaf(unit[s * LP + c0 + t], v[t], sum[t]);
   }
 }
+// More than kIntSlices slices (the 54-bit form): the leading three and the
+// remaining slices each combine exactly in int64 (below 2^42), then
+// P = hi * 512^(S-3) + lo in FP64 (one rounding)
+__device__ __forceinline__ void combine_slices_fp64(uint32_t lane_base, int c0, int LP, int S, double* out) {
+  float v[8];
+  long long hi[8] = {0, 0, 0, 0, 0, 0, 0, 0}, lo[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int s = 0; s < S; ++s) {
+    tmem_ld8(lane_base + s * LP + c0, v);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      if (s < kIntSlices)
+        hi[t] = hi[t] * (1 << kDigitBits) + __float2ll_rn(v[t]);
+      else
+        lo[t] = lo[t] * (1 << kDigitBits) + __float2ll_rn(v[t]);
+    }
+  }
+  const double sh = exp2i(kDigitBits * (S - kIntSlices));
+#pragma unroll
+  for (int t = 0; t < 8; ++t) out[t] = fma((double)hi[t], sh, (double)lo[t]);
+}
+__device__ __forceinline__ void store_f64x8(double* dst, const double* v) {
+#pragma unroll
+  for (int t = 0; t < 8; t += 2) *reinterpret_cast<double2*>(dst + t) = make_double2(v[t], v[t + 1]);
+}
 __device__ __forceinline__ void store_f32x8(float* dst, const float* v) {
   *reinterpret_cast<float4*>(dst) = make_float4(v[0], v[1], v[2], v[3]);
   *reinterpret_cast<float4*>(dst + 4) = make_float4(v[4], v[5], v[6], v[7]);
@@ -557,10 +581,16 @@ __global__ void __launch_bounds__(kThreads, 2)
         } else {
           // genotypes: every slice sum is an integer below 2^23, combined
           // exactly in int64 in units of the last slice
-          long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-          if (ok) combine_slices_exact(lane_base, c0, LP, S, acc);
-          if (j < a.nsnp)
-            store_i64x8(reinterpret_cast<long long*>(a.part) + ((size_t)blockIdx.y * a.nsnp + j) * LP + c0, acc);
+          const size_t off = ((size_t)blockIdx.y * a.nsnp + j) * LP + c0;
+          if (S <= kIntSlices) {
+            long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (ok) combine_slices_exact(lane_base, c0, LP, S, acc);
+            if (j < a.nsnp) store_i64x8(reinterpret_cast<long long*>(a.part) + off, acc);
+          } else {
+            double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (ok) combine_slices_fp64(lane_base, c0, LP, S, acc);
+            if (j < a.nsnp) store_f64x8(reinterpret_cast<double*>(a.part) + off, acc);
+          }
         }
       }
     }
@@ -727,9 +757,15 @@ __global__ void __launch_bounds__(kThreads, 2)
           if (ok) store_slice_sum(lane_base, c0, LP, S, unit, sum);
           store_f32x8(reinterpret_cast<float*>(a.hpart) + row * LP + c0, sum);
         } else {
-          long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-          if (ok) combine_slices_exact(lane_base, c0, LP, S, acc);
-          store_i64x8(reinterpret_cast<long long*>(a.hpart) + row * LP + c0, acc);
+          if (S <= kIntSlices) {
+            long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (ok) combine_slices_exact(lane_base, c0, LP, S, acc);
+            store_i64x8(reinterpret_cast<long long*>(a.hpart) + row * LP + c0, acc);
+          } else {
+            double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (ok) combine_slices_fp64(lane_base, c0, LP, S, acc);
+            store_f64x8(reinterpret_cast<double*>(a.hpart) + row * LP + c0, acc);
+          }
         }
       }
     }
@@ -808,41 +844,43 @@ __global__ void __launch_bounds__(256) k_colred(const double* __restrict__ A, in
   if (tid == 0) *cnt = 0u;
 }
 
-// Split v (|v| < 2^E) into S integer slices: m = rint(v * 2^(9S-1-E)) has
-// |m| <= 2^(9S-1), and its balanced base-512 digits w_s (m = sum_s w_s
-// 512^(S-1-s), |w_s| <= 256, exact in BF16) are the slices, with units
-// u_s = 2^(E-8-9s).  Returns the represented value m * u_(S-1).  Integer
-// digit arithmetic keeps the FP64 work to one multiply and one conversion.
-// The digits are stored as BF16 or (f16) FP16 bit patterns, exact in both.
-// *m_out (optional) receives m.
+// Split v (|v| < 2^E) into S integer slices (S <= kMaxSlices): m = rint(v *
+// 2^(9S-1-E)) has |m| <= 2^(9S-1) (at most 2^53: exact in FP64), and its
+// balanced base-512 digits w_s (m = sum_s w_s 512^(S-1-s), |w_s| <= 256, exact
+// in BF16) are the slices, with units u_s = 2^(E-8-9s).  Returns the
+// represented value m * u_(S-1).  Integer digit arithmetic keeps the FP64 work
+// to one multiply and one conversion.  The digits are stored as BF16 or (f16)
+// FP16 bit patterns, exact in both.  *m_out (optional) receives the integer
+// the sparse terms use: m itself for S <= kIntSlices, else the rounding of v
+// to kIntSlices slices (27 bits; unit u_(kIntSlices-1)).
 __device__ __forceinline__ uint16_t digit_bits(int w, bool f16) {
   return f16 ? __half_as_ushort(__int2half_rn(w)) : __bfloat16_as_ushort(__float2bfloat16_rn((float)w));
 }
 __device__ __forceinline__ double split_store(double v, int E, int S, uint16_t* dst, size_t slice_stride, bool f16,
                                               int* m_out = nullptr) {
-  constexpr int kBase = 1 << kDigitBits, kHalf = kBase / 2;
-  const int m = __double2int_rn(v * exp2i(kDigitBits * S - 1 - E));
-  if (m_out) *m_out = m;
-  int rest = m;
+  constexpr long long kBase = 1 << kDigitBits, kHalf = kBase / 2;
+  const long long m = __double2ll_rn(v * exp2i(kDigitBits * S - 1 - E));
+  if (m_out) *m_out = S <= kIntSlices ? (int)m : __double2int_rn(v * exp2i(kDigitBits * kIntSlices - 1 - E));
+  long long rest = m;
   for (int s = S - 1; s > 0; --s) {
-    const int w = ((rest + kHalf) & (kBase - 1)) - kHalf;
-    dst[(size_t)s * slice_stride] = digit_bits(w, f16);
+    const long long w = ((rest + kHalf) & (kBase - 1)) - kHalf;
+    dst[(size_t)s * slice_stride] = digit_bits((int)w, f16);
     rest = (rest - w) / kBase;  // exact: rest - w is a multiple of the base
   }
-  dst[0] = digit_bits(rest, f16);
+  dst[0] = digit_bits((int)rest, f16);
   return (double)m * exp2i(E - kDigitBits * S + 1);
 }
 
 // W slices of Omega (S*LP rows x npad, K-major) and the represented W, in FP64
-// and as the integer m (|m| <= 2^26; the value is m times the last slice unit).
-// A block takes 64 rows of Omega (coalesced reads, and coalesced writes of the
+// and as the integer of the sparse terms (|m| <= 2^26, see split_store).
+// A block takes 32 rows of Omega (coalesced reads, and coalesced writes of the
 // represented values), keeps their digits in shared memory and writes each
-// slice row's 64 digits as one 128-byte run.  npad is a multiple of 64.
-constexpr int kOmgRows = 64;
+// slice row's 32 digits as one 64-byte run.  npad is a multiple of 32.
+constexpr int kOmgRows = 32;
 __global__ void __launch_bounds__(256) k_omega_slices(const double* __restrict__ omg, int npad, int N, int LP, int S,
                                                       const int* __restrict__ E, uint16_t* __restrict__ w,
                                                       double* __restrict__ rep, int32_t* __restrict__ wint, int f16) {
-  __shared__ uint16_t dg[3 * 112 * kOmgRows];  // [s][l][row]
+  __shared__ uint16_t dg[kMaxSlices * 112 * kOmgRows];  // [s][l][row]
   const int i0 = blockIdx.x * kOmgRows;
   for (int e = threadIdx.x; e < kOmgRows * LP; e += blockDim.x) {
     const int il = e / LP, l = e % LP;
@@ -898,13 +936,19 @@ __global__ void k_tc_g_finish(GFinishArgs a) {
         ph = t;
       }
       pd = (double)ph + (double)pl;
-    } else {
+    } else if (a.nslice <= kIntSlices) {
       // genotypes: exact int64 sum of the chunks' slice combinations (below
       // 2^53), one conversion, scaled by the last slice unit (a power of two)
       const long long* part = reinterpret_cast<const long long*>(a.part);
       long long ps = 0;
       for (int c = 0; c < a.nchunks; ++c) ps += part[((size_t)c * a.nsnp + j) * LP + l];
-      pd = (double)ps * a.wunit_m[l];
+      pd = (double)ps * a.wunit_p[l];
+    } else {
+      // the 54-bit form: FP64 chunk sums
+      const double* part = reinterpret_cast<const double*>(a.part);
+      double ps = 0.0;
+      for (int c = 0; c < a.nchunks; ++c) ps += part[((size_t)c * a.nsnp + j) * LP + l];
+      pd = ps * a.wunit_p[l];
     }
     double miss = 0.0;
     if (a.gisum) {
@@ -925,9 +969,11 @@ __global__ void k_tc_g_finish(GFinishArgs a) {
 // Gh slices (columns nsnp .. ldg-1 zeroed) with per-column exponents Eh, the
 // represented Gh as integers (ghint, for the EM term of H), and Gm = 2 f Gh
 // represented as an integer per entry (exponent Eh + 1: |Gm| <= 2 |Gh|; the
-// value is gmint * u'_l, u'_l the last slice unit) together with its terms of
-// c = sum_j Gm_j, so that the centring and missing-entry terms of H use the
-// same represented Gm.
+// value is gmint * u'_l, u'_l the unit of slice min(S, kIntSlices) - 1)
+// together with its terms of c = sum_j Gm_j, so that the centring and
+// missing-entry terms of H use the same represented Gm.  With more than
+// kIntSlices slices (the 54-bit form) c takes 2 f Gh at full precision
+// instead, and only the missing entries use the 27-bit Gm.
 __global__ void k_tc_gh_slices(GFinishArgs a, const int* __restrict__ Eh) {
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (idx >= (int64_t)a.ldg * a.LP) return;
@@ -947,10 +993,11 @@ __global__ void k_tc_gh_slices(GFinishArgs a, const int* __restrict__ Eh) {
       a.gmint[(size_t)j * LP + l] = 0;
       a.cpart[(size_t)j * LP + l] = a.F[snp] * ghq;
     } else {
-      const int e = Eh[l] + 1;
-      const int m = __double2int_rn(2.0 * a.F[snp] * ghq * exp2i(kDigitBits * S - 1 - e));
+      const int e = Eh[l] + 1, Si = min(S, kIntSlices);
+      const double gm = 2.0 * a.F[snp] * ghq;
+      const int m = __double2int_rn(gm * exp2i(kDigitBits * Si - 1 - e));
       a.gmint[(size_t)j * LP + l] = m;
-      a.cpart[(size_t)j * LP + l] = (double)m * exp2i(e - kDigitBits * S + 1);
+      a.cpart[(size_t)j * LP + l] = S > kIntSlices ? gm : (double)m * exp2i(e - kDigitBits * Si + 1);
     }
   } else {
     for (int s = 0; s < S; ++s) dh[s * sstride] = 0;
@@ -980,7 +1027,7 @@ __global__ void k_tc_h_finish(HFinishArgs a) {
     const float* hp = reinterpret_cast<const float*>(a.hpart);
     h = 0.0;
     for (int s = 0; s < a.nsplit; ++s) h += (double)hp[((size_t)s * a.npad + i) * LP + l];
-  } else {
+  } else if (a.nslice <= kIntSlices) {
     const long long* hp = reinterpret_cast<const long long*>(a.hpart);
     long long t = 0;
     for (int s = 0; s < a.nsplit; ++s) t += hp[((size_t)s * a.npad + i) * LP + l];
@@ -994,6 +1041,22 @@ __global__ void k_tc_h_finish(HFinishArgs a) {
       }
     }
     h = (double)t * (a.hunit_m[l] * (1.0 / 32768.0));
+  } else {
+    // the 54-bit form: FP64 split sums (units of the last slice) and the
+    // missing-entry sums of the 27-bit integers
+    const double* hp = reinterpret_cast<const double*>(a.hpart);
+    double t = 0.0;
+    for (int s = 0; s < a.nsplit; ++s) t += hp[((size_t)s * a.npad + i) * LP + l];
+    h = t * a.hunit_p[l];
+    if (a.hisum) {
+      double m = (double)(long long)a.hisum[idx] * 65536.0;
+      a.hisum[idx] = 0ull;
+      if (a.hesum) {
+        m += (double)(long long)a.hesum[idx];
+        a.hesum[idx] = 0ull;
+      }
+      h += m * (a.hunit_m[l] * (1.0 / 32768.0));
+    }
   }
   a.Hx[idx] += h - a.c[l];
 }
@@ -1181,7 +1244,7 @@ void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv
                          double* colsum, int* E, double* rep, int32_t* wint, bool f16, const ColRedScratch& cr,
                          cudaStream_t s) {
   launch_colred<true>(omg, N, LP, cr, nullptr, E, s);
-  if (npad % kOmgRows != 0 || S > 3 || LP > 112) throw Error(-6, "test-matrix slices: unsupported shape");
+  if (npad % kOmgRows != 0 || S > kMaxSlices || LP > 112) throw Error(-6, "test-matrix slices: unsupported shape");
   k_omega_slices<<<npad / kOmgRows, 256, 0, s>>>(omg, npad, N, LP, S, E, reinterpret_cast<uint16_t*>(w), rep, wint,
                                                  f16 ? 1 : 0);
   PCAONE_LAUNCH_CHECK();

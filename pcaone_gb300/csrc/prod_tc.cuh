@@ -21,7 +21,8 @@ struct GArgs {
   int nstages;            // pipeline depth
   int tmem_cols;          // TMEM columns allocated per CTA
   const double* wscale;   // S x LP units of the W slices (dense input)
-  void* part;             // [nchunks][nsnp][LP]: int64 slice combinations (genotypes) or FP32 sums (dense)
+  void* part;             // [nchunks][nsnp][LP]: int64 slice combinations (genotypes; FP64 beyond
+                          // kIntSlices slices) or FP32 sums (dense)
   int* err;               // set to 1 when a bounded wait gave up
   int dense;              // 1: FP16 values (FileBinary input) instead of packed codes
 };
@@ -40,7 +41,7 @@ struct HArgs {
   int nstages;
   int tmem_cols;
   const double* hscale;   // S x LP units of the Gh slices (dense input)
-  void* hpart;            // [nsplit][npad][LP]: int64 slice combinations (genotypes) or FP32 sums (dense)
+  void* hpart;            // [nsplit][npad][LP]: as GArgs::part
   int* err;
   int dense;              // 1: FP16 values instead of packed codes
 };
@@ -48,10 +49,12 @@ struct HArgs {
 // H rows of one window: Hx += sum of the split partials + missing-entry terms - c
 struct HFinishArgs {
   int nsamples, npad, L, LP, nsplit, dense;
+  int nslice;
   const void* hpart;          // as HArgs::hpart
   const double* c;            // LP centring terms
   double* Hx;
-  const double* hunit_m;      // per column unit of the Gh integers (the last slice unit)
+  const double* hunit_m;      // per column unit of the Gh integers of the sparse terms
+  const double* hunit_p;      // per column unit of the partials (the last slice unit)
   unsigned long long* hisum;  // npad x LP int64 sums of Gm over missing entries (nullptr: none), cleared
   unsigned long long* hesum;  // npad x LP int64 EM product sums (nullptr: no EM), cleared
 };
@@ -62,12 +65,14 @@ struct GFinishArgs {
   int nsnp;
   int L, LP, nslice, nchunks;
   int ldg;                       // columns of the Gh operand (window length rounded up to 64)
-  const void* part;              // chunk partials of D W (int64 for genotypes, FP32 for dense input)
+  const void* part;              // chunk partials of D W (int64 for genotypes; FP64 with more than
+                                 // kIntSlices slices; FP32 for dense input)
   const double* colsum;          // column sums of the sliced W
   const double* F;
   const double* scale;
   const int32_t* perm;
-  const double* wunit_m;         // per column unit of the integer W (the last slice unit)
+  const double* wunit_m;         // per column unit of the integer W of the sparse terms
+  const double* wunit_p;         // per column unit of the partials (the last slice unit)
   unsigned long long* gisum;     // nsnp x LP int64 sums over missing entries (nullptr: none), cleared
   unsigned long long* gesum;     // nsnp x LP int64 EM product sums (nullptr: no EM), cleared
   double* G;                     // nsnps x LP (FP64)
@@ -90,7 +95,13 @@ int stages_for(int LP, int nslice, int pbytes, bool dense);
 int tmem_cols_for(int ncols);
 int tmem_cols_needed(int LP, int nslice, int nstages, bool dense);
 // Slice digits: balanced base-512 integers, |w| <= 256, exact in BF16 and FP16.
+// Three slices (27 bits) in the tensor-core form, six (54 bits, at least the
+// FP64 significand relative to each column's maximum) in the FP64-grade form;
+// the integers of the sparse missing-entry terms always carry kIntSlices
+// slices (27 bits).
 constexpr int kDigitBits = 9;
+constexpr int kMaxSlices = 6;
+constexpr int kIntSlices = 3;
 // Exact accumulation: a product d*w of a genotype dosage (<= 2) and a slice
 // digit is at most 512 in magnitude, so a CTA that sums at most 2^14 K elements
 // keeps every FP32 accumulator an exactly represented integer (|v| <= 2^23).
