@@ -28,9 +28,12 @@ counts and allele frequencies -> window-based RSVD (winSVD, 7 epochs for the
   PCs, and the FP32 form's time over ``value``.
 * EM workloads (``c4``: ``--emu``) report the EM iterations and, with
   ``--warm-start``, the learned start's statistics.
-* ``cpu_baseline`` / ``--impl reference``: the oracle (numpy/LAPACK restatement
-  of the reference's Eigen/OpenMP path) on a bounded sample of the same
-  workload, scaled to the full workload by N*M.
+* ``cpu_baseline`` / ``--impl reference``: the reference's own CPU path (its
+  sources compiled for this host into oracle/_ref/ref_driver, OpenMP on every
+  host core) on two bounded samples of the same population model (REF_SAMPLES),
+  extrapolated to the whole workload linearly in N*M and labelled so; the
+  numpy/LAPACK restatement (oracle/) stands in when the reference cannot be
+  built on the host.
 
 Multi-GPU: the path is not sharded (replicas only); under torchrun each rank
 runs its own replica and the slowest rank's time is reported.
@@ -190,6 +193,156 @@ def cpu_sample_run(name: str):
     return t, t * scale, desc, cores
 
 
+# ---------------------------------------------------------------------------
+# The reference's own CPU path (oracle/_ref/ref_driver: the reference's sources
+# compiled for this host, driven like src/Halko.cpp:271-320) on bounded samples
+# of the workload's population model, with every host core.
+# ---------------------------------------------------------------------------
+# a half-size and a full-size sample: their times per genotype show the N*M
+# scaling that the extrapolation to the whole workload uses
+REF_SAMPLES = ({"nsamples": 8000, "nsnps": 25000}, {"nsamples": 8000, "nsnps": 50000})
+REF_DRIVER = os.path.join(REPO, "oracle", "_ref", "ref_driver")
+
+
+def host_cores() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+
+def cpu_model() -> str:
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+_gen_model = None
+
+
+def _gen_init(model):
+    global _gen_model
+    _gen_model = model
+
+
+def _gen_chunk(span):
+    from pcaone_gb300 import synthetic
+    lo, hi = span
+    return lo, synthetic.pack_codes(synthetic.sample_codes(_gen_model, lo, hi), False, _gen_model.seed + lo)
+
+
+def write_sample_plink(name: str, nsamples: int, nsnps: int, prefix: str) -> None:
+    """The workload's population model at nsamples x nsnps, drawn by the numpy
+    generator in a pool of host processes (chunks of 4096 SNPs, the same bytes
+    as synthetic.sample_packed_bed), written as a PLINK fileset."""
+    import multiprocessing as mp
+    from pcaone_gb300 import synthetic
+    model = synthetic.model_for(name, seed=1, nsamples=nsamples, nsnps=nsnps)
+    packed = np.empty((nsnps, synthetic.bytes_per_snp(nsamples)), dtype=np.uint8)
+    spans = [(lo, min(nsnps, lo + 4096)) for lo in range(0, nsnps, 4096)]
+    with mp.get_context("spawn").Pool(max(1, min(host_cores(), len(spans))), _gen_init, (model,)) as pool:
+        for lo, block in pool.imap_unordered(_gen_chunk, spans):
+            packed[lo:lo + block.shape[0]] = block
+    synthetic.write_plink(prefix, packed, nsamples)
+
+
+def ref_driver():
+    """oracle/_ref/ref_driver, built from the reference tree (PCAONE_REF_TREE) or
+    the staged copy in oracle/_ref/tree when missing; None if neither builds."""
+    if not os.path.exists(REF_DRIVER):
+        subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "ref", f"-j{host_cores()}"],
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    return REF_DRIVER if os.path.exists(REF_DRIVER) else None
+
+
+def ref_options(wl: dict) -> list:
+    """PCAone options of the workload (the driver keeps p as given)."""
+    opts = ["-d", str(wl.get("svd", 2)), "-k", str(wl["k"]), "--maxp", str(wl["maxp"]), "-w", str(wl["bands"]),
+            "--seed", "112", "--force-oversamples", str(wl["p"])]
+    if not wl.get("perm", 1):
+        opts.append("-S")
+    if wl.get("emu"):
+        opts += ["--emu", "--tol-em", str(wl.get("tolem", 1e-5)), "--maxiter", str(wl.get("maxiter", 100))]
+    return opts
+
+
+def ref_run(drv: str, prefix: str, outdir: str, wl: dict, threads: int) -> dict:
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    cmd = [drv, outdir, "--timing", "-b", prefix] + ref_options(wl)
+    t0 = time.perf_counter()
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    wall = time.perf_counter() - t0
+    if r.returncode != 0:
+        raise RuntimeError(f"reference driver failed ({r.returncode}): {r.stderr[-400:]}")
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    out["wall_s"] = wall
+    return out
+
+
+class RefSamples:
+    """The two PLINK samples of one workload in a temporary directory."""
+
+    def __init__(self, name: str):
+        self.dir = tempfile.mkdtemp(prefix="pcaone_ref_")
+        self.prefixes = []
+        for q, smp in enumerate(REF_SAMPLES):
+            prefix = os.path.join(self.dir, f"s{q}")
+            write_sample_plink(name, smp["nsamples"], smp["nsnps"], prefix)
+            self.prefixes.append(prefix)
+
+    def close(self):
+        import shutil
+        shutil.rmtree(self.dir, ignore_errors=True)
+
+
+def ref_extrapolate(wl: dict, small: dict, large: list) -> dict:
+    """Per-genotype time of the two sample sizes and the whole-workload
+    seconds extrapolated linearly in N*M from the larger sample."""
+    full = wl["nsamples"] * wl["nsnps"]
+    n_large = large[0]["nsamples"] * large[0]["nsnps"]
+    s_e = small["total_s"] / (small["nsamples"] * small["nsnps"])
+    t_large = statistics.median(r["total_s"] for r in large)
+    return {"value": t_large * full / n_large, "t_large": t_large,
+            "ns_per_genotype": {"half_sample": s_e * 1e9, "sample": t_large / n_large * 1e9},
+            "factor": full / n_large}
+
+
+def ref_sample_desc(wl: dict, ex: dict, small: dict, large: list, threads: int) -> str:
+    L = large[0]
+    return (f"the reference's own CPU path (its sources compiled on this host, -O3, OpenMP, Eigen GEMM) through "
+            f"oracle/_ref/ref_driver: read .bed, allele frequencies, decode, standardise, shuffle, winSVD "
+            f"{wl['maxp'] + 1} epochs, k={wl['k']}, p={wl['p']}, {wl['bands']} windows; samples of the same "
+            f"population model: {L['nsamples']} x {L['nsnps']} ({ex['t_large']:.2f} s, of which prepare "
+            f"{L['prepare_s']:.2f} s) and {small['nsamples']} x {small['nsnps']} ({small['total_s']:.2f} s); "
+            f"{ex['ns_per_genotype']['sample']:.2f} vs {ex['ns_per_genotype']['half_sample']:.2f} ns per genotype; "
+            f"EXTRAPOLATED linearly in N*M (x{ex['factor']:.0f}) to the whole workload; {threads} threads "
+            f"({cpu_model()})")
+
+
+def reference_cpu_baseline(name: str, wl: dict):
+    """One timing of the reference at each sample size (the repo arm's
+    cpu_baseline); None when the reference cannot be built on this host."""
+    drv = None if wl.get("dense") else ref_driver()
+    if drv is None:
+        return None
+    smp = RefSamples(name)
+    try:
+        threads = host_cores()
+        small = ref_run(drv, smp.prefixes[0], smp.dir, wl, threads)
+        large = [ref_run(drv, smp.prefixes[1], smp.dir, wl, threads)]
+    finally:
+        smp.close()
+    ex = ref_extrapolate(wl, small, large)
+    return {"value": ex["value"], "unit": "s", "cores": threads, "kind": "reference",
+            "sample": ref_sample_desc(wl, ex, small, large, threads), "measured_s": ex["t_large"]}
+
+
 def timed_call(fn):
     """(seconds by CUDA events, result) of one call, synchronised on both sides."""
     import torch
@@ -255,28 +408,56 @@ def barrier(ws: int):
 
 
 def run_reference(args):
+    """The reference arm: the reference's own CPU path on bounded samples of the
+    workload (REF_SAMPLES), all host threads; rank 0 only.  Falls back to the
+    numpy/LAPACK restatement (kind "port") when the reference cannot be built
+    on this host."""
     rank, ws, _ = dist_init()
     if rank != 0:
         return
     wl_name = args.workload
     from pcaone_gb300 import synthetic
     wl = synthetic.WORKLOADS[wl_name]
-    times = []
-    desc, cores = "", 1
-    for it in range(args.warmup + args.steps):
-        _, scaled, desc, cores = cpu_sample_run(wl_name)
-        if it >= args.warmup:
-            times.append(scaled)
-    v = statistics.median(times)
-    line = {
-        "impl": "reference", "metric": "sec_to_topk_pcs", "value": v, "unit": "s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{wl_name}: N={wl['nsamples']} x M={wl['nsnps']} PLINK, k={wl['k']}, "
-                               f"p={wl['p']}, winSVD {wl['bands']} windows, {wl['maxp'] + 1} epochs"},
-        "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": desc},
-        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
+    config = {"workload": f"{wl_name}: N={wl['nsamples']} x M={wl['nsnps']} "
+                          f"{'FP16 dosages' if wl.get('dense') else 'PLINK'}, k={wl['k']}, p={wl['p']}, winSVD "
+                          f"{wl['bands']} windows, {wl['maxp'] + 1} epochs"}
+    drv = None if wl.get("dense") else ref_driver()
+    line = {"impl": "reference", "metric": "sec_to_topk_pcs", "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config}
+    if drv is not None:
+        threads = host_cores()
+        smp = RefSamples(wl_name)
+        try:
+            small = ref_run(drv, smp.prefixes[0], smp.dir, wl, threads)
+            for _ in range(max(0, args.warmup - 1)):
+                ref_run(drv, smp.prefixes[1], smp.dir, wl, threads)
+            large = [ref_run(drv, smp.prefixes[1], smp.dir, wl, threads) for _ in range(args.steps)]
+        finally:
+            smp.close()
+        ex = ref_extrapolate(wl, small, large)
+        v = ex["value"]
+        line.update({"value": v, "value_kind": "extrapolated from the measured sample (cpu_baseline.sample)",
+                     "ms_per_step": statistics.median(r["wall_s"] for r in large) * 1e3,
+                     "ms_per_step_note": "measured wall time of one step (one run of the sample)",
+                     "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "reference",
+                                      "sample": ref_sample_desc(wl, ex, small, large, threads),
+                                      "measured_s": ex["t_large"]},
+                     "extrapolation": ex})
+    else:
+        times, walls = [], []
+        desc, cores = "", 1
+        for it in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            _, scaled, desc, cores = cpu_sample_run(wl_name)
+            if it >= args.warmup:
+                times.append(scaled)
+                walls.append(time.perf_counter() - t0)
+        v = statistics.median(times)
+        line.update({"value": v, "value_kind": "extrapolated from the measured sample (cpu_baseline.sample)",
+                     "ms_per_step": statistics.median(walls) * 1e3,
+                     "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": desc}})
+    line["e2e"] = {"value": line["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     print(json.dumps(line), flush=True)
 
 
@@ -457,11 +638,13 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        t_s, t_full, desc, cores = cpu_sample_run(args.workload)
-        if wl.get("emu"):
-            t_full *= (em_iters[-1] + 2) if em_iters else 1
-            desc += f"; scaled by {em_iters[-1] + 2 if em_iters else 1} RSVD passes (EM iterations + 2)"
-        cpu = {"value": t_full, "unit": "s", "cores": cores, "kind": "port", "sample": desc}
+        cpu = reference_cpu_baseline(args.workload, wl)
+        if cpu is None:
+            t_s, t_full, desc, cores = cpu_sample_run(args.workload)
+            if wl.get("emu"):
+                t_full *= (em_iters[-1] + 2) if em_iters else 1
+                desc += f"; scaled by {em_iters[-1] + 2 if em_iters else 1} RSVD passes (EM iterations + 2)"
+            cpu = {"value": t_full, "unit": "s", "cores": cores, "kind": "port", "sample": desc}
 
     if rank == 0:
         line = {

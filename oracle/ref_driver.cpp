@@ -4,8 +4,20 @@
 // but writes U, S, V, F and the column permutation at full double precision
 // (the reference's text writers keep 6 significant digits, src/Data.cpp:215).
 //
-// usage: ref_driver OUTDIR <PCAone command-line options, e.g. -b prefix -k 10 -d 2>
-//        (PLINK -b input, or FileBinary -B input with -C 0)
+// usage: ref_driver OUTDIR [driver options] <PCAone command-line options,
+//        e.g. -b prefix -k 10 -d 2> (PLINK -b input, or FileBinary -B input with -C 0)
+//
+// Driver options:
+//   --dump-g0             also write G0.npy (below)
+//   --project-new PREFIX  also write P1.npy, P2.npy (below)
+//   --force-oversamples P run with P oversamples although the CLI raises them to
+//                         at least k (src/Cmd.cpp:216): the field of the parsed
+//                         Param is set before the operator is built; the
+//                         reference's code is unchanged
+//   --timing              write no arrays; print one JSON line with the wall
+//                         time of prepare() (read, allele frequencies, decode)
+//                         and of the RSVD (operator construction, shuffle and
+//                         computeUSV), and the OpenMP thread count
 //
 // Outputs (numpy .npy, float64 column-major / int64):
 //   F.npy         allele frequencies after the AF pass (src/FilePlink.cpp:33-62; PLINK only)
@@ -22,6 +34,9 @@
 //                 run_projection does (src/Projection.cpp:236-247,
 //                 src/Data.cpp:17-32)
 #define _DECLARE_TOOLBOX_HERE
+#include <omp.h>
+
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -74,7 +89,8 @@ int main(int argc, char** argv) {
     return 2;
   }
   std::string outdir = argv[1];
-  bool dump_g0 = false;
+  bool dump_g0 = false, timing = false;
+  int force_os = -1;
   std::string project_new;
   std::vector<char*> args;
   args.push_back(argv[0]);
@@ -87,18 +103,31 @@ int main(int argc, char** argv) {
       project_new = argv[++i];
       continue;
     }
+    if (std::strcmp(argv[i], "--force-oversamples") == 0 && i + 1 < argc) {
+      force_os = std::atoi(argv[++i]);
+      continue;
+    }
+    if (std::strcmp(argv[i], "--timing") == 0) {
+      timing = true;
+      continue;
+    }
     args.push_back(argv[i]);
   }
   Param params((int)args.size(), args.data());
+  if (force_os >= 0) params.oversamples = force_os;
   cao.cao.open(outdir + "/ref.log");
   cao.is_screen = false;
   if (params.file_t != FileType::PLINK && params.file_t != FileType::BINARY) {
     std::fprintf(stderr, "only PLINK and binary input are driven here\n");
     return 2;
   }
+  using clk = std::chrono::steady_clock;
+  const auto t0 = clk::now();
   Data* data = params.file_t == FileType::PLINK ? (Data*)new FileBed(params) : (Data*)new FileBin(params);
   data->prepare();
-  if (params.file_t == FileType::PLINK) dump1(outdir, "F", data->F);
+  const auto t1 = clk::now();
+  if (timing) dump_g0 = false;
+  if (params.file_t == FileType::PLINK && !timing) dump1(outdir, "F", data->F);
   if (dump_g0) dump(outdir, "G0", data->G);
 
   // operator selection and call sequence of run_pca_with_halko (src/Halko.cpp:271-320)
@@ -107,7 +136,7 @@ int main(int argc, char** argv) {
     rsvd = new FancyRsvdOpData(data, params.k, params.oversamples);
   else
     rsvd = new NormalRsvdOpData(data, params.k, params.oversamples);
-  dump(outdir, "Omg0", rsvd->Omg);
+  if (!timing) dump(outdir, "Omg0", rsvd->Omg);
   int em_iters = 0;
   if (!params.missme) {
     rsvd->setFlags(false, params.ld ? false : true);
@@ -130,6 +159,17 @@ int main(int argc, char** argv) {
       rsvd->computeUSV(params.maxp, params.tol);
       flip_UV(rsvd->U, rsvd->V, false);
     }
+  }
+  const auto t2 = clk::now();
+  if (timing) {
+    std::printf("{\"prepare_s\": %.6f, \"rsvd_s\": %.6f, \"total_s\": %.6f, \"threads\": %d, \"nsamples\": %lld, "
+                "\"nsnps\": %lld, \"k\": %d, \"oversamples\": %d, \"em_iters\": %d, \"S0\": %.17g}\n",
+                std::chrono::duration<double>(t1 - t0).count(), std::chrono::duration<double>(t2 - t1).count(),
+                std::chrono::duration<double>(t2 - t0).count(), omp_get_max_threads(), (long long)data->nsamples,
+                (long long)data->nsnps, (int)params.k, (int)params.oversamples, em_iters, (double)rsvd->S(0));
+    delete rsvd;
+    delete data;
+    return 0;
   }
   dump(outdir, "U", rsvd->U);
   dump1(outdir, "S", rsvd->S);

@@ -23,6 +23,19 @@ __global__ void k_sanitize(uint8_t* bed, int64_t stride, int64_t nsnps, int nsam
   *p = (uint8_t)(*p & ((1u << (2 * rem)) - 1u));
 }
 
+// Rows of `bps` bytes from a packed source (pitch src_pitch) into rows of
+// dst_pitch bytes; one block per row, 16-, 4- or 1-byte moves as the pitches
+// and bases allow.
+template <class T>
+__global__ void k_repitch(const uint8_t* __restrict__ src, int64_t src_pitch, uint8_t* __restrict__ dst,
+                          int64_t dst_pitch, int64_t bps) {
+  const int64_t r = blockIdx.x;
+  const T* s = reinterpret_cast<const T*>(src + r * src_pitch);
+  T* d = reinterpret_cast<T*>(dst + r * dst_pitch);
+  const int64_t n = bps / (int64_t)sizeof(T);
+  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) d[q] = s[q];
+}
+
 // One warp per SNP row.  Per 32-bit word of 16 lanes: lo = bit 0 of each lane,
 // hi = bit 1.  n11 = popc(lo & hi), n01 = popc(lo & ~hi), n10 = popc(hi & ~lo);
 // n00 = N - the rest (padding lanes are code 00 and drop out).
@@ -135,6 +148,19 @@ __global__ void k_synth(uint8_t* __restrict__ bed, int64_t stride, int64_t snp0,
 }
 
 }  // namespace
+
+void launch_repitch(const uint8_t* src, int64_t src_pitch, uint8_t* dst, int64_t dst_pitch, int64_t nrows, int64_t bps,
+                    cudaStream_t s) {
+  if (nrows <= 0) return;
+  const uintptr_t al = (uintptr_t)src | (uintptr_t)dst | (uintptr_t)src_pitch | (uintptr_t)dst_pitch | (uintptr_t)bps;
+  if ((al & 15u) == 0)
+    k_repitch<uint4><<<(unsigned)nrows, 256, 0, s>>>(src, src_pitch, dst, dst_pitch, bps);
+  else if ((al & 3u) == 0)
+    k_repitch<uint32_t><<<(unsigned)nrows, 256, 0, s>>>(src, src_pitch, dst, dst_pitch, bps);
+  else
+    k_repitch<uint8_t><<<(unsigned)nrows, 256, 0, s>>>(src, src_pitch, dst, dst_pitch, bps);
+  PCAONE_LAUNCH_CHECK();
+}
 
 void launch_sanitize_padding(uint8_t* bed, int64_t stride, int64_t nsnps, int nsamples, cudaStream_t s) {
   if ((nsamples & 3) == 0 || nsnps == 0) return;

@@ -171,6 +171,20 @@ struct Context {
 
   BedView view() const { return BedView{bed.p, stride, M, N}; }
 
+  // host loads (load_bed_host): a copy stream, two staging buffers and their
+  // events; ev_free[2] marks where the context's stream stood when a load began
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[3] = {nullptr, nullptr, nullptr};
+  DBuf<uint8_t> stage;
+  void ensure_copy_stream() {
+    if (!copy_stream) {
+      PCAONE_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+      for (auto* e : {&ev_copied[0], &ev_copied[1], &ev_free[0], &ev_free[1], &ev_free[2]})
+        PCAONE_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    PCAONE_CUDA(cudaEventRecord(ev_free[2], stream));
+  }
+
   cudaEvent_t next_event() {
     if (ev_used == ev_pool.size()) {
       cudaEvent_t e;
@@ -194,12 +208,20 @@ struct Context {
   }
   ~Context() {
     for (auto e : ev_pool) cudaEventDestroy(e);
+    if (copy_stream) {
+      cudaStreamSynchronize(copy_stream);
+      cudaStreamDestroy(copy_stream);
+      for (auto e : {ev_copied[0], ev_copied[1], ev_free[0], ev_free[1], ev_free[2]}) cudaEventDestroy(e);
+    }
   }
 };
 
 // ------------------------------------------------------------------------
 // data
 // ------------------------------------------------------------------------
+// bytes of one staging buffer of the host loads
+constexpr size_t kStageBytes = (size_t)512 << 20;
+
 static void load_common(Context& c, uint64_t nsnps, uint32_t nsamples, bool dense = false) {
   if (nsamples == 0 || nsnps == 0) throw Error(PCAONE_E_ARG, "empty genotype matrix");
   if (nsnps > 0x7fffffffull) throw Error(PCAONE_E_LIMIT, "more than 2^31-1 SNPs");
@@ -239,10 +261,35 @@ static void ensure_missing_total(Context& c) {
   c.counts_total_missing = t;
 }
 
+// The .bed body from host memory: contiguous chunks of whole rows are copied
+// into two staging buffers on a second stream (large linear copies run at the
+// host link's rate, where one pitched copy of short rows does not) while the
+// context's stream re-pitches the previous chunk into the padded rows.
 static void load_bed_host(Context& c, const uint8_t* packed, uint64_t nsnps, uint32_t nsamples) {
   load_common(c, nsnps, nsamples);
-  const size_t bps = ((size_t)nsamples + 3) / 4;
-  PCAONE_CUDA(cudaMemcpy2DAsync(c.bed.p, c.stride, packed, bps, bps, nsnps, cudaMemcpyHostToDevice, c.stream));
+  const int64_t bps = ((int64_t)nsamples + 3) / 4;
+  if (bps == c.stride) {
+    PCAONE_CUDA(cudaMemcpyAsync(c.bed.p, packed, (size_t)c.M * bps, cudaMemcpyHostToDevice, c.stream));
+    finish_load(c);
+    return;
+  }
+  c.ensure_copy_stream();
+  const int64_t rows = std::max<int64_t>(1, std::min<int64_t>(c.M, (int64_t)(kStageBytes / bps)));
+  c.stage.ensure((size_t)(2 * rows * bps), c.stream, false);
+  for (int64_t j0 = 0, q = 0; j0 < c.M; j0 += rows, ++q) {
+    const int b = (int)(q & 1);
+    const int64_t n = std::min<int64_t>(rows, c.M - j0);
+    uint8_t* buf = c.stage.p + (size_t)b * rows * bps;
+    // the buffer is free once the re-pitch that last read it has run (for the
+    // first two chunks: once the context's stream reached this load)
+    PCAONE_CUDA(cudaStreamWaitEvent(c.copy_stream, q >= 2 ? c.ev_free[b] : c.ev_free[2], 0));
+    PCAONE_CUDA(cudaMemcpyAsync(buf, packed + (size_t)j0 * bps, (size_t)n * bps, cudaMemcpyHostToDevice,
+                                c.copy_stream));
+    PCAONE_CUDA(cudaEventRecord(c.ev_copied[b], c.copy_stream));
+    PCAONE_CUDA(cudaStreamWaitEvent(c.stream, c.ev_copied[b], 0));
+    launch_repitch(buf, bps, c.bed.p + (size_t)j0 * c.stride, c.stride, n, bps, c.stream);
+    PCAONE_CUDA(cudaEventRecord(c.ev_free[b], c.stream));
+  }
   finish_load(c);
 }
 

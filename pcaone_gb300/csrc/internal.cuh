@@ -120,6 +120,9 @@ struct BedView {
 
 // bed.cu
 void launch_sanitize_padding(uint8_t* bed, int64_t stride, int64_t nsnps, int nsamples, cudaStream_t s);
+// nrows rows of bps bytes: src (pitch src_pitch) -> dst (pitch dst_pitch)
+void launch_repitch(const uint8_t* src, int64_t src_pitch, uint8_t* dst, int64_t dst_pitch, int64_t nrows, int64_t bps,
+                    cudaStream_t s);
 void launch_counts(const BedView& v, int32_t* counts, double* F, cudaStream_t s);
 // per-SNP decode table: lut[j] = {x(00), x(01), x(10), x(11)} with x(c) =
 // scale_j * (BED2GENO[c] - F_j), x(01) = 0; lut64 likewise in double.
