@@ -561,8 +561,12 @@ def run_ours(args):
         em_iters.append(out[3])
         return out
 
+    load_s = []
+
     def step_e2e():
+        t0 = time.perf_counter()
         ctx.load_bed_ptr(pinned.data_ptr(), M, N)
+        load_s.append(time.perf_counter() - t0)
         return ctx.run_halko(params)
 
     for _ in range(args.warmup):
@@ -655,7 +659,9 @@ def run_ours(args):
                        "precision": args.precision, "l2": "inputs larger than L2 (packed matrix resident in HBM)",
                        "replicas": ws},
             "clocks": clocks.summary(),
-            "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "load_s": statistics.median(load_s[1:]) if len(load_s) > 1 else None,
+                    "load_gbs": M * bps / statistics.median(load_s[1:]) / 1e9 if len(load_s) > 1 else None},
             "gpu_launches": int(launches),
             "roofline": roof,
             "cpu_baseline": cpu,

@@ -116,6 +116,18 @@ void pcaone_gpu_mlp_default_params(pcaone_gpu_mlp_params* p);
 /* Fills p with the reference's defaults (src/Cmd.hpp:29-95). */
 void pcaone_gpu_default_params(pcaone_gpu_params* p);
 
+/* ---- host-side random streams (no GPU, no context) ----------------------
+ * The initial test matrix of RsvdOpData::initOmg (src/Halko.cpp:15-23,
+ * StandardNormalRandom / UniformRandom of src/RSVD.hpp:20-59): rows x cols,
+ * column-major, N(0,1) when gaussian (--rand 1) else U(-1,1), drawn with
+ * std::default_random_engine seeded with `seed` -- the matrix pcaone_gpu_op_init
+ * uses unless pcaone_gpu_set_omega replaced it. */
+int pcaone_gpu_random_omega(int seed, int gaussian, uint64_t rows, uint32_t cols, double* out);
+/* The in-core SNP shuffle of PCAone::permute_matrix (src/RSVD.hpp:61-70):
+ * perm[i] = original SNP of working column i (std::shuffle of 0..n-1 with a
+ * default-constructed engine), as pcaone_gpu_get_perm returns it. */
+int pcaone_gpu_shuffle_order(uint64_t n, int32_t* perm);
+
 /* ---- context ------------------------------------------------------------ */
 int pcaone_gpu_open(const pcaone_gpu_desc* desc, pcaone_gpu_ctx** out);
 int pcaone_gpu_close(pcaone_gpu_ctx* ctx);
@@ -135,6 +147,13 @@ int pcaone_gpu_timings(const pcaone_gpu_ctx* ctx, double t[4]);
 int pcaone_gpu_set_profiling(pcaone_gpu_ctx* ctx, int on);
 int pcaone_gpu_kernel_stats(pcaone_gpu_ctx* ctx, double ms[2], double flops[2], long long launches[2]);
 unsigned long long pcaone_gpu_launch_count(void);
+/* Test hook with no counterpart in the reference: the limit, in SM clock
+ * cycles, of every pipeline wait in the tensor-core product kernels (0, the
+ * default: about two seconds).  A wait that runs out makes its tile give up:
+ * the tile waits (bounded) for its own copies and MMAs in flight, frees its
+ * tensor memory and flags the error, and the call returns PCAONE_E_CUDA; the
+ * context stays usable. */
+int pcaone_gpu_set_wait_limit(pcaone_gpu_ctx* ctx, long long cycles);
 
 /* ---- data: replaces FileBed::read_all (src/FilePlink.cpp:26-120) --------- */
 /* packed: the .bed body after the 3 magic bytes, nsnps rows of (nsamples+3)/4
@@ -239,14 +258,15 @@ int pcaone_gpu_mlp_forward_backward(int device, const float* X, const float* y, 
                                     float* out, float* loss, float* grads);
 
 /* ---- Arnoldi matvec: replaces ArnoldiOpData::perform_op (Arnoldi.cpp:18-46) */
-/* y = X X^T x over the loaded genotypes (X samples x SNPs, centred, scaled
- * when standardize != 0), x and y of length N. */
+/* y = X X^T x over the loaded genotypes (X samples x SNPs, centred, scaled by
+ * sqrt(ploidy)/sd when standardize != 0, the ploidy of the last
+ * pcaone_gpu_op_init or 2), x and y of length N. */
 int pcaone_gpu_matvec(pcaone_gpu_ctx* ctx, const double* x, double* y, int standardize);
 
 /* ---- matvec without device allocation (no counterpart in the reference) --
  * y = X X^T x like pcaone_gpu_matvec, for callers that cannot call cudaMalloc
- * (code recorded into a CUDA graph, hosts whose memory manager owns all device
- * memory, loops that cannot afford an allocation's synchronisation).  All
+ * (a host whose own allocator or memory arena owns all device memory, or a
+ * loop that cannot afford an allocation's implicit synchronisation).  All
  * pointers are device pointers the caller owns: d_packed holds nsnps rows of
  * row_pitch bytes (the .bed body, row_pitch >= (nsamples+3)/4), d_F the allele
  * frequencies (pcaone_gpu_counts), d_x and d_y nsamples doubles; the work is
@@ -257,7 +277,10 @@ int pcaone_gpu_matvec(pcaone_gpu_ctx* ctx, const double* x, double* y, int stand
  * larger inputs return PCAONE_E_LIMIT.  The first call on a device resolves
  * the array's device address (cudaGetSymbolAddress); make that first call
  * before any stream capture.  Calls share the array: calls whose work overlaps
- * on the GPU race and must be serialised by the caller. */
+ * on the GPU race and must be serialised by the caller.  The scale is the
+ * diploid one, sqrt(2)/sd (standardize != 0).  The cached address belongs to
+ * the device's primary context: callers on another driver context, or after a
+ * cudaDeviceReset, are not supported. */
 int pcaone_gpu_matvec_static(const uint8_t* d_packed, uint64_t row_pitch, uint64_t nsnps, uint32_t nsamples,
                              const double* d_F, int standardize, const double* d_x, double* d_y, void* stream);
 

@@ -14,6 +14,10 @@
 //                         at least k (src/Cmd.cpp:216): the field of the parsed
 //                         Param is set before the operator is built; the
 //                         reference's code is unchanged
+//   --eigs-files          also write the reference's text outputs through
+//                         Data::write_eigs_files (src/Data.cpp:211-240) as
+//                         src/Halko.cpp:339 does (needs -o PREFIX; -V for the
+//                         .loadings)
 //   --timing              write no arrays; print one JSON line with the wall
 //                         time of prepare() (read, allele frequencies, decode)
 //                         and of the RSVD (operator construction, shuffle and
@@ -89,7 +93,7 @@ int main(int argc, char** argv) {
     return 2;
   }
   std::string outdir = argv[1];
-  bool dump_g0 = false, timing = false;
+  bool dump_g0 = false, timing = false, eigs_files = false;
   int force_os = -1;
   std::string project_new;
   std::vector<char*> args;
@@ -105,6 +109,10 @@ int main(int argc, char** argv) {
     }
     if (std::strcmp(argv[i], "--force-oversamples") == 0 && i + 1 < argc) {
       force_os = std::atoi(argv[++i]);
+      continue;
+    }
+    if (std::strcmp(argv[i], "--eigs-files") == 0) {
+      eigs_files = true;
       continue;
     }
     if (std::strcmp(argv[i], "--timing") == 0) {
@@ -171,6 +179,7 @@ int main(int argc, char** argv) {
     delete data;
     return 0;
   }
+  if (eigs_files) data->write_eigs_files(rsvd->S.array().square() / data->nsnps, rsvd->S, rsvd->U, rsvd->V);
   dump(outdir, "U", rsvd->U);
   dump1(outdir, "S", rsvd->S);
   dump(outdir, "V", rsvd->V);

@@ -33,6 +33,7 @@ EXPORTS = [
     "pcaone_gpu_matvec_static", "pcaone_gpu_mlp_default_params", "pcaone_gpu_set_warm_start",
     "pcaone_gpu_mlp_stats", "pcaone_gpu_mlp_forward_backward", "pcaone_gpu_load_dense",
     "pcaone_gpu_load_binary_file_image", "pcaone_gpu_load_synthetic_dense", "pcaone_gpu_project",
+    "pcaone_gpu_random_omega", "pcaone_gpu_shuffle_order", "pcaone_gpu_set_wait_limit",
 ]
 MLP_PARAMS, MLP_INPUTS = 82689, 64
 
@@ -110,12 +111,33 @@ def load(path: str = LIBPATH) -> ctypes.CDLL:
     lib.pcaone_gpu_mlp_stats.argtypes = [c_void_p, c_void_p]
     lib.pcaone_gpu_mlp_forward_backward.argtypes = [c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
                                                     c_void_p]
+    lib.pcaone_gpu_random_omega.argtypes = [c_int, c_int, c_uint64, c_uint32, c_void_p]
+    lib.pcaone_gpu_shuffle_order.argtypes = [c_uint64, c_void_p]
+    lib.pcaone_gpu_set_wait_limit.argtypes = [c_void_p, ctypes.c_longlong]
     for name in EXPORTS:
         if name not in ("pcaone_gpu_default_params", "pcaone_gpu_last_error", "pcaone_gpu_mlp_default_params"):
             getattr(lib, name).restype = c_int
     lib.pcaone_gpu_launch_count.restype = ctypes.c_ulonglong
     _lib = lib
     return lib
+
+
+def random_omega(seed: int, rows: int, cols: int, gaussian: bool = True) -> np.ndarray:
+    """The library's initial test matrix (pcaone_gpu_random_omega): host only."""
+    out = np.empty((rows, cols), dtype=np.float64, order="F")
+    rc = load().pcaone_gpu_random_omega(seed, int(gaussian), rows, cols, out.ctypes.data)
+    if rc != PCAONE_OK:
+        raise PcaoneError(rc, "pcaone_gpu_random_omega failed")
+    return out
+
+
+def shuffle_order(n: int) -> np.ndarray:
+    """The library's in-core SNP order (pcaone_gpu_shuffle_order): host only."""
+    out = np.empty(n, dtype=np.int32)
+    rc = load().pcaone_gpu_shuffle_order(n, out.ctypes.data)
+    if rc != PCAONE_OK:
+        raise PcaoneError(rc, "pcaone_gpu_shuffle_order failed")
+    return out
 
 
 def default_params(**kw) -> Params:
@@ -335,6 +357,9 @@ class Context:
         y = np.empty_like(x)
         self._check(self.lib.pcaone_gpu_matvec(self.h, _ptr(x), _ptr(y), int(standardize)))
         return y
+
+    def set_wait_limit(self, cycles: int):
+        self._check(self.lib.pcaone_gpu_set_wait_limit(self.h, int(cycles)))
 
     def set_profiling(self, on: bool):
         self._check(self.lib.pcaone_gpu_set_profiling(self.h, int(on)))

@@ -157,6 +157,7 @@ struct Context {
   int ldg = 0, win_max = 0;
   int nslice_cur = 1, w_slices = 0;
   int max_slices = 3;  // slices of the chosen form: 3, or 6 in the FP64-grade form
+  long long wait_cycles = 0;  // limit of the tensor-core pipeline waits (0: the kernels' default)
   bool fp64 = false;   // FP64-grade form: the QR and small-SVD kernels in plain FP64 too
 
   // optional per-kernel CUDA-event timing of the window products
@@ -608,6 +609,16 @@ static int read_status(Context& c) {
   return st;
 }
 
+// a tensor-core tile that gave up a bounded wait leaves its partial sums
+// unwritten: report that (PCAONE_E_CUDA) before any numerical consequence
+static void check_tc_err(Context& c) {
+  if (!c.tc) return;
+  int e = 0;
+  PCAONE_CUDA(cudaMemcpyAsync(&e, c.err.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  if (e) throw Error(PCAONE_E_CUDA, "tensor-core pipeline: a bounded wait gave up (kernel aborted its tile)");
+}
+
 // Orthonormal factor of A (rows x LP, in place) by CholeskyQR2, or shifted
 // CholeskyQR3 when the first Gram is not numerically positive definite
 // (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa 2020).  With need_r, Rt
@@ -627,13 +638,19 @@ static void cholqr(Context& c, double* A, int64_t rows, bool need_r) {
     for (int i = 0; i < L; ++i) tr += w[(size_t)i * LP + i];
     const double shift = 11.0 * ((double)rows * L + (double)L * (L + 1)) * 1.1102230246251565e-16 * tr;
     launch_chol_inv_shift(c.W.p, L, LP, shift, c.R1.p, c.R1i.p, c.status.p, c.stream, c.fp64);
-    if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: Gram matrix not positive definite");
+    if (read_status(c) != 0) {
+      check_tc_err(c);
+      throw Error(PCAONE_E_NUMERIC, "CholeskyQR: Gram matrix not positive definite");
+    }
     shifted = true;
   }
   launch_gemm_tall_upper(A, rows, LP, c.R1i.p, c.stream, c.fp64);
   launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream, c.fp64);
   launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R2.p, c.R2i.p, c.status.p, c.stream, c.fp64);
-  if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: second Gram not positive definite");
+  if (read_status(c) != 0) {
+    check_tc_err(c);
+    throw Error(PCAONE_E_NUMERIC, "CholeskyQR: second Gram not positive definite");
+  }
   launch_gemm_tall_upper(A, rows, LP, c.R2i.p, c.stream, c.fp64);
   if (need_r) {
     launch_mult_small(c.R2.p, c.R1.p, c.Rt.p, LP, c.stream);     // R = R2 R1
@@ -642,7 +659,10 @@ static void cholqr(Context& c, double* A, int64_t rows, bool need_r) {
   if (shifted) {
     launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream, c.fp64);
     launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R3.p, c.R3i.p, c.status.p, c.stream, c.fp64);
-    if (read_status(c) != 0) throw Error(PCAONE_E_NUMERIC, "CholeskyQR: third Gram not positive definite");
+    if (read_status(c) != 0) {
+      check_tc_err(c);
+      throw Error(PCAONE_E_NUMERIC, "CholeskyQR: third Gram not positive definite");
+    }
     launch_gemm_tall_upper(A, rows, LP, c.R3i.p, c.stream, c.fp64);
     if (need_r) {
       launch_mult_small(c.R3.p, c.Rt.p, c.R1.p, LP, c.stream);
@@ -853,6 +873,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ga.part = c.tpart.p;
   ga.err = c.err.p;
   ga.dense = c.dense ? 1 : 0;
+  ga.wait_cycles = c.wait_cycles;
   mark(0);
   tc::launch_g(c.map_bed_g, c.map_w, ga, c.stream);
   close_mark();
@@ -917,6 +938,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ha.hpart = c.thpart.p;
   ha.err = c.err.p;
   ha.dense = c.dense ? 1 : 0;
+  ha.wait_cycles = c.wait_cycles;
   if (any_miss) {
     // sum_j Gm_j (and sum_j 2 e_j Gh_j) over each sample's missing SNPs of the window
     SegGatherArgs sg{};
@@ -1049,13 +1071,6 @@ static int slices_for_epoch(const Context& c, int pi) {
   return c.max_slices;
 }
 
-static void check_tc_err(Context& c) {
-  if (!c.tc) return;
-  int e = 0;
-  PCAONE_CUDA(cudaMemcpyAsync(&e, c.err.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
-  if (e) throw Error(PCAONE_E_CUDA, "tensor-core pipeline: a bounded wait gave up (kernel aborted its tile)");
-}
 
 static void compute_g_and_h(Context& c, int pi) {
   c.nslice_cur = c.tc ? slices_for_epoch(c, pi) : 1;
@@ -1068,6 +1083,7 @@ static void compute_g_and_h(Context& c, int pi) {
 // RsvdOpData::computeUSV (src/Halko.cpp:46-97)
 static int compute_usv(Context& c, int p, double tol) {
   const int64_t M = c.M;
+  if (c.tc) PCAONE_CUDA(cudaMemsetAsync(c.err.p, 0, sizeof(int), c.stream));  // a fresh abort flag per call
   const int N = c.N, L = c.L, LP = c.LP, k = c.k;
   int epochs = 0;
   bool done = false, ucur_in_upre = false;
@@ -1335,7 +1351,9 @@ static void matvec(Context& c, const double* x, double* y, int standardize) {
   const int nsplit = matvec_splits(c.M, N);
   c.mv_ypart.ensure((size_t)nsplit * N, c.stream, false);
   PCAONE_CUDA(cudaMemcpyAsync(c.mv_x.p, x, N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-  launch_lut(c.F.p, c.M, standardize, 2, nullptr, nullptr, c.mv_scale.p, c.stream);
+  // the scale sqrt(ploidy)/sd of src/FilePlink.cpp:146, with the ploidy of the
+  // operator's parameters (2 before any pcaone_gpu_op_init)
+  launch_lut(c.F.p, c.M, standardize, c.have_op ? c.P.ploidy : 2, nullptr, nullptr, c.mv_scale.p, c.stream);
   launch_matvec(c.view(), c.F.p, c.mv_scale.p, c.mv_x.p, c.mv_t.p, c.mv_y.p, c.mv_ypart.p, nsplit, c.stream);
   PCAONE_CUDA(cudaMemcpyAsync(y, c.mv_y.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
   PCAONE_CUDA(cudaStreamSynchronize(c.stream));
@@ -1396,6 +1414,22 @@ void pcaone_gpu_default_params(pcaone_gpu_params* p) {
 
 int pcaone_gpu_abi_version(void) { return PCAONE_GPU_ABI_VERSION; }
 
+int pcaone_gpu_random_omega(int seed, int gaussian, uint64_t rows, uint32_t cols, double* out) {
+  if (!out || rows == 0 || cols == 0) return PCAONE_E_ARG;
+  try {
+    pcaone::host_random_omega(seed, gaussian ? 1 : 0, (int64_t)rows, (int64_t)cols, out);
+  } catch (const std::exception&) {
+    return PCAONE_E_ARG;
+  }
+  return PCAONE_OK;
+}
+
+int pcaone_gpu_shuffle_order(uint64_t n, int32_t* perm) {
+  if (!perm || n == 0 || n > 0x7fffffffull) return PCAONE_E_ARG;
+  pcaone::host_shuffle_columns((int64_t)n, perm);
+  return PCAONE_OK;
+}
+
 int pcaone_gpu_open(const pcaone_gpu_desc* desc, pcaone_gpu_ctx** out) {
   if (!out) return PCAONE_E_ARG;
   *out = nullptr;
@@ -1424,6 +1458,13 @@ int pcaone_gpu_close(pcaone_gpu_ctx* ctx) {
 
 const char* pcaone_gpu_last_error(const pcaone_gpu_ctx* ctx) {
   return ctx ? ctx->c.last_error.c_str() : "null context";
+}
+
+int pcaone_gpu_set_wait_limit(pcaone_gpu_ctx* ctx, long long cycles) {
+  return guarded(ctx, [&](Context& c) {
+    if (cycles < 0) throw Error(PCAONE_E_ARG, "negative wait limit");
+    c.wait_cycles = cycles;
+  });
 }
 
 int pcaone_gpu_set_profiling(pcaone_gpu_ctx* ctx, int on) {

@@ -347,12 +347,15 @@ __device__ __forceinline__ void mma_cat(uint32_t tmem_col0, uint32_t a_addr, uin
 constexpr int kDecodeWarp0 = 2;
 constexpr int kDecoders = 256;
 
-__device__ __forceinline__ bool role_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+// limit: cycles before the wait gives up (the kernel argument wait_cycles;
+// kTimeoutCycles when it is 0)
+__device__ __forceinline__ bool role_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          long long limit) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
     if (*abort_flag) return false;
-    if (clock64() - t0 > kTimeoutCycles) {
+    if (clock64() - t0 > limit) {
       *abort_flag = 1;
       return false;
     }
@@ -362,6 +365,27 @@ __device__ __forceinline__ bool role_wait(uint64_t* bar, uint32_t parity, volati
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// After an abort: wait (each wait bounded) for the TMA copies that may still
+// be in flight.  Stage st is reused only after its previous copy was consumed,
+// so only the last nst issued copies can be pending; waiting on older phases
+// would alias their parity with the stage's current phase.
+__device__ __forceinline__ void drain_copies(uint64_t* full_bar, int issued, int nst) {
+  for (int kb = issued > nst ? issued - nst : 0; kb < issued; ++kb)
+    mbar_wait(&full_bar[kb % nst], (uint32_t)(kb / nst) & 1u);
+}
+
+// End of a CTA: after an abort the epilogue has not waited for the MMAs (acc_bar
+// arrives once every issued MMA has completed; the MMA thread always commits
+// it), so warp 0 waits for it, bounded, before it frees the TMEM.
+__device__ __forceinline__ void cta_release(uint64_t& acc_bar, volatile int& abort_flag, int warp, int lane,
+                                            uint32_t tmem, uint32_t cols) {
+  if (warp != 0) return;
+  if (abort_flag && lane == 0) mbar_wait(&acc_bar, 0u);
+  __syncwarp();
+  tc_fence_after();
+  tmem_dealloc(tmem, cols);
 }
 
 // Epilogue helpers.  The accumulator of slice s for columns c0 .. c0+7 of a
@@ -449,6 +473,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   const int nk = (kend - kbeg + kStepK - 1) / kStepK;
   const int nst = a.nstages;
   const int ncat = S * LP;  // slices concatenated along N
+  const long long wlim = a.wait_cycles > 0 ? a.wait_cycles : kTimeoutCycles;
 
   if (tid == 0) {
     abort_sh = 0;
@@ -483,7 +508,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         const int st = kb % nst;
         if (kb + kPrefetchSteps < nk)
           tma_prefetch_2d(&map_bed, (kbeg + (kb + kPrefetchSteps) * kStepK) >> kdiv, (int)(a.pos0 + row0));
-        if (kb >= nst && !role_wait(&empty_bar[st], (uint32_t)(kb / nst - 1) & 1u, &abort_sh)) break;
+        if (kb >= nst && !role_wait(&empty_bar[st], (uint32_t)(kb / nst - 1) & 1u, &abort_sh, wlim)) break;
         uint8_t* base = smem + st * lay.stage_bytes;
         const int k0 = kbeg + kb * kStepK;
         mbar_expect_tx(&full_bar[st], tx_bytes);
@@ -491,16 +516,14 @@ __global__ void __launch_bounds__(kThreads, 2)
         for (int s = 0; s < S; ++s) tma_load_2d(base + lay.b + s * LP * 128, &map_w, k0, s * LP, &full_bar[st]);
         issued = kb + 1;
       }
-      if (abort_sh) {  // let every issued copy land before the CTA exits
-        for (int kb = 0; kb < issued; ++kb) mbar_wait(&full_bar[kb % nst], (uint32_t)(kb / nst) & 1u);
-      }
+      if (abort_sh) drain_copies(full_bar, issued, nst);
     }
   } else if (warp == 1) {
     // ---- MMA issuer ----
     if (lane == 0) {
       for (int kb = 0; kb < nk; ++kb) {
         const int st = kb % nst;
-        if (!role_wait(&dec_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
+        if (!role_wait(&dec_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh, wlim)) break;
         tc_fence_after();
         uint8_t* base = smem + st * lay.stage_bytes;
         const uint32_t bb = smem_u32(base + lay.b);
@@ -529,7 +552,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
     for (int kb = 0; kb < nk; ++kb) {
       const int st = kb % nst;
-      if (!role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
+      if (!role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh, wlim)) break;
       uint8_t* base = smem + st * lay.stage_bytes;
       uint32_t wd[16];
       if (kDense) {
@@ -566,7 +589,7 @@ __global__ void __launch_bounds__(kThreads, 2)
       mbar_arrive(&dec_bar[st]);
     }
     // ---- epilogue ----
-    const bool ok = nk > 0 && role_wait(&acc_bar, 0u, &abort_sh);
+    const bool ok = nk > 0 && role_wait(&acc_bar, 0u, &abort_sh, wlim);
     tc_fence_after();
     const int quarter = warp & 3, chalf = (warp - kDecodeWarp0) >> 2;
     const int j = row0 + quarter * 32 + lane;
@@ -598,7 +621,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   tc_fence_before();
   __syncthreads();
   if (tid == 0 && abort_sh) *a.err = 1;
-  if (warp == 0) tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
+  cta_release(acc_bar, abort_sh, warp, lane, tmem, (uint32_t)a.tmem_cols);
 }
 
 // ---------------------------------------------------------------------------
@@ -629,6 +652,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   const int nk = je > jb ? (je - jb + kStepK - 1) / kStepK : 0;
   const int nst = a.nstages;
   const int ncat = S * LP;
+  const long long wlim = a.wait_cycles > 0 ? a.wait_cycles : kTimeoutCycles;
 
   if (kDense)
     for (int e = tid; e < ncat; e += kThreads) unit[e] = (float)a.hscale[e];
@@ -662,7 +686,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         const int st = kb % nst;
         if (kb + kPrefetchSteps < nk)
           tma_prefetch_2d(&map_bed, scol, (int)(a.pos0 + jb + (kb + kPrefetchSteps) * kStepK));
-        if (kb >= nst && !role_wait(&empty_bar[st], (uint32_t)(kb / nst - 1) & 1u, &abort_sh)) break;
+        if (kb >= nst && !role_wait(&empty_bar[st], (uint32_t)(kb / nst - 1) & 1u, &abort_sh, wlim)) break;
         uint8_t* base = smem + st * lay.stage_bytes;
         const int j0 = jb + kb * kStepK;
         mbar_expect_tx(&full_bar[st], tx_bytes);
@@ -670,15 +694,13 @@ __global__ void __launch_bounds__(kThreads, 2)
         for (int r = 0; r < S; ++r) tma_load_2d(base + lay.b + r * LP * 128, &map_g, j0, r * LP, &full_bar[st]);
         issued = kb + 1;
       }
-      if (abort_sh) {
-        for (int kb = 0; kb < issued; ++kb) mbar_wait(&full_bar[kb % nst], (uint32_t)(kb / nst) & 1u);
-      }
+      if (abort_sh) drain_copies(full_bar, issued, nst);
     }
   } else if (warp == 1) {
     if (lane == 0) {
       for (int kb = 0; kb < nk; ++kb) {
         const int st = kb % nst;
-        if (!role_wait(&dec_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh)) break;
+        if (!role_wait(&dec_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh, wlim)) break;
         tc_fence_after();
         uint8_t* base = smem + st * lay.stage_bytes;
         const uint32_t bb = smem_u32(base + lay.b);
@@ -708,7 +730,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     for (int kb = 0; kb < nk; ++kb) {
       const int st = kb % nst;
       // warp-uniform outcome: the genotype decode below shuffles across the warp
-      if (!__all_sync(0xffffffffu, role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh))) break;
+      if (!__all_sync(0xffffffffu, role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh, wlim))) break;
       uint8_t* base = smem + st * lay.stage_bytes;
       uint32_t wd[16];
       if (kDense) {
@@ -744,7 +766,7 @@ __global__ void __launch_bounds__(kThreads, 2)
       }
       mbar_arrive(&dec_bar[st]);
     }
-    const bool ok = nk > 0 && role_wait(&acc_bar, 0u, &abort_sh);
+    const bool ok = nk > 0 && role_wait(&acc_bar, 0u, &abort_sh, wlim);
     tc_fence_after();
     const int quarter = warp & 3, chalf = (warp - kDecodeWarp0) >> 2;
     const int i = samp0 + quarter * 32 + lane;
@@ -773,7 +795,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   tc_fence_before();
   __syncthreads();
   if (tid == 0 && abort_sh) *a.err = 1;
-  if (warp == 0) tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
+  cta_release(acc_bar, abort_sh, warp, lane, tmem, (uint32_t)a.tmem_cols);
 }
 
 // ---------------------------------------------------------------------------

@@ -25,6 +25,7 @@ struct GArgs {
                           // kIntSlices slices) or FP32 sums (dense)
   int* err;               // set to 1 when a bounded wait gave up
   int dense;              // 1: FP16 values (FileBinary input) instead of packed codes
+  long long wait_cycles;  // limit of the pipeline waits in SM cycles (0: about 2 s)
 };
 
 // H += X_w^T * Gh for one SNP window (dosage part; k_tc_h_finish adds the
@@ -44,6 +45,7 @@ struct HArgs {
   void* hpart;            // [nsplit][npad][LP]: as GArgs::part
   int* err;
   int dense;              // 1: FP16 values instead of packed codes
+  long long wait_cycles;  // as GArgs::wait_cycles
 };
 
 // H rows of one window: Hx += sum of the split partials + missing-entry terms - c

@@ -6,9 +6,9 @@
 // in-core SNP shuffle of src/RSVD.hpp:61-70 (std::shuffle of 0..M-1 with a
 // default-constructed engine).
 //
-// Built with -ffp-contract=off so that the stream is the same on every host
-// (a reference built with -march=native may contract the polar method's
-// arithmetic into FMAs and differ in the last bits).
+// Built with FP contraction into fused multiply-adds (pcaone_gb300/build.py),
+// as the reference's -march=native / -mcpu=native build contracts the polar
+// method's arithmetic: the drawn matrix equals the reference's bit for bit.
 #include <algorithm>
 #include <cstdint>
 #include <numeric>

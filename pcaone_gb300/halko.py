@@ -80,7 +80,7 @@ class Param:
     tolem: float = 1e-5
     noshuffle: bool = False
     ploidy: int = 2
-    precision: int = capi.PREC_FP32
+    precision: int = capi.PREC_BF16
 
     def finalize(self) -> "Param":
         self.oversamples = max(self.oversamples, self.k)
@@ -147,9 +147,51 @@ class FancyRsvdOpData(RsvdOpData):
     svd = 2
 
 
-def run_pca_with_halko(data: FileBed, params: Param, omega: Optional[np.ndarray] = None):
-    """run_pca_with_halko (src/Halko.cpp:271-320): returns (U, S, V, em_iters);
-    V rows are in the working SNP order, ``data.ctx.perm()`` maps them back."""
+def run_pca_with_halko(data: FileBed, params: Param, omega: Optional[np.ndarray] = None,
+                       fileout: Optional[str] = None, printv: bool = True):
+    """run_pca_with_halko (src/Halko.cpp:271-345): returns (U, S, V, em_iters);
+    V rows are in the working SNP order, ``data.ctx.perm()`` maps them back.
+    With ``fileout`` the text outputs are written as the reference writes them
+    at the end of the run (write_eigs_files below)."""
     if omega is not None:
         data.ctx.set_omega(omega)
-    return data.ctx.run_halko(params.to_c())
+    U, S, V, it = data.ctx.run_halko(params.to_c())
+    if fileout is not None:
+        write_eigs_files(fileout, S, U, V, data.nsnps, data.ctx.perm(), printv=printv)
+    return U, S, V, it
+
+
+def _fmt(x: float) -> str:
+    # a C++ stream at precision 6 in the default float field: printf's %.6g
+    return f"{x:.6g}"
+
+
+def _rows(A: np.ndarray) -> str:
+    return "".join("\t".join(_fmt(x) for x in row) + "\n" for row in np.atleast_2d(A))
+
+
+def write_eigs_files(fileout: str, S: np.ndarray, U: np.ndarray, V: Optional[np.ndarray], nsnps: int,
+                     perm: Optional[np.ndarray] = None, printv: bool = True) -> None:
+    """Data::write_eigs_files (src/Data.cpp:211-240) as run_pca_with_halko calls
+    it (src/Halko.cpp:339): ``.sigvals`` (header ``#N,M``, then S), ``.eigvals``
+    (S^2 / M), ``.eigvecs`` (U, N x k) and, with ``printv``, ``.loadings`` (V,
+    M x k, rows back in the file's SNP order: working row i is SNP perm[i]);
+    tab-separated, 6 significant digits.  The .mbim file (SNP metadata with
+    allele frequencies) is left to the caller, which owns the .bim."""
+    S = np.asarray(S, dtype=np.float64)
+    U = np.asarray(U, dtype=np.float64)
+    with open(fileout + ".sigvals", "w") as f:
+        f.write(f"#{U.shape[0]},{nsnps if V is None else V.shape[0]}\n")
+        f.write(_rows(S[:, None]))
+    with open(fileout + ".eigvals", "w") as f:
+        f.write(_rows((S ** 2 / nsnps)[:, None]))
+    with open(fileout + ".eigvecs", "w") as f:
+        f.write(_rows(U))
+    if printv and V is not None:
+        V = np.asarray(V, dtype=np.float64)
+        if perm is not None and len(perm) == V.shape[0]:
+            Vf = np.empty_like(V)
+            Vf[np.asarray(perm, dtype=np.int64)] = V
+            V = Vf
+        with open(fileout + ".loadings", "w") as f:
+            f.write(_rows(V))

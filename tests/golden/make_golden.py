@@ -3,8 +3,9 @@
 Run in a container that has the reference tree (the fixtures are committed;
 tests never run this):
 
-    make -C oracle ref            # builds oracle/_ref/ref_driver from the reference sources
-    python tests/golden/make_golden.py
+    make -C oracle ref REF=<reference tree>   # builds oracle/_ref/ref_driver
+    python tests/golden/make_golden.py         # all fixtures
+    python tests/golden/make_golden.py --eigs-only   # only tests/golden/eigs/
 
 Each case draws a seeded synthetic PLINK fileset (pcaone_gb300.synthetic),
 runs the reference's RSVD operators through oracle/_ref/ref_driver with the
@@ -143,9 +144,43 @@ def run_projection_case(name: str, model_kw: dict, n_base: int, opts: list) -> d
     return res
 
 
+# the reference's own text outputs (Data::write_eigs_files, src/Data.cpp:211-240:
+# .sigvals, .eigvals = S^2/M, .eigvecs = U, .loadings = V in file SNP order,
+# 6 significant digits) for two of the cases above: shuffled winSVD, and EM
+# (whose outputs pass through flip_UV)
+EIGS_CASES = ("wsvd_n301", "em_wsvd_noshuffle")
+EIGS_DIR = os.path.join(HERE, "eigs")
+
+
+def run_eigs_case(name: str) -> None:
+    kw = dict(CASES[name][0])
+    opts = CASES[name][1]
+    pad_garbage = kw.pop("pad_garbage", False)
+    model = synthetic.draw_population_model(**kw)
+    packed = synthetic.sample_packed_bed(model, pad_garbage=pad_garbage)
+    os.makedirs(EIGS_DIR, exist_ok=True)
+    with tempfile.TemporaryDirectory() as td:
+        prefix = os.path.join(td, name)
+        synthetic.write_plink(prefix, packed, model.nsamples)
+        out = os.path.join(td, "out")
+        os.makedirs(out)
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        subprocess.check_call([DRIVER, out, "--eigs-files", "-b", prefix, "-o", os.path.join(out, name), "-V"] + opts,
+                              env=env)
+        for ext in ("sigvals", "eigvals", "eigvecs", "loadings"):
+            with open(os.path.join(out, name + "." + ext)) as f, open(os.path.join(EIGS_DIR, name + "." + ext),
+                                                                          "w") as g:
+                g.write(f.read())
+    print(name, "text outputs written to", EIGS_DIR)
+
+
 def main() -> None:
     if not os.path.exists(DRIVER):
         sys.exit("build the reference driver first: make -C oracle ref")
+    if "--eigs-only" in sys.argv:
+        for name in EIGS_CASES:
+            run_eigs_case(name)
+        return
     for name, (mkw, opts) in CASES.items():
         res = run_case(name, mkw, opts)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
@@ -158,6 +193,8 @@ def main() -> None:
         res = run_projection_case(name, mkw, nb, opts)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
         print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"], "P2[0]=", res["P2"][0])
+    for name in EIGS_CASES:
+        run_eigs_case(name)
 
 
 if __name__ == "__main__":
