@@ -40,7 +40,14 @@ extern "C" {
                                  (27 bits), exact integer accumulation in TMEM, slices combined
                                  exactly in int64, FP64 epilogue; missing genotypes as an exact
                                  sparse term */
-#define PCAONE_PREC_FP8 2     /* reserved: FP8 e4m3 operands (not built yet) */
+#define PCAONE_PREC_FP8 2     /* FP8 form: the range-finding epochs run tcgen05 kind::f8f6f4 products on
+                                 E4M3 operands (exact dosages; the test matrix and G as two base-16
+                                 integer digits, an 8-bit integer per entry, exact integer
+                                 accumulation); the final epochs run the 27-bit BF16 form: at least two,
+                                 and more (up to 16 beyond maxp) until the leading PCs separated by a
+                                 relative eigen-gap above 5% move by less than 1e-7 (sine of the largest
+                                 principal angle) between two exact epochs.  PLINK input;
+                                 computeGandH alone runs E4M3 epochs */
 #define PCAONE_PREC_BF16X3 3  /* same as PCAONE_PREC_BF16 */
 #define PCAONE_PREC_FP64 4    /* FP64-grade form for checking the other forms (no counterpart in the
                                  reference): the tensor-core form with six slices (54 bits per column:

@@ -787,6 +787,20 @@ __global__ void k_matvec_reduce(const double* __restrict__ ypart, int nsplit, in
   y[i] = s;
 }
 
+// R = Y_n - X_n M for the leading n columns of two orthonormal N x k blocks
+// (row-major, ld k) with M = X_n^T Y_n (n x n, row-major): the part of Y_n's
+// columns outside span(X_n), in FP64
+__global__ void k_subspace_residual(const double* __restrict__ X, const double* __restrict__ Y, int k, int n,
+                                    const double* __restrict__ M, int64_t rows, double* __restrict__ R) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= rows * n) return;
+  const int64_t r = e / n;
+  const int c = (int)(e - r * n);
+  double v = Y[r * k + c];
+  for (int j = 0; j < n; ++j) v = fma(-X[r * k + j], M[j * n + c], v);
+  R[e] = v;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -982,6 +996,14 @@ void launch_mev(const double* X, const double* Y, int64_t rows, int k, double* o
   launch_cross(X, k, k, Y, k, k, rows, 0, W, k, part, nblocks, s);
   k_mev_finish<<<1, 128, 0, s>>>(W, k, out);
   PCAONE_LAUNCH_CHECK();
+}
+
+void launch_subspace_change(const double* X, const double* Y, int64_t rows, int k, int n, double* M, double* R,
+                            double* W, double* part, int nblocks, cudaStream_t s) {
+  launch_cross(X, k, n, Y, k, n, rows, 0, M, n, part, nblocks, s, true);
+  k_subspace_residual<<<ceil_div(rows * n, 256), 256, 0, s>>>(X, Y, k, n, M, rows, R);
+  PCAONE_LAUNCH_CHECK();
+  launch_cross(R, n, n, R, n, n, rows, 1, W, n, part, nblocks, s, true);
 }
 
 void launch_em_fill(const int32_t* epos, const int32_t* sample, double* value, int64_t nnz, const int32_t* perm,

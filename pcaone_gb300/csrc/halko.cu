@@ -135,6 +135,7 @@ struct Context {
   DBuf<double> W, R1, R1i, R2, R2i, R3, R3i, Rt, Rti, UB, sigma, T, tmp, sgn, red, mevv;
   DBuf<int> status, flag;
   DBuf<double> U, Upre, V, Vpre;
+  DBuf<double> rres;  // FP8 form: residual of the leading-PC change
   bool have_usv = false;
   DBuf<double> outbuf;
   DBuf<double> mv_t, mv_ypart, mv_x, mv_y, mv_scale;
@@ -154,9 +155,14 @@ struct Context {
   DBuf<double> cr_part;    // column-reduction partials (tc::kColRedBlocks x LP)
   DBuf<unsigned> cr_cnt;   // its completion counter, zero between launches
   CUtensorMap map_bed_g{}, map_bed_h{}, map_w{}, map_gt{};
+  // the FP8 form's operands: 128-sample / 128-SNP packed tiles, E4M3 digit slices
+  CUtensorMap map_bed_g8{}, map_bed_h8{}, map_w8{}, map_gt8{};
   int ldg = 0, win_max = 0;
   int nslice_cur = 1, w_slices = 0;
   int max_slices = 3;  // slices of the chosen form: 3, or 6 in the FP64-grade form
+  bool fp8_form = false;  // PCAONE_PREC_FP8: E4M3 range-finding epochs, exact final epochs
+  bool fp8_now = false;   // the current epoch runs the E4M3 products
+  int w_mode = -1;        // slices and format of the W slices now held (S * 4 + format)
   long long wait_cycles = 0;  // limit of the tensor-core pipeline waits (0: the kernels' default)
   bool fp64 = false;   // FP64-grade form: the QR and small-SVD kernels in plain FP64 too
 
@@ -412,6 +418,11 @@ static void tc_make_bed_maps(Context& c) {
                   128, false);
   tc::make_map_2d(&c.map_bed_h, c.bed_work, tc::kMapU8, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 32,
                   64, false);
+  // E4M3 form: 128 samples (32 bytes) per G stage, 128 SNP rows per H stage
+  tc::make_map_2d(&c.map_bed_g8, c.bed_work, tc::kMapU8, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 32,
+                  128, false);
+  tc::make_map_2d(&c.map_bed_h8, c.bed_work, tc::kMapU8, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 32,
+                  128, false);
 }
 
 // launch shapes of one window's tensor-core products: G tiles of 128 SNPs x
@@ -419,7 +430,9 @@ static void tc_make_bed_maps(Context& c) {
 // Genotypes (exact integer accumulation, K per CTA <= kMaxKExact): the fewest
 // waves of long CTAs (tc::k_parts).  Dense FP16 input accumulates in FP32, so
 // its error grows with K per CTA: at least 304 CTAs of at most 4096.
-static void tc_shapes(const Context& c, int win, int S, int& chunk, int& nchunks, int& per_split, int& nsplit) {
+static void tc_shapes(const Context& c, int win, int S, bool fp8, int& chunk, int& nchunks, int& per_split,
+                      int& nsplit) {
+  const int gran = fp8 ? 128 : 64;  // K elements per pipeline stage
   if (c.dense) {
     const int xt = ceil_div(win, 128), xh = c.npad / 128;
     chunk = std::min(round_up(ceil_div(c.npad, std::max(1, ceil_div(304, xt))), 64), tc::kMaxKDense);
@@ -427,9 +440,9 @@ static void tc_shapes(const Context& c, int win, int S, int& chunk, int& nchunks
   } else {
     const int slots = tc::cta_slots(c.LP, S, false);
     const int nch = tc::k_parts(ceil_div(win, 128), c.npad, tc::kMaxKExact, slots);
-    chunk = round_up(ceil_div(c.npad, nch), 64);
+    chunk = round_up(ceil_div(c.npad, nch), gran);
     const int nsp = tc::k_parts(c.npad / 128, win, tc::kMaxKExact, slots);
-    per_split = round_up(ceil_div(win, nsp), 64);
+    per_split = round_up(ceil_div(win, nsp), gran);
   }
   nchunks = ceil_div(c.npad, chunk);
   nsplit = ceil_div(win, per_split);
@@ -442,11 +455,13 @@ static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
   size_t need_part = 1, need_hpart = 1;
   for (int64_t n : lens) {
     if (n <= 0) continue;
-    for (int S = 1; S <= 3; ++S) {
-      int ch, nch, per, nsp;
-      tc_shapes(c, (int)n, S, ch, nch, per, nsp);
-      need_part = std::max(need_part, (size_t)nch * n * LP);
-      need_hpart = std::max(need_hpart, (size_t)nsp * c.npad * LP);
+    for (int S = 1; S <= c.max_slices; ++S) {
+      for (int f8 = 0; f8 < 2; ++f8) {
+        int ch, nch, per, nsp;
+        tc_shapes(c, (int)n, S, f8 != 0, ch, nch, per, nsp);
+        need_part = std::max(need_part, (size_t)nch * n * LP);
+        need_hpart = std::max(need_hpart, (size_t)nsp * c.npad * LP);
+      }
     }
   }
   const int smax = c.max_slices;
@@ -479,7 +494,12 @@ static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
   const int sl = c.dense ? tc::kMapF16 : tc::kMapBF16;  // slice digits: FP16 for dense input, else BF16
   tc::make_map_2d(&c.map_w, c.wsl.p, sl, (uint64_t)c.npad, (uint64_t)smax * LP, (uint64_t)c.npad * 2, 64, LP, true);
   tc::make_map_2d(&c.map_gt, c.gt.p, sl, (uint64_t)c.ldg, (uint64_t)smax * LP, (uint64_t)c.ldg * 2, 64, LP, true);
+  // the same buffers seen as rows of E4M3 digits (one byte per K element)
+  tc::make_map_2d(&c.map_w8, c.wsl.p, tc::kMapU8, (uint64_t)c.npad, (uint64_t)smax * LP, (uint64_t)c.npad, 128, LP,
+                  true);
+  tc::make_map_2d(&c.map_gt8, c.gt.p, tc::kMapU8, (uint64_t)c.ldg, (uint64_t)smax * LP, (uint64_t)c.ldg, 128, LP, true);
   c.w_slices = 0;
+  c.w_mode = -1;
 }
 
 static void op_init(Context& c, const pcaone_gpu_params& p) {
@@ -492,8 +512,10 @@ static void op_init(Context& c, const pcaone_gpu_params& p) {
   if (p.svd == PCAONE_SVD_WINDOW && (p.bands < 4 || (p.bands & (p.bands - 1)) != 0))
     throw Error(PCAONE_E_ARG, "the -w/--batches must be a power of 2 and the minimun is 4.");
   if (p.precision != PCAONE_PREC_FP32 && p.precision != PCAONE_PREC_BF16 && p.precision != PCAONE_PREC_BF16X3 &&
-      p.precision != PCAONE_PREC_FP64)
-    throw Error(PCAONE_E_ARG, "precision form not available in this build of the operator");
+      p.precision != PCAONE_PREC_FP64 && p.precision != PCAONE_PREC_FP8)
+    throw Error(PCAONE_E_ARG, "unknown precision form");
+  if (c.dense && p.precision == PCAONE_PREC_FP8)
+    throw Error(PCAONE_E_ARG, "the FP8 form takes PLINK genotypes (dense FP16 values are not E4M3 numbers)");
   if (c.dense && p.precision == PCAONE_PREC_FP32)
     throw Error(PCAONE_E_ARG, "dense (FileBinary) input runs in the tensor-core form only");
   if (c.dense && p.precision == PCAONE_PREC_FP64)
@@ -505,6 +527,8 @@ static void op_init(Context& c, const pcaone_gpu_params& p) {
   c.tc = p.precision != PCAONE_PREC_FP32;
   c.max_slices = p.precision == PCAONE_PREC_FP64 ? tc::kMaxSlices : tc::kIntSlices;
   c.fp64 = p.precision == PCAONE_PREC_FP64;
+  c.fp8_form = p.precision == PCAONE_PREC_FP8;
+  c.fp8_now = c.fp8_form;
   c.LP = c.tc ? round_up(L, 16) : round_up(L, 8);
   c.update = c.standardize = c.scaled = c.fitted = false;
   c.have_usv = false;
@@ -832,13 +856,16 @@ static void prepare_epoch0(Context& c, bool window) {
 // tensor-core form of one window (prod_tc.cu)
 static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   const int LP = c.LP, S = c.nslice_cur;
-  if (c.w_slices != S) {
+  const bool fp8 = c.fp8_now;
+  const int fmt = fp8 ? tc::kFmtE4M3 : c.dense ? tc::kFmtF16 : tc::kFmtBF16;
+  if (c.w_slices != S || c.w_mode != S * 4 + fmt) {
     tc::launch_omega_slices(c.Omg.p, c.npad, c.N, LP, S, c.wsl.p, c.wunit.p, c.colsum.p, c.wexp.p, c.wrep.p,
-                            c.wint.p, c.dense, tc::ColRedScratch{c.cr_part.p, c.cr_cnt.p}, c.stream);
+                            c.wint.p, fmt, tc::ColRedScratch{c.cr_part.p, c.cr_cnt.p}, c.stream);
     c.w_slices = S;
+    c.w_mode = S * 4 + fmt;
   }
   int chunk, nch, per, nsp;
-  tc_shapes(c, (int)n, S, chunk, nch, per, nsp);
+  tc_shapes(c, (int)n, S, fp8, chunk, nch, per, nsp);
   if ((size_t)nch * n * LP > c.tpart.n || (size_t)nsp * c.npad * LP > c.thpart.n || n > c.win_max)
     throw Error(PCAONE_E_ARG, "internal: tensor-core window scratch too small");
   const bool any_miss = c.counts_total_missing > 0;
@@ -867,15 +894,16 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ga.chunk = chunk;
   ga.npad = c.npad;
   ga.nchunks = nch;
-  ga.nstages = tc::stages_for(LP, S, tc::g_tile_bytes(c.dense), c.dense);
+  ga.nstages = tc::stages_for(LP, S, tc::g_tile_bytes(c.dense, fp8), c.dense);
   ga.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ga.nstages, c.dense));
   ga.wscale = c.wunit.p;
   ga.part = c.tpart.p;
   ga.err = c.err.p;
   ga.dense = c.dense ? 1 : 0;
   ga.wait_cycles = c.wait_cycles;
+  ga.fp8 = fp8 ? 1 : 0;
   mark(0);
-  tc::launch_g(c.map_bed_g, c.map_w, ga, c.stream);
+  tc::launch_g(fp8 ? c.map_bed_g8 : c.map_bed_g, fp8 ? c.map_w8 : c.map_w, ga, c.stream);
   close_mark();
   if (any_miss) {
     // f sum_i W_i (and sum_i e_i W_i) over each SNP's missing samples
@@ -903,6 +931,8 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   fa.LP = LP;
   fa.nslice = S;
   fa.nchunks = nch;
+  fa.fmt = fmt;
+  fa.digit_bits = tc::digit_bits_of(fmt);
   // the B operand tensor map spans ldg columns; windows shorter than the
   // longest one leave the tail zeroed by the slicing kernel
   fa.ldg = c.ldg;
@@ -932,13 +962,14 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ha.per_split = per;
   ha.nsplit = nsp;
   ha.npad = c.npad;
-  ha.nstages = tc::stages_for(LP, S, tc::h_tile_bytes(c.dense), c.dense);
+  ha.nstages = tc::stages_for(LP, S, tc::h_tile_bytes(c.dense, fp8), c.dense);
   ha.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ha.nstages, c.dense));
   ha.hscale = c.hunit.p;
   ha.hpart = c.thpart.p;
   ha.err = c.err.p;
   ha.dense = c.dense ? 1 : 0;
   ha.wait_cycles = c.wait_cycles;
+  ha.fp8 = fp8 ? 1 : 0;
   if (any_miss) {
     // sum_j Gm_j (and sum_j 2 e_j Gh_j) over each sample's missing SNPs of the window
     SegGatherArgs sg{};
@@ -958,7 +989,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
     launch_seg_gather(sg, c.stream);
   }
   mark(1);
-  tc::launch_h(c.map_bed_h, c.map_gt, ha, c.stream);
+  tc::launch_h(fp8 ? c.map_bed_h8 : c.map_bed_h, fp8 ? c.map_gt8 : c.map_gt, ha, c.stream);
   close_mark();
   tc::HFinishArgs hf{};
   hf.nsamples = c.N;
@@ -1064,16 +1095,83 @@ static void compute_g_and_h_window(Context& c, int pi) {
   }
 }
 
-// integer slices of the tensor-core forms in every epoch: three (27 bits per
-// column), or six (54 bits) in the FP64-grade form
-static int slices_for_epoch(const Context& c, int pi) {
-  (void)pi;
-  return c.max_slices;
+// integer slices of the tensor-core forms: three (27 bits per column), six
+// (54 bits) in the FP64-grade form, and in the FP8 form's E4M3 epochs two
+// base-16 digits (an 8-bit integer representation)
+static int slices_for_epoch(const Context& c) { return c.fp8_now ? 2 : c.max_slices; }
+
+// The FP8 form runs its range-finding epochs on E4M3 operands and at least
+// kExactEpochs final epochs in the exact 27-bit form; after those it stops
+// only once the leading PCs (those separated from the next by a relative
+// eigen-gap above 5%) are within kFp8Settle of their limit: the change d
+// between two exact epochs (sine of the largest principal angle) times
+// r / (1 - r), with r = (sigma_L / sigma_n)^2 the per-epoch contraction of
+// subspace iteration on the leading n of L columns (sigma_L bounds the first
+// singular value outside the sketch); at most kFp8MaxExtra epochs beyond the
+// schedule's own.
+constexpr int kExactEpochs = 2;
+constexpr double kFp8Settle = 1e-7;
+constexpr int kFp8MaxExtra = 16;
+
+// largest eigenvalue of a small symmetric matrix (row-major n x n), cyclic
+// Jacobi rotations in FP64
+static double sym_max_eig(std::vector<double> a, int n) {
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) off += a[p * n + q] * a[p * n + q];
+    if (off < 1e-300) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = a[p * n + q];
+        if (apq == 0.0) continue;
+        const double theta = (a[q * n + q] - a[p * n + p]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+        for (int r = 0; r < n; ++r) {  // columns p, q
+          const double arp = a[r * n + p], arq = a[r * n + q];
+          a[r * n + p] = cs * arp - sn * arq;
+          a[r * n + q] = sn * arp + cs * arq;
+        }
+        for (int r = 0; r < n; ++r) {  // rows p, q
+          const double apr = a[p * n + r], aqr = a[q * n + r];
+          a[p * n + r] = cs * apr - sn * aqr;
+          a[q * n + r] = sn * apr + cs * aqr;
+        }
+      }
+  }
+  double m = 0.0;
+  for (int i = 0; i < n; ++i) m = std::max(m, a[i * n + i]);
+  return m;
+}
+
+// FP8 form: the predicted distance of the leading well-separated PCs of U
+// (this epoch) from their limit, from their change against Upre (the
+// previous epoch); 0 when no PC is separated from the next
+static double fp8_leading_change(Context& c) {
+  std::vector<double> sg((size_t)c.L);
+  PCAONE_CUDA(cudaMemcpyAsync(sg.data(), c.sigma.p, c.L * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  int n = 0;
+  for (int i = 0; i + 1 < c.k; ++i) {
+    const double e0 = sg[i] * sg[i], e1 = sg[i + 1] * sg[i + 1];
+    if (e0 > 0.0 && (e0 - e1) / e0 > 0.05) n = i + 1;
+  }
+  if (n == 0) return 0.0;
+  const double q = sg[c.L - 1] / sg[n - 1];
+  const double r = std::min(0.999, q * q);
+  c.rres.ensure((size_t)c.npad * n, c.stream, false);
+  launch_subspace_change(c.U.p, c.Upre.p, c.N, c.k, n, c.tmp.p, c.rres.p, c.W.p, c.red.p, cross_blocks(c.N),
+                         c.stream);
+  std::vector<double> w((size_t)n * n);
+  PCAONE_CUDA(cudaMemcpyAsync(w.data(), c.W.p, w.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  return std::sqrt(std::max(0.0, sym_max_eig(w, n))) * r / (1.0 - r);
 }
 
 
 static void compute_g_and_h(Context& c, int pi) {
-  c.nslice_cur = c.tc ? slices_for_epoch(c, pi) : 1;
+  c.nslice_cur = c.tc ? slices_for_epoch(c) : 1;
   if (c.P.svd == PCAONE_SVD_WINDOW)
     compute_g_and_h_window(c, pi);
   else
@@ -1087,8 +1185,16 @@ static int compute_usv(Context& c, int p, double tol) {
   const int N = c.N, L = c.L, LP = c.LP, k = c.k;
   int epochs = 0;
   bool done = false, ucur_in_upre = false;
+  // FP8 form: E4M3 epochs while kExactEpochs epochs remain after them and the
+  // range finder has not converged; then exact epochs, of which at least
+  // kExactEpochs run before the convergence rule may stop the loop
+  bool switched = false;
+  int exact_done = 0;
+  const int p_cap = p + kFp8MaxExtra;
   for (int pi = 0; pi <= p; ++pi) {
     auto t0 = clk::now();
+    c.fp8_now = c.fp8_form && !switched && pi + kExactEpochs <= p;
+    if (!c.fp8_now) ++exact_done;
     compute_g_and_h(c, pi);
     PCAONE_CUDA(cudaStreamSynchronize(c.stream));
     check_tc_err(c);
@@ -1114,6 +1220,16 @@ static int compute_usv(Context& c, int p, double tol) {
       if (diff < tol || pi == p) {
         if (c.P.svd == PCAONE_SVD_WINDOW && std::ldexp(1.0, pi) < c.P.bands) {
           p = (int)std::log2((double)c.P.bands);
+        } else if (c.fp8_form && (c.fp8_now || exact_done < kExactEpochs)) {
+          // the E4M3 range finder has converged (or too few exact epochs ran):
+          // continue with exact epochs
+          switched = true;
+          p = std::max(p, pi + kExactEpochs - (c.fp8_now ? 0 : exact_done));
+          set_upre = true;
+        } else if (c.fp8_form && pi < p_cap && fp8_leading_change(c) > kFp8Settle) {
+          // the leading PCs still move after the E4M3 epochs: one more exact epoch
+          p = std::max(p, pi + 1);
+          set_upre = true;
         } else {
           launch_gemm_tall(c.G.p, M, LP, c.UB.p, LP, k, c.V.p, k, c.stream, c.fp64);  // V = Q2 U_B[:, :k]
           done = true;

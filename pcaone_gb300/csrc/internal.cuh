@@ -190,6 +190,12 @@ void launch_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
 void launch_mult_small(const double* A, const double* B, double* C, int LP, cudaStream_t s);
 void launch_usv_small(const double* Rinv, const double* Wh, int L, int LP, int k, double* UB, double* sigma,
                       double* T, double* tmp, int* status, cudaStream_t s);
+// W = R^T R with R = Y_n - X_n (X_n^T Y_n), the leading n columns of the
+// orthonormal blocks X, Y (rows x k, ld k): the largest eigenvalue of W is the
+// squared sine of the largest principal angle between span(X_n) and
+// span(Y_n).  M (n x n) and R (rows x n) are scratch; FP64 throughout.
+void launch_subspace_change(const double* X, const double* Y, int64_t rows, int k, int n, double* M, double* R,
+                            double* W, double* part, int nblocks, cudaStream_t s);
 void launch_mev(const double* X, const double* Y, int64_t rows, int k, double* out, double* W, double* part,
                 int nblocks, cudaStream_t s);
 void launch_em_fill(const int32_t* epos, const int32_t* sample, double* value, int64_t nnz, const int32_t* perm,

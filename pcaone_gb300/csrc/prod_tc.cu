@@ -49,6 +49,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cuda_fp8.h>
+
 #include <algorithm>
 #include <cstring>
 
@@ -233,6 +235,23 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
 __host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
   return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
+// Instruction descriptor, kind::f8f6f4: D FP32, A and B both E4M3 (format 0),
+// both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_e4m3(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// D[tmem] (+)= A[tmem] * B[smem desc]^T, kind::f8f6f4 (E4M3); A rows = TMEM
+// lanes, four E4M3 K elements per 32-bit column
+__device__ __forceinline__ void mma_e4m3_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
+                                            uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
 
 
 // SWAR decode of two 2-bit codes held at bits 0-1 and 16-17 of x into two BF16
@@ -256,6 +275,21 @@ __device__ __forceinline__ void lut_init(uint32_t* lut, int tid, int nthreads) {
     const uint32_t n = (uint32_t)i >> 5;
     lut[i] = dosage_pair((n & 3u) | (((n >> 2) & 3u) << 16));
   }
+}
+
+// The FP8 form's table: the two E4M3 dosages of a 4-bit pair of codes (low
+// byte from the code in bits 0-1): 00 -> 2.0 (0x40), 10 -> 1.0 (0x38), 01
+// (missing) and 11 -> 0; 32 copies laid out as lut_init's.  dec8 turns a
+// packed byte (four codes) into four E4M3 dosages, first code in the low byte.
+__device__ __forceinline__ uint32_t e4m3_dosage(uint32_t code) { return code == 0u ? 0x40u : code == 2u ? 0x38u : 0u; }
+__device__ __forceinline__ void lut_init8(uint32_t* lut, int tid, int nthreads) {
+  for (int i = tid; i < kLutWords; i += nthreads) {
+    const uint32_t n = (uint32_t)i >> 5;
+    lut[i] = e4m3_dosage(n & 3u) | (e4m3_dosage((n >> 2) & 3u) << 8);
+  }
+}
+__device__ __forceinline__ uint32_t dec8(const uint32_t* lut_l, uint32_t byte) {
+  return lut_l[(byte & 15u) << 5] | (lut_l[((byte >> 4) & 15u) << 5] << 16);
 }
 
 // One stage of a warp transpose of a 32 x 32 matrix of 2-bit codes held as
@@ -319,18 +353,29 @@ __host__ __device__ inline SmemLayout layout_for(int LP, int nslice, int pbytes,
 // MMA shape limit for M = 128: N <= 256 columns.
 constexpr int kMaxNTmemA = 256;
 
+// Kernel forms: genotypes with BF16 operands (dosages in TMEM), dense FP16
+// values (A in shared memory), genotypes with E4M3 operands (the FP8 form).
+// A pipeline stage covers 64 K elements of 16-bit operands or 128 of 8-bit
+// ones: 128-byte rows of B either way, 32 TMEM columns of A, four MMAs of 32
+// bytes of K.
+constexpr int kModeGeno = 0, kModeDense = 1, kModeGeno8 = 2;
+
 // a_addr: TMEM address of the A operand (!kASmem) or its shared-memory
 // address (kASmem)
-template <bool kF16, bool kASmem>
+template <int kMode, bool kASmem>
 __device__ __forceinline__ void mma_cat(uint32_t tmem_col0, uint32_t a_addr, uint32_t b_addr, int ncols,
                                         uint32_t accumulate) {
   for (int n0 = 0; n0 < ncols; n0 += kMaxNTmemA) {
     const int n = min(kMaxNTmemA, ncols - n0);
-    const uint32_t id = kF16 ? idesc_f16(128, n) : idesc_bf16(128, n);
-    if constexpr (kASmem)
-      mma_bf16_ss(tmem_col0 + n0, desc_sw128(a_addr), desc_sw128(b_addr + n0 * 128), id, accumulate);
-    else
-      mma_bf16_ta(tmem_col0 + n0, a_addr, desc_sw128(b_addr + n0 * 128), id, accumulate);
+    if constexpr (kMode == kModeGeno8) {
+      mma_e4m3_ta(tmem_col0 + n0, a_addr, desc_sw128(b_addr + n0 * 128), idesc_e4m3(128, n), accumulate);
+    } else {
+      const uint32_t id = kMode == kModeDense ? idesc_f16(128, n) : idesc_bf16(128, n);
+      if constexpr (kASmem)
+        mma_bf16_ss(tmem_col0 + n0, desc_sw128(a_addr), desc_sw128(b_addr + n0 * 128), id, accumulate);
+      else
+        mma_bf16_ta(tmem_col0 + n0, a_addr, desc_sw128(b_addr + n0 * 128), id, accumulate);
+    }
   }
 }
 
@@ -393,13 +438,15 @@ __device__ __forceinline__ void cta_release(uint64_t& acc_bar, volatile int& abo
 //
 // Genotype input: each slice sum is an exact integer (|v| <= 512 K <= 2^23),
 // so the slices combine exactly in int64, in units of the last slice:
-//   P = sum_s v_s 512^(S-1-s)   (|P| < 2^42 for S = 3)
-__device__ __forceinline__ void combine_slices_exact(uint32_t lane_base, int c0, int LP, int S, long long* acc) {
+//   P = sum_s v_s B^(S-1-s)   (digit base B = 2^db: 512, or 16 in the FP8
+//   form; |P| < 2^42 for three 9-bit slices)
+__device__ __forceinline__ void combine_slices_exact(uint32_t lane_base, int c0, int LP, int S, long long* acc,
+                                                     int db) {
   float v[8];
   for (int s = 0; s < S; ++s) {
     tmem_ld8(lane_base + s * LP + c0, v);
 #pragma unroll
-    for (int t = 0; t < 8; ++t) acc[t] = acc[t] * (1 << kDigitBits) + __float2ll_rn(v[t]);
+    for (int t = 0; t < 8; ++t) acc[t] = acc[t] * (1 << db) + __float2ll_rn(v[t]);
   }
 }
 // Dense input: slice sums times their power-of-two units, smallest units first
@@ -449,12 +496,14 @@ __device__ __forceinline__ void store_i64x8(long long* dst, const long long* v) 
 // ---------------------------------------------------------------------------
 // G product
 // ---------------------------------------------------------------------------
-template <bool kDense>
+template <int kMode>
 __global__ void __launch_bounds__(kThreads, 2)
     k_tc_g(const __grid_constant__ CUtensorMap map_bed, const __grid_constant__ CUtensorMap map_w, GArgs a) {
-  // A tile per stage: 128 SNP rows x 64 samples, packed (16 B per row) or FP16
-  // (128 B per row, 128-byte swizzle)
-  constexpr int kTileBytes = kDense ? 128 * 128 : 128 * 16;
+  constexpr bool kDense = kMode == kModeDense, kFp8 = kMode == kModeGeno8;
+  constexpr int kK = kFp8 ? 128 : kStepK;  // K elements (samples) per stage
+  // A tile per stage: 128 SNP rows x kK samples, packed (kK/4 B per row) or
+  // FP16 (128 B per row, 128-byte swizzle)
+  constexpr int kTileBytes = kDense ? 128 * 128 : 128 * (kK / 4);
   constexpr bool kASmem = kDense;  // A operand in shared memory (else TMEM)
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -467,10 +516,13 @@ __global__ void __launch_bounds__(kThreads, 2)
   const int LP = a.LP, S = a.nslice;
   const SmemLayout lay = layout_for(LP, S, kTileBytes, kASmem);
   const int row0 = blockIdx.x * 128;
-  if (!kDense) lut_init(lut, tid, kThreads);                  // window-local first SNP of the tile
+  if (kFp8)
+    lut_init8(lut, tid, kThreads);
+  else if (!kDense)
+    lut_init(lut, tid, kThreads);
   const int kbeg = blockIdx.y * a.chunk;
   const int kend = min(kbeg + a.chunk, a.npad);
-  const int nk = (kend - kbeg + kStepK - 1) / kStepK;
+  const int nk = (kend - kbeg + kK - 1) / kK;
   const int nst = a.nstages;
   const int ncat = S * LP;  // slices concatenated along N
   const long long wlim = a.wait_cycles > 0 ? a.wait_cycles : kTimeoutCycles;
@@ -503,14 +555,14 @@ __global__ void __launch_bounds__(kThreads, 2)
       const int kdiv = kDense ? 0 : 2;  // inner TMA coordinate: samples, or packed bytes
       int issued = 0;
       for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
-        tma_prefetch_2d(&map_bed, (kbeg + kb * kStepK) >> kdiv, (int)(a.pos0 + row0));
+        tma_prefetch_2d(&map_bed, (kbeg + kb * kK) >> kdiv, (int)(a.pos0 + row0));
       for (int kb = 0; kb < nk; ++kb) {
         const int st = kb % nst;
         if (kb + kPrefetchSteps < nk)
-          tma_prefetch_2d(&map_bed, (kbeg + (kb + kPrefetchSteps) * kStepK) >> kdiv, (int)(a.pos0 + row0));
+          tma_prefetch_2d(&map_bed, (kbeg + (kb + kPrefetchSteps) * kK) >> kdiv, (int)(a.pos0 + row0));
         if (kb >= nst && !role_wait(&empty_bar[st], (uint32_t)(kb / nst - 1) & 1u, &abort_sh, wlim)) break;
         uint8_t* base = smem + st * lay.stage_bytes;
-        const int k0 = kbeg + kb * kStepK;
+        const int k0 = kbeg + kb * kK;
         mbar_expect_tx(&full_bar[st], tx_bytes);
         tma_load_2d(base + lay.p, &map_bed, k0 >> kdiv, (int)(a.pos0 + row0), &full_bar[st]);
         for (int s = 0; s < S; ++s) tma_load_2d(base + lay.b + s * LP * 128, &map_w, k0, s * LP, &full_bar[st]);
@@ -530,13 +582,13 @@ __global__ void __launch_bounds__(kThreads, 2)
         if constexpr (kASmem) {
           const uint32_t aa = smem_u32(base + lay.a);
 #pragma unroll
-          for (int kk = 0; kk < kStepK / 16; ++kk)
-            mma_cat<kDense, true>(tmem, aa + kk * 32, bb + kk * 32, ncat, (kb | kk) != 0);
+          for (int kk = 0; kk < 4; ++kk)
+            mma_cat<kMode, true>(tmem, aa + kk * 32, bb + kk * 32, ncat, (kb | kk) != 0);
         } else {
           const uint32_t ad = tmem + a_col0 + st * 32;
 #pragma unroll
-          for (int kk = 0; kk < kStepK / 16; ++kk)
-            mma_cat<kDense, false>(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
+          for (int kk = 0; kk < 4; ++kk)
+            mma_cat<kMode, false>(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
         }
         mma_commit(&empty_bar[st]);
       }
@@ -568,6 +620,13 @@ __global__ void __launch_bounds__(kThreads, 2)
           wd[4 * q + 2] = v.z;
           wd[4 * q + 3] = v.w;
         }
+      } else if (kFp8) {
+        // samples 64ch .. 64ch+63 of the step: 16 packed bytes, one per word
+        const uint4 pk = *reinterpret_cast<const uint4*>(base + lay.p + r * 32 + ch * 16);
+        const uint32_t pw[4] = {pk.x, pk.y, pk.z, pk.w};
+        const uint32_t* lut_l = lut + lane;
+#pragma unroll
+        for (int e = 0; e < 16; ++e) wd[e] = dec8(lut_l, pw[e >> 2] >> (8 * (e & 3)));
       } else {
         const uint2 pk = *reinterpret_cast<const uint2*>(base + lay.p + r * 16 + ch * 8);
         const uint32_t* lut_l = lut + lane;
@@ -607,7 +666,7 @@ __global__ void __launch_bounds__(kThreads, 2)
           const size_t off = ((size_t)blockIdx.y * a.nsnp + j) * LP + c0;
           if (S <= kIntSlices) {
             long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            if (ok) combine_slices_exact(lane_base, c0, LP, S, acc);
+            if (ok) combine_slices_exact(lane_base, c0, LP, S, acc, kFp8 ? kDigitBits8 : kDigitBits);
             if (j < a.nsnp) store_i64x8(reinterpret_cast<long long*>(a.part) + off, acc);
           } else {
             double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -627,13 +686,15 @@ __global__ void __launch_bounds__(kThreads, 2)
 // ---------------------------------------------------------------------------
 // H product
 // ---------------------------------------------------------------------------
-template <bool kDense>
+template <int kMode>
 __global__ void __launch_bounds__(kThreads, 2)
     k_tc_h(const __grid_constant__ CUtensorMap map_bed, const __grid_constant__ CUtensorMap map_g, HArgs a) {
-  // A tile per stage: 64 SNP rows x 128 samples, packed (32 B per row) or FP16
+  constexpr bool kDense = kMode == kModeDense, kFp8 = kMode == kModeGeno8;
+  constexpr int kK = kFp8 ? 128 : kStepK;  // K elements (SNPs) per stage
+  // A tile per stage: kK SNP rows x 128 samples, packed (32 B per row) or FP16
   // (256 B per row, unswizzled)
   constexpr int kRowBytes = kDense ? 256 : 32;
-  constexpr int kTileBytes = 64 * kRowBytes;
+  constexpr int kTileBytes = kK * kRowBytes;
   constexpr bool kASmem = kDense;  // A operand in shared memory (else TMEM)
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -643,13 +704,16 @@ __global__ void __launch_bounds__(kThreads, 2)
   __shared__ float unit[3 * 112];
   __shared__ uint32_t lut[kDense ? 1 : kLutWords];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  if (!kDense) lut_init(lut, tid, kThreads);
+  if (kFp8)
+    lut_init8(lut, tid, kThreads);
+  else if (!kDense)
+    lut_init(lut, tid, kThreads);
   const int LP = a.LP, S = a.nslice;
   const SmemLayout lay = layout_for(LP, S, kTileBytes, kASmem);
   const int samp0 = blockIdx.x * 128;
   const int jb = blockIdx.y * a.per_split;
   const int je = min(jb + a.per_split, a.nsnp);
-  const int nk = je > jb ? (je - jb + kStepK - 1) / kStepK : 0;
+  const int nk = je > jb ? (je - jb + kK - 1) / kK : 0;
   const int nst = a.nstages;
   const int ncat = S * LP;
   const long long wlim = a.wait_cycles > 0 ? a.wait_cycles : kTimeoutCycles;
@@ -681,14 +745,14 @@ __global__ void __launch_bounds__(kThreads, 2)
       const int scol = kDense ? samp0 : (samp0 >> 2);  // inner TMA coordinate
       int issued = 0;
       for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
-        tma_prefetch_2d(&map_bed, scol, (int)(a.pos0 + jb + kb * kStepK));
+        tma_prefetch_2d(&map_bed, scol, (int)(a.pos0 + jb + kb * kK));
       for (int kb = 0; kb < nk; ++kb) {
         const int st = kb % nst;
         if (kb + kPrefetchSteps < nk)
-          tma_prefetch_2d(&map_bed, scol, (int)(a.pos0 + jb + (kb + kPrefetchSteps) * kStepK));
+          tma_prefetch_2d(&map_bed, scol, (int)(a.pos0 + jb + (kb + kPrefetchSteps) * kK));
         if (kb >= nst && !role_wait(&empty_bar[st], (uint32_t)(kb / nst - 1) & 1u, &abort_sh, wlim)) break;
         uint8_t* base = smem + st * lay.stage_bytes;
-        const int j0 = jb + kb * kStepK;
+        const int j0 = jb + kb * kK;
         mbar_expect_tx(&full_bar[st], tx_bytes);
         tma_load_2d(base + lay.p, &map_bed, scol, (int)(a.pos0 + j0), &full_bar[st]);
         for (int r = 0; r < S; ++r) tma_load_2d(base + lay.b + r * LP * 128, &map_g, j0, r * LP, &full_bar[st]);
@@ -707,13 +771,13 @@ __global__ void __launch_bounds__(kThreads, 2)
         if constexpr (kASmem) {
           const uint32_t aa = smem_u32(base + lay.a);
 #pragma unroll
-          for (int kk = 0; kk < kStepK / 16; ++kk)
-            mma_cat<kDense, true>(tmem, aa + kk * 32, bb + kk * 32, ncat, (kb | kk) != 0);
+          for (int kk = 0; kk < 4; ++kk)
+            mma_cat<kMode, true>(tmem, aa + kk * 32, bb + kk * 32, ncat, (kb | kk) != 0);
         } else {
           const uint32_t ad = tmem + a_col0 + st * 32;
 #pragma unroll
-          for (int kk = 0; kk < kStepK / 16; ++kk)
-            mma_cat<kDense, false>(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
+          for (int kk = 0; kk < 4; ++kk)
+            mma_cat<kMode, false>(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
         }
         mma_commit(&empty_bar[st]);
       }
@@ -741,6 +805,20 @@ __global__ void __launch_bounds__(kThreads, 2)
         for (int e = 0; e < 16; ++e) {
           const uint32_t v0 = pt[(ch * 32 + 2 * e) * 128], v1 = pt[(ch * 32 + 2 * e + 1) * 128];
           wd[e] = v0 | (v1 << 16);
+        }
+      } else if (kFp8) {
+        // SNP rows 64ch .. 64ch+63 of the step in two blocks of 32: lane l loads
+        // row 64ch + 32t + l of the warp's 32 samples; after the transpose lane
+        // r holds sample r's 32 codes, byte q of lo / hi = rows 4q .. 4q+3 /
+        // 16+4q .. 16+4q+3, one E4M3 word each
+        const uint32_t* lut_l = lut + lane;
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+          const uint2 rowv = *reinterpret_cast<const uint2*>(base + lay.p + (ch * 64 + t * 32 + lane) * 32 + q4 * 8);
+          uint32_t lo = rowv.x, hi = rowv.y;
+          xpose2_warp(lo, hi, lane);
+#pragma unroll
+          for (int e = 0; e < 8; ++e) wd[8 * t + e] = dec8(lut_l, (e < 4 ? lo : hi) >> (8 * (e & 3)));
         }
       } else {
         // lane l loads SNP row 32ch + l of the warp's 32 samples (8 bytes); the
@@ -781,7 +859,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         } else {
           if (S <= kIntSlices) {
             long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            if (ok) combine_slices_exact(lane_base, c0, LP, S, acc);
+            if (ok) combine_slices_exact(lane_base, c0, LP, S, acc, kFp8 ? kDigitBits8 : kDigitBits);
             store_i64x8(reinterpret_cast<long long*>(a.hpart) + row * LP + c0, acc);
           } else {
             double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -866,31 +944,36 @@ __global__ void __launch_bounds__(256) k_colred(const double* __restrict__ A, in
   if (tid == 0) *cnt = 0u;
 }
 
-// Split v (|v| < 2^E) into S integer slices (S <= kMaxSlices): m = rint(v *
-// 2^(9S-1-E)) has |m| <= 2^(9S-1) (at most 2^53: exact in FP64), and its
-// balanced base-512 digits w_s (m = sum_s w_s 512^(S-1-s), |w_s| <= 256, exact
-// in BF16) are the slices, with units u_s = 2^(E-8-9s).  Returns the
-// represented value m * u_(S-1).  Integer digit arithmetic keeps the FP64 work
-// to one multiply and one conversion.  The digits are stored as BF16 or (f16)
-// FP16 bit patterns, exact in both.  *m_out (optional) receives the integer
-// the sparse terms use: m itself for S <= kIntSlices, else the rounding of v
-// to kIntSlices slices (27 bits; unit u_(kIntSlices-1)).
-__device__ __forceinline__ uint16_t digit_bits(int w, bool f16) {
-  return f16 ? __half_as_ushort(__int2half_rn(w)) : __bfloat16_as_ushort(__float2bfloat16_rn((float)w));
+// Split v (|v| < 2^E) into S integer slices of db-bit digits: m = rint(v *
+// 2^(db*S-1-E)) has |m| <= 2^(db*S-1) (at most 2^53: exact in FP64), and its
+// balanced base-2^db digits w_s (m = sum_s w_s 2^(db(S-1-s)), |w_s| <= 2^(db-1))
+// are the slices, with units u_s = 2^(E-(db-1)-db*s).  Returns the represented
+// value m * u_(S-1).  Integer digit arithmetic keeps the FP64 work to one
+// multiply and one conversion.  The digits are stored in the operand format:
+// BF16 or FP16 (db = 9, |w| <= 256) or E4M3 (db = 4, |w| <= 8), exact in each.
+// *m_out (optional) receives the integer the sparse terms use: m itself for
+// S <= kIntSlices, else the rounding of v to kIntSlices slices (27 bits; unit
+// u_(kIntSlices-1)).
+__device__ __forceinline__ void put_digit(uint16_t* dst, int w, int fmt) {
+  *dst = fmt == kFmtF16 ? __half_as_ushort(__int2half_rn(w)) : __bfloat16_as_ushort(__float2bfloat16_rn((float)w));
 }
-__device__ __forceinline__ double split_store(double v, int E, int S, uint16_t* dst, size_t slice_stride, bool f16,
+__device__ __forceinline__ void put_digit(uint8_t* dst, int w, int) {
+  *dst = (uint8_t)__nv_cvt_float_to_fp8((float)w, __NV_SATFINITE, __NV_E4M3);
+}
+template <class D>
+__device__ __forceinline__ double split_store(double v, int E, int S, int db, D* dst, size_t slice_stride, int fmt,
                                               int* m_out = nullptr) {
-  constexpr long long kBase = 1 << kDigitBits, kHalf = kBase / 2;
-  const long long m = __double2ll_rn(v * exp2i(kDigitBits * S - 1 - E));
-  if (m_out) *m_out = S <= kIntSlices ? (int)m : __double2int_rn(v * exp2i(kDigitBits * kIntSlices - 1 - E));
+  const long long kBase = 1ll << db, kHalf = kBase / 2;
+  const long long m = __double2ll_rn(v * exp2i(db * S - 1 - E));
+  if (m_out) *m_out = S <= kIntSlices ? (int)m : __double2int_rn(v * exp2i(db * kIntSlices - 1 - E));
   long long rest = m;
   for (int s = S - 1; s > 0; --s) {
     const long long w = ((rest + kHalf) & (kBase - 1)) - kHalf;
-    dst[(size_t)s * slice_stride] = digit_bits((int)w, f16);
+    put_digit(dst + (size_t)s * slice_stride, (int)w, fmt);
     rest = (rest - w) / kBase;  // exact: rest - w is a multiple of the base
   }
-  dst[0] = digit_bits((int)rest, f16);
-  return (double)m * exp2i(E - kDigitBits * S + 1);
+  put_digit(dst, (int)rest, fmt);
+  return (double)m * exp2i(E - db * S + 1);
 }
 
 // W slices of Omega (S*LP rows x npad, K-major) and the represented W, in FP64
@@ -899,10 +982,11 @@ __device__ __forceinline__ double split_store(double v, int E, int S, uint16_t* 
 // represented values), keeps their digits in shared memory and writes each
 // slice row's 32 digits as one 64-byte run.  npad is a multiple of 32.
 constexpr int kOmgRows = 32;
+template <class D>
 __global__ void __launch_bounds__(256) k_omega_slices(const double* __restrict__ omg, int npad, int N, int LP, int S,
-                                                      const int* __restrict__ E, uint16_t* __restrict__ w,
-                                                      double* __restrict__ rep, int32_t* __restrict__ wint, int f16) {
-  __shared__ uint16_t dg[kMaxSlices * 112 * kOmgRows];  // [s][l][row]
+                                                      int db, const int* __restrict__ E, D* __restrict__ w,
+                                                      double* __restrict__ rep, int32_t* __restrict__ wint, int fmt) {
+  __shared__ D dg[kMaxSlices * 112 * kOmgRows];  // [s][l][row]
   const int i0 = blockIdx.x * kOmgRows;
   for (int e = threadIdx.x; e < kOmgRows * LP; e += blockDim.x) {
     const int il = e / LP, l = e % LP;
@@ -910,7 +994,7 @@ __global__ void __launch_bounds__(256) k_omega_slices(const double* __restrict__
     const size_t idx = (size_t)i * LP + l;
     const double v = i < N ? omg[idx] : 0.0;
     int m = 0;
-    const double r = split_store(v, E[l], S, dg + l * kOmgRows + il, (size_t)LP * kOmgRows, f16 != 0, &m);
+    const double r = split_store(v, E[l], S, db, dg + l * kOmgRows + il, (size_t)LP * kOmgRows, fmt, &m);
     rep[idx] = r;
     wint[idx] = m;
   }
@@ -921,11 +1005,11 @@ __global__ void __launch_bounds__(256) k_omega_slices(const double* __restrict__
   }
 }
 
-__global__ void k_units(const int* __restrict__ E, int LP, int S, int eoff, double* __restrict__ unit) {
+__global__ void k_units(const int* __restrict__ E, int LP, int S, int db, int eoff, double* __restrict__ unit) {
   const int idx = threadIdx.x + blockIdx.x * blockDim.x;
   if (idx >= S * LP) return;
   const int s = idx / LP, l = idx % LP;
-  unit[idx] = ldexp(1.0, E[l] + eoff - (kDigitBits - 1) - kDigitBits * s);
+  unit[idx] = ldexp(1.0, E[l] + eoff - (db - 1) - db * s);
 }
 
 // G rows of the window: FP64 sum of the chunk partials, the centring term, and
@@ -996,19 +1080,21 @@ __global__ void k_tc_g_finish(GFinishArgs a) {
 // missing-entry terms of H use the same represented Gm.  With more than
 // kIntSlices slices (the 54-bit form) c takes 2 f Gh at full precision
 // instead, and only the missing entries use the 27-bit Gm.
+template <class D>
 __global__ void k_tc_gh_slices(GFinishArgs a, const int* __restrict__ Eh) {
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (idx >= (int64_t)a.ldg * a.LP) return;
   const int j = (int)(idx / a.LP), l = (int)(idx % a.LP);
   const int S = a.nslice, LP = a.LP;
   const size_t sstride = (size_t)LP * a.ldg;
-  uint16_t* dh = reinterpret_cast<uint16_t*>(a.gt) + (size_t)l * a.ldg + j;
+  D* dh = reinterpret_cast<D*>(a.gt) + (size_t)l * a.ldg + j;
   const bool f16 = a.vfac == 1.0;  // dense input: FP16 operands
+  const int db = a.digit_bits;
   if (j < a.nsnp && l < a.L) {
     const int64_t pos = a.pos0 + j;
     const int64_t snp = a.perm ? (int64_t)a.perm[pos] : pos;
     int mh = 0;
-    const double ghq = split_store(a.gh[(size_t)j * LP + l], Eh[l], S, dh, sstride, f16, &mh);
+    const double ghq = split_store(a.gh[(size_t)j * LP + l], Eh[l], S, db, dh, sstride, a.fmt, &mh);
     a.ghint[(size_t)j * LP + l] = mh;
     if (f16) {
       // dense: c = sum_j mu_j Gh_j (no missing entries)
@@ -1017,9 +1103,9 @@ __global__ void k_tc_gh_slices(GFinishArgs a, const int* __restrict__ Eh) {
     } else {
       const int e = Eh[l] + 1, Si = min(S, kIntSlices);
       const double gm = 2.0 * a.F[snp] * ghq;
-      const int m = __double2int_rn(gm * exp2i(kDigitBits * Si - 1 - e));
+      const int m = __double2int_rn(gm * exp2i(db * Si - 1 - e));
       a.gmint[(size_t)j * LP + l] = m;
-      a.cpart[(size_t)j * LP + l] = S > kIntSlices ? gm : (double)m * exp2i(e - kDigitBits * Si + 1);
+      a.cpart[(size_t)j * LP + l] = S > kIntSlices ? gm : (double)m * exp2i(e - db * Si + 1);
     }
   } else {
     for (int s = 0; s < S; ++s) dh[s * sstride] = 0;
@@ -1195,38 +1281,43 @@ int tmem_cols_for(int ncols) {
   return c;
 }
 
-template <bool kDense>
+template <int kMode>
 void launch_g_t(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs& a, size_t smem, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    PCAONE_CUDA(cudaFuncSetAttribute(k_tc_g<kDense>, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
+    PCAONE_CUDA(cudaFuncSetAttribute(k_tc_g<kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
     attr = true;
   }
   dim3 grid((a.nsnp + 127) / 128, a.nchunks);
-  k_tc_g<kDense><<<grid, kThreads, smem, s>>>(map_bed, map_w, a);
+  k_tc_g<kMode><<<grid, kThreads, smem, s>>>(map_bed, map_w, a);
 }
 
-template <bool kDense>
+template <int kMode>
 void launch_h_t(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs& a, size_t smem, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    PCAONE_CUDA(cudaFuncSetAttribute(k_tc_h<kDense>, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
+    PCAONE_CUDA(cudaFuncSetAttribute(k_tc_h<kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
     attr = true;
   }
   dim3 grid(a.npad / 128, a.nsplit);
-  k_tc_h<kDense><<<grid, kThreads, smem, s>>>(map_bed, map_g, a);
+  k_tc_h<kMode><<<grid, kThreads, smem, s>>>(map_bed, map_g, a);
 }
 
 void launch_g(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArgs& a, cudaStream_t s) {
   if (a.nstages < 1 || a.nstages > kMaxStages || a.tmem_cols > 512 ||
       a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.nstages, a.dense != 0))
     throw Error(-6, "tensor-core G product: pipeline plan exceeds TMEM or the stage limit");
-  const size_t smem = smem_bytes(a.LP, a.nslice, g_tile_bytes(a.dense != 0), a.nstages, a.tmem_cols, a.dense != 0);
+  const size_t smem =
+      smem_bytes(a.LP, a.nslice, g_tile_bytes(a.dense != 0, a.fp8 != 0), a.nstages, a.tmem_cols, a.dense != 0);
   if (smem > 214 * 1024) throw Error(-6, "tensor-core G product: pipeline plan exceeds shared memory");
+  if (a.dense && a.fp8) throw Error(-1, "tensor-core G product: no E4M3 form for dense input");
+  if (a.fp8 && a.chunk % 128 != 0) throw Error(-1, "tensor-core G product: E4M3 chunks must hold whole 128-sample stages");
   if (a.dense)
-    launch_g_t<true>(map_bed, map_w, a, smem, s);
+    launch_g_t<kModeDense>(map_bed, map_w, a, smem, s);
+  else if (a.fp8)
+    launch_g_t<kModeGeno8>(map_bed, map_w, a, smem, s);
   else
-    launch_g_t<false>(map_bed, map_w, a, smem, s);
+    launch_g_t<kModeGeno>(map_bed, map_w, a, smem, s);
   PCAONE_LAUNCH_CHECK();
 }
 
@@ -1234,12 +1325,18 @@ void launch_h(const CUtensorMap& map_bed, const CUtensorMap& map_g, const HArgs&
   if (a.nstages < 1 || a.nstages > kMaxStages || a.tmem_cols > 512 ||
       a.tmem_cols < tmem_cols_needed(a.LP, a.nslice, a.nstages, a.dense != 0))
     throw Error(-6, "tensor-core H product: pipeline plan exceeds TMEM or the stage limit");
-  const size_t smem = smem_bytes(a.LP, a.nslice, h_tile_bytes(a.dense != 0), a.nstages, a.tmem_cols, a.dense != 0);
+  const size_t smem =
+      smem_bytes(a.LP, a.nslice, h_tile_bytes(a.dense != 0, a.fp8 != 0), a.nstages, a.tmem_cols, a.dense != 0);
   if (smem > 214 * 1024) throw Error(-6, "tensor-core H product: pipeline plan exceeds shared memory");
+  if (a.dense && a.fp8) throw Error(-1, "tensor-core H product: no E4M3 form for dense input");
+  if (a.fp8 && a.per_split % 128 != 0)
+    throw Error(-1, "tensor-core H product: E4M3 splits must hold whole 128-SNP stages");
   if (a.dense)
-    launch_h_t<true>(map_bed, map_g, a, smem, s);
+    launch_h_t<kModeDense>(map_bed, map_g, a, smem, s);
+  else if (a.fp8)
+    launch_h_t<kModeGeno8>(map_bed, map_g, a, smem, s);
   else
-    launch_h_t<false>(map_bed, map_g, a, smem, s);
+    launch_h_t<kModeGeno>(map_bed, map_g, a, smem, s);
   PCAONE_LAUNCH_CHECK();
 }
 
@@ -1262,15 +1359,20 @@ void launch_colred(const double* A, int64_t rows, int LP, const ColRedScratch& c
   PCAONE_LAUNCH_CHECK();
 }
 
-void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv_bfloat16* w, double* wunit,
-                         double* colsum, int* E, double* rep, int32_t* wint, bool f16, const ColRedScratch& cr,
+void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, void* w, double* wunit,
+                         double* colsum, int* E, double* rep, int32_t* wint, int fmt, const ColRedScratch& cr,
                          cudaStream_t s) {
   launch_colred<true>(omg, N, LP, cr, nullptr, E, s);
   if (npad % kOmgRows != 0 || S > kMaxSlices || LP > 112) throw Error(-6, "test-matrix slices: unsupported shape");
-  k_omega_slices<<<npad / kOmgRows, 256, 0, s>>>(omg, npad, N, LP, S, E, reinterpret_cast<uint16_t*>(w), rep, wint,
-                                                 f16 ? 1 : 0);
+  const int db = digit_bits_of(fmt);
+  if (fmt == kFmtE4M3)
+    k_omega_slices<uint8_t><<<npad / kOmgRows, 256, 0, s>>>(omg, npad, N, LP, S, db, E, reinterpret_cast<uint8_t*>(w),
+                                                           rep, wint, fmt);
+  else
+    k_omega_slices<uint16_t><<<npad / kOmgRows, 256, 0, s>>>(omg, npad, N, LP, S, db, E,
+                                                            reinterpret_cast<uint16_t*>(w), rep, wint, fmt);
   PCAONE_LAUNCH_CHECK();
-  k_units<<<ceil_div(S * LP, 128), 128, 0, s>>>(E, LP, S, 0, wunit);
+  k_units<<<ceil_div(S * LP, 128), 128, 0, s>>>(E, LP, S, db, 0, wunit);
   PCAONE_LAUNCH_CHECK();
   launch_colred<false>(rep, N, LP, cr, colsum, nullptr, s);
 }
@@ -1280,11 +1382,14 @@ void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* gmuni
   k_tc_g_finish<<<ceil_div((int64_t)a.nsnp * a.LP, 256), 256, 0, s>>>(a);
   PCAONE_LAUNCH_CHECK();
   launch_colred<true>(a.gh, a.nsnp, a.LP, cr, nullptr, Eh, s);
-  k_tc_gh_slices<<<ceil_div((int64_t)a.ldg * a.LP, 256), 256, 0, s>>>(a, Eh);
+  if (a.fmt == kFmtE4M3)
+    k_tc_gh_slices<uint8_t><<<ceil_div((int64_t)a.ldg * a.LP, 256), 256, 0, s>>>(a, Eh);
+  else
+    k_tc_gh_slices<uint16_t><<<ceil_div((int64_t)a.ldg * a.LP, 256), 256, 0, s>>>(a, Eh);
   PCAONE_LAUNCH_CHECK();
-  k_units<<<ceil_div(a.nslice * a.LP, 128), 128, 0, s>>>(Eh, a.LP, a.nslice, 0, hunit);
+  k_units<<<ceil_div(a.nslice * a.LP, 128), 128, 0, s>>>(Eh, a.LP, a.nslice, a.digit_bits, 0, hunit);
   PCAONE_LAUNCH_CHECK();
-  k_units<<<ceil_div(a.nslice * a.LP, 128), 128, 0, s>>>(Eh, a.LP, a.nslice, 1, gmunit);
+  k_units<<<ceil_div(a.nslice * a.LP, 128), 128, 0, s>>>(Eh, a.LP, a.nslice, a.digit_bits, 1, gmunit);
   PCAONE_LAUNCH_CHECK();
   launch_colred<false>(a.cpart, a.nsnp, a.LP, cr, c_out, nullptr, s);
 }

@@ -26,6 +26,7 @@ struct GArgs {
   int* err;               // set to 1 when a bounded wait gave up
   int dense;              // 1: FP16 values (FileBinary input) instead of packed codes
   long long wait_cycles;  // limit of the pipeline waits in SM cycles (0: about 2 s)
+  int fp8;                // 1: E4M3 operands (128 samples per pipeline stage)
 };
 
 // H += X_w^T * Gh for one SNP window (dosage part; k_tc_h_finish adds the
@@ -46,6 +47,7 @@ struct HArgs {
   int* err;
   int dense;              // 1: FP16 values instead of packed codes
   long long wait_cycles;  // as GArgs::wait_cycles
+  int fp8;                // 1: E4M3 operands (128 SNPs per pipeline stage)
 };
 
 // H rows of one window: Hx += sum of the split partials + missing-entry terms - c
@@ -66,6 +68,7 @@ struct GFinishArgs {
   int64_t pos0;
   int nsnp;
   int L, LP, nslice, nchunks;
+  int fmt, digit_bits;           // operand format of the slices (kFmt*) and their digit width
   int ldg;                       // columns of the Gh operand (window length rounded up to 64)
   const void* part;              // chunk partials of D W (int64 for genotypes; FP64 with more than
                                  // kIntSlices slices; FP32 for dense input)
@@ -81,16 +84,16 @@ struct GFinishArgs {
   double* gh;                    // nsnp x LP (FP64): Gh of the window
   int32_t* ghint;                // nsnp x LP: Gh as represented by its slices, as integers
   int32_t* gmint;                // nsnp x LP: Gm = 2 f Gh represented as integers
-  __nv_bfloat16* gt;             // (nslice*LP) x ldg, K-major B operand of the H product
+  void* gt;                      // (nslice*LP) x ldg, K-major B operand of the H product (format fmt)
   double* cpart;                 // nsnp x LP partial terms of c
 };
 
-constexpr int kMapU8 = 0, kMapBF16 = 1, kMapF16 = 2;
+constexpr int kMapU8 = 0, kMapBF16 = 1, kMapF16 = 2;  // (E4M3 digits use kMapU8)
 void make_map_2d(CUtensorMap* map, const void* base, int dtype, uint64_t inner, uint64_t outer, uint64_t pitch_bytes,
                  uint32_t box_inner, uint32_t box_outer, bool swizzle128);
 // A tile bytes per pipeline stage of the G and H products
-inline int g_tile_bytes(bool dense) { return dense ? 128 * 128 : 128 * 16; }
-inline int h_tile_bytes(bool dense) { return dense ? 64 * 256 : 64 * 32; }
+inline int g_tile_bytes(bool dense, bool fp8 = false) { return dense ? 128 * 128 : fp8 ? 128 * 32 : 128 * 16; }
+inline int h_tile_bytes(bool dense, bool fp8 = false) { return dense ? 64 * 256 : fp8 ? 128 * 32 : 64 * 32; }
 // pipeline stages within shared memory (B slices + packed tile per stage) and
 // TMEM (nslice * LP accumulator columns + 32 A columns per stage)
 int stages_for(int LP, int nslice, int pbytes, bool dense);
@@ -104,6 +107,12 @@ int tmem_cols_needed(int LP, int nslice, int nstages, bool dense);
 constexpr int kDigitBits = 9;
 constexpr int kMaxSlices = 6;
 constexpr int kIntSlices = 3;
+// The FP8 form's slices: balanced base-16 digits, |w| <= 8, exact in E4M3
+// (two slices: an 8-bit integer representation of each column).
+constexpr int kDigitBits8 = 4;
+// operand formats of the slice digits
+constexpr int kFmtBF16 = 0, kFmtF16 = 1, kFmtE4M3 = 2;
+inline __host__ __device__ int digit_bits_of(int fmt) { return fmt == kFmtE4M3 ? kDigitBits8 : kDigitBits; }
 // Exact accumulation: a product d*w of a genotype dosage (<= 2) and a slice
 // digit is at most 512 in magnitude, so a CTA that sums at most 2^14 K elements
 // keeps every FP32 accumulator an exactly represented integer (|v| <= 2^23).
@@ -125,8 +134,8 @@ struct ColRedScratch {
   double* part;
   unsigned* cnt;
 };
-void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, __nv_bfloat16* w, double* wunit,
-                         double* colsum, int* E, double* rep, int32_t* wint, bool f16, const ColRedScratch& cr,
+void launch_omega_slices(const double* omg, int npad, int N, int LP, int S, void* w, double* wunit,
+                         double* colsum, int* E, double* rep, int32_t* wint, int fmt, const ColRedScratch& cr,
                          cudaStream_t s);
 // G finish, Gh slices and their units (hunit), Gm integers with their units
 // (gmunit: S x LP, the last slice row is the unit of gmint), c
