@@ -145,14 +145,15 @@ int pcaone_gpu_abi_version(void);
 int pcaone_gpu_timings(const pcaone_gpu_ctx* ctx, double t[4]);
 
 /* Instrumentation with no counterpart in the reference.  set_profiling(1)
- * records CUDA events on the context's stream around every launch of the two
- * window-product kernels (class 0: G = X_w * Omega, class 1: H += X_w^T * G)
+ * records CUDA events on the context's stream around every launch of the
+ * window-product kernels (class 0: G = X_w * Omega, class 1: H += X_w^T * G,
+ * in the exact forms; classes 2 and 3: the same in the FP8 form's E4M3 epochs)
  * and resets the totals; kernel_stats returns per class the summed device
  * milliseconds, algorithmic flops (2 * N * SNPs * L per launch) and launches.
  * launch_count is the number of kernels the library has launched so far in
  * this process. */
 int pcaone_gpu_set_profiling(pcaone_gpu_ctx* ctx, int on);
-int pcaone_gpu_kernel_stats(pcaone_gpu_ctx* ctx, double ms[2], double flops[2], long long launches[2]);
+int pcaone_gpu_kernel_stats(pcaone_gpu_ctx* ctx, double ms[4], double flops[4], long long launches[4]);
 unsigned long long pcaone_gpu_launch_count(void);
 /* Test hook with no counterpart in the reference: the limit, in SM clock
  * cycles, of every pipeline wait in the tensor-core product kernels (0, the

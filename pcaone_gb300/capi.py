@@ -365,12 +365,15 @@ class Context:
         self._check(self.lib.pcaone_gpu_set_profiling(self.h, int(on)))
 
     def kernel_stats(self):
-        ms = np.zeros(2)
-        fl = np.zeros(2)
-        n = np.zeros(2, dtype=np.int64)
+        """Per window-product class: device ms, algorithmic flops, launches
+        (g/h_product: exact forms; g/h_product_e4m3: the FP8 form's E4M3 epochs)."""
+        ms = np.zeros(4)
+        fl = np.zeros(4)
+        n = np.zeros(4, dtype=np.int64)
         self._check(self.lib.pcaone_gpu_kernel_stats(self.h, _ptr(ms), _ptr(fl), _ptr(n)))
-        return {"g_product": dict(ms=ms[0], flops=fl[0], launches=int(n[0])),
-                "h_product": dict(ms=ms[1], flops=fl[1], launches=int(n[1]))}
+        names = ("g_product", "h_product", "g_product_e4m3", "h_product_e4m3")
+        return {names[i]: dict(ms=float(ms[i]), flops=float(fl[i]), launches=int(n[i])) for i in range(4)
+                if i < 2 or n[i] > 0}
 
     def launch_count(self) -> int:
         return int(self.lib.pcaone_gpu_launch_count())

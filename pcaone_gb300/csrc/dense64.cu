@@ -36,7 +36,9 @@ constexpr int kRowsTile = 32;
 template <int Q, bool F64>
 __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict__ A, int lda, int na,
                                                        const double* __restrict__ B, int ldb, int nb, int64_t rows,
-                                                       int64_t rows_per_block, int sym, double* __restrict__ part) {
+                                                       int64_t rows_per_block, int sym, double* __restrict__ part,
+                                                       const int* __restrict__ only_if) {
+  if (only_if && *only_if == 0) return;
   extern __shared__ float smf[];
   float* Ah = smf;                       // kRowsTile x na
   float* Al = Ah + kRowsTile * na;
@@ -128,7 +130,8 @@ __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict_
 // blocks lane, lane+32, ... and a butterfly combines them (a fixed order, so
 // the result does not depend on scheduling); sym mirrors the upper triangle.
 __global__ void k_cross_reduce(const double* __restrict__ part, int nblocks, int na, int nb, int sym,
-                               double* __restrict__ W, int ldw) {
+                               double* __restrict__ W, int ldw, const int* __restrict__ only_if) {
+  if (only_if && *only_if == 0) return;
   const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (e >= (int64_t)na * nb) return;  // warp-uniform
@@ -158,8 +161,14 @@ __global__ void k_zero(double* p, int64_t n) {
 //     next pivot's root and reciprocal while the others update;
 //   inverse, step k = L-1 .. 0 of R X = I with X = I initially: row k of X
 //     times 1/d_k, then rows i < k updated x_ic -= r_ik x_kc.
-// The padding block of R and Rinv is the identity.  status: 0 ok, 1
-// non-positive or non-finite pivot.
+// The padding block of R and Rinv is the identity.  A non-positive or
+// non-finite pivot ORs 1 into *status.  With retry_rows >= 0 a failed factor
+// is taken again of W + shift I with the shift of shifted CholeskyQR3,
+// 11 (m n + n (n + 1)) u ||A||_F^2 = 11 (rows L + L (L + 1)) 2^-53 trace(W)
+// (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa 2020), and *shifted (when
+// given) records whether it was.  With only_if given and *only_if == 0 the
+// kernel does nothing: the later passes of CholeskyQR3 run only when the
+// first factor needed the shift, decided on the device.
 constexpr int kCholThreads = 512;
 // the arithmetic of the factor: double-float (dd) or, in the FP64-grade form,
 // FP64 (sqrt and division as CUDA provides them)
@@ -189,35 +198,53 @@ __device__ __forceinline__ void chol_pivot(const T* a, int L, int k, T* dg, T* r
 }
 
 template <class T>
-__global__ void __launch_bounds__(kCholThreads) k_chol_inv(const double* __restrict__ W, int L, int LP, double shift,
-                                                           double* __restrict__ R, double* __restrict__ Rinv,
-                                                           int* __restrict__ status) {
+__global__ void __launch_bounds__(kCholThreads) k_chol_inv(const double* __restrict__ W, int L, int LP,
+                                                           int64_t retry_rows, double* __restrict__ R,
+                                                           double* __restrict__ Rinv, int* __restrict__ status,
+                                                           int* __restrict__ shifted, const int* __restrict__ only_if) {
+  if (only_if && *only_if == 0) return;
   extern __shared__ dd sdd[];  // L x L factor, L x L inverse, L roots, L reciprocals
   T* a = reinterpret_cast<T*>(sdd);
   T* x = a + L * L;
   T* dg = x + L * L;
   T* rdg = dg + L;
   __shared__ int fail;
+  __shared__ double shift;
   const int tid = threadIdx.x, nt = blockDim.x;
-  if (tid == 0) fail = 0;
-  for (int e = tid; e < L * L; e += nt) {
-    const int i = e / L, j = e % L;
-    a[e] = num_from(W[i * LP + j] + (i == j ? shift : 0.0), (T*)nullptr);
-    x[e] = num_from(i == j ? 1.0 : 0.0, (T*)nullptr);
-  }
-  __syncthreads();
-  if (tid == 0) chol_pivot(a, L, 0, dg, rdg, &fail);
-  __syncthreads();
-  for (int k = 0; k < L; ++k) {
-    const T rk = rdg[k];
-    for (int j = k + 1 + tid; j < L; j += nt) a[k * L + j] = num_mul(a[k * L + j], rk);
-    __syncthreads();
-    const int m = L - k - 1;
-    for (int e = tid; e < m * m; e += nt) {
-      const int i = k + 1 + e / m, j = k + 1 + e % m;
-      if (j >= i) a[i * L + j] = num_fms(a[i * L + j], a[k * L + i], a[k * L + j]);
-      if (e == 0) chol_pivot(a, L, k + 1, dg, rdg, &fail);  // element (k+1, k+1) is final now
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    if (tid == 0) {
+      fail = 0;
+      double sh = 0.0;
+      if (attempt == 1) {
+        double tr = 0.0;
+        for (int i = 0; i < L; ++i) tr += W[i * LP + i];
+        sh = 11.0 * ((double)retry_rows * L + (double)L * (L + 1)) * 1.1102230246251565e-16 * tr;
+      }
+      shift = sh;
     }
+    __syncthreads();
+    for (int e = tid; e < L * L; e += nt) {
+      const int i = e / L, j = e % L;
+      a[e] = num_from(W[i * LP + j] + (i == j ? shift : 0.0), (T*)nullptr);
+      x[e] = num_from(i == j ? 1.0 : 0.0, (T*)nullptr);
+    }
+    __syncthreads();
+    if (tid == 0) chol_pivot(a, L, 0, dg, rdg, &fail);
+    __syncthreads();
+    for (int k = 0; k < L; ++k) {
+      const T rk = rdg[k];
+      for (int j = k + 1 + tid; j < L; j += nt) a[k * L + j] = num_mul(a[k * L + j], rk);
+      __syncthreads();
+      const int m = L - k - 1;
+      for (int e = tid; e < m * m; e += nt) {
+        const int i = k + 1 + e / m, j = k + 1 + e % m;
+        if (j >= i) a[i * L + j] = num_fms(a[i * L + j], a[k * L + i], a[k * L + j]);
+        if (e == 0) chol_pivot(a, L, k + 1, dg, rdg, &fail);  // element (k+1, k+1) is final now
+      }
+      __syncthreads();
+    }
+    if (tid == 0 && shifted) *shifted = attempt;
+    if (!fail || retry_rows < 0) break;  // fail and retry_rows are uniform over the block
     __syncthreads();
   }
   for (int k = L - 1; k >= 0; --k) {
@@ -243,7 +270,7 @@ __global__ void __launch_bounds__(kCholThreads) k_chol_inv(const double* __restr
     R[e] = v;
     Rinv[e] = w;
   }
-  if (tid == 0) *status = fail;
+  if (tid == 0 && fail) atomicOr(status, 1);
 }
 
 // C[rows x n] = A[rows x LP] * B[LP x n]; B (zero-padded to a multiple of 48
@@ -345,7 +372,8 @@ __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows
 constexpr int kUpperMaxQ = 14;  // columns per warp: LP / 8 with LP <= 112
 template <bool F64>
 __global__ void __launch_bounds__(256) k_gemm_tall_upper(double* A, int64_t rows, int LP,
-                                                         const double* __restrict__ B) {
+                                                         const double* __restrict__ B, const int* __restrict__ only_if) {
+  if (only_if && *only_if == 0) return;
   extern __shared__ float smf[];
   const int las = LP + 1;  // odd row stride of the A tile: lanes hit distinct banks
   float* Bh = smf;         // LP x LP
@@ -526,7 +554,8 @@ __global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, in
 
 // C = A * B for LP x LP row-major (single CTA, operands staged in shared memory)
 __global__ void __launch_bounds__(512) k_mult_small(const double* __restrict__ A, const double* __restrict__ B,
-                                                    double* __restrict__ C, int LP) {
+                                                    double* __restrict__ C, int LP, const int* __restrict__ only_if) {
+  if (only_if && *only_if == 0) return;
   extern __shared__ double sab[];
   double* As = sab;
   double* Bs = sab + LP * LP;
@@ -801,6 +830,13 @@ __global__ void k_subspace_residual(const double* __restrict__ X, const double* 
   R[e] = v;
 }
 
+__global__ void k_copy_if(const double* __restrict__ src, double* __restrict__ dst, int64_t n,
+                          const int* __restrict__ only_if) {
+  if (*only_if == 0) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i];
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -814,26 +850,26 @@ size_t cross_smem(int na, int nb, int sym) {
 
 template <int Q, bool F64>
 void launch_cross_qf(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int64_t per,
-                     int sym, double* part, int nblocks, size_t smem, cudaStream_t s) {
+                     int sym, double* part, int nblocks, size_t smem, cudaStream_t s, const int* only_if) {
   static bool attr_set = false;
   if (!attr_set) {
     PCAONE_CUDA(
         cudaFuncSetAttribute(k_cross_partial<Q, F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_set = true;
   }
-  k_cross_partial<Q, F64><<<nblocks, 256, smem, s>>>(A, lda, na, B, ldb, nb, rows, per, sym, part);
+  k_cross_partial<Q, F64><<<nblocks, 256, smem, s>>>(A, lda, na, B, ldb, nb, rows, per, sym, part, only_if);
 }
 template <int Q>
 void launch_cross_q(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int64_t per,
-                    int sym, double* part, int nblocks, size_t smem, bool f64, cudaStream_t s) {
+                    int sym, double* part, int nblocks, size_t smem, bool f64, cudaStream_t s, const int* only_if) {
   if (f64)
-    launch_cross_qf<Q, true>(A, lda, na, B, ldb, nb, rows, per, sym, part, nblocks, smem, s);
+    launch_cross_qf<Q, true>(A, lda, na, B, ldb, nb, rows, per, sym, part, nblocks, smem, s, only_if);
   else
-    launch_cross_qf<Q, false>(A, lda, na, B, ldb, nb, rows, per, sym, part, nblocks, smem, s);
+    launch_cross_qf<Q, false>(A, lda, na, B, ldb, nb, rows, per, sym, part, nblocks, smem, s, only_if);
 }
 
 void launch_cross(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int sym,
-                  double* W, int ldw, double* part, int nblocks, cudaStream_t s, bool f64) {
+                  double* W, int ldw, double* part, int nblocks, cudaStream_t s, bool f64, const int* only_if) {
   if (na * nb > 64 * 256 || na > 0xffff) throw Error(-6, "cross product wider than 128 x 128");
   if (rows == 0) {
     k_zero<<<ceil_div((int64_t)na * ldw, 256), 256, 0, s>>>(W, (int64_t)na * ldw);
@@ -848,38 +884,39 @@ void launch_cross(const double* A, int lda, int na, const double* B, int ldb, in
   const double* Bv = sym ? A : B;
   const int ldbv = sym ? lda : ldb;
   if (q <= 4)
-    launch_cross_q<4>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s);
+    launch_cross_q<4>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s, only_if);
   else if (q <= 8)
-    launch_cross_q<8>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s);
+    launch_cross_q<8>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s, only_if);
   else if (q <= 16)
-    launch_cross_q<16>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s);
+    launch_cross_q<16>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s, only_if);
   else if (q <= 32)
-    launch_cross_q<32>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s);
+    launch_cross_q<32>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s, only_if);
   else
-    launch_cross_q<64>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s);
+    launch_cross_q<64>(A, lda, na, Bv, ldbv, nb, rows, per, sym, part, nblocks, smem, f64, s, only_if);
   PCAONE_LAUNCH_CHECK();
-  k_cross_reduce<<<ceil_div((int64_t)na * nb * 32, 256), 256, 0, s>>>(part, nblocks, na, nb, sym, W, ldw);
+  k_cross_reduce<<<ceil_div((int64_t)na * nb * 32, 256), 256, 0, s>>>(part, nblocks, na, nb, sym, W, ldw, only_if);
   PCAONE_LAUNCH_CHECK();
 }
 
 template <class T>
-void launch_chol_t(const double* W, int L, int LP, double shift, double* R, double* Rinv, int* status,
-                   cudaStream_t s) {
+void launch_chol_t(const double* W, int L, int LP, int64_t retry_rows, double* R, double* Rinv, int* status,
+                   int* shifted, const int* only_if, cudaStream_t s) {
   static bool attr_set = false;
   if (!attr_set) {
     PCAONE_CUDA(cudaFuncSetAttribute(k_chol_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_set = true;
   }
   static_assert(sizeof(T) == sizeof(dd), "factor element size");
-  k_chol_inv<T><<<1, kCholThreads, sizeof(T) * (2 * L * L + 2 * L), s>>>(W, L, LP, shift, R, Rinv, status);
+  k_chol_inv<T><<<1, kCholThreads, sizeof(T) * (2 * L * L + 2 * L), s>>>(W, L, LP, retry_rows, R, Rinv, status,
+                                                                         shifted, only_if);
 }
 
-void launch_chol_inv_shift(const double* W, int L, int LP, double shift, double* R, double* Rinv, int* status,
-                           cudaStream_t s, bool f64) {
+void launch_chol_inv(const double* W, int L, int LP, double* R, double* Rinv, int* status, cudaStream_t s, bool f64,
+                     int64_t retry_rows, int* shifted, const int* only_if) {
   if (f64)
-    launch_chol_t<double>(W, L, LP, shift, R, Rinv, status, s);
+    launch_chol_t<double>(W, L, LP, retry_rows, R, Rinv, status, shifted, only_if, s);
   else
-    launch_chol_t<dd>(W, L, LP, shift, R, Rinv, status, s);
+    launch_chol_t<dd>(W, L, LP, retry_rows, R, Rinv, status, shifted, only_if, s);
   PCAONE_LAUNCH_CHECK();
 }
 
@@ -908,7 +945,7 @@ void launch_gemm_tall(const double* A, int64_t rows, int LP, const double* B, in
 }
 
 template <bool F64>
-void launch_gemm_tall_upper_t(double* A, int64_t rows, int LP, const double* B, cudaStream_t s) {
+void launch_gemm_tall_upper_t(double* A, int64_t rows, int LP, const double* B, cudaStream_t s, const int* only_if) {
   static bool attr_set = false;
   if (!attr_set) {
     PCAONE_CUDA(
@@ -917,16 +954,17 @@ void launch_gemm_tall_upper_t(double* A, int64_t rows, int LP, const double* B, 
   }
   const size_t smem = 2 * sizeof(float) * ((size_t)LP * LP + (size_t)kRowsTile * (LP + 1));
   const int grid = (int)std::min<int64_t>((rows + kRowsTile - 1) / kRowsTile, 152 * 8);
-  k_gemm_tall_upper<F64><<<grid, 256, smem, s>>>(A, rows, LP, B);
+  k_gemm_tall_upper<F64><<<grid, 256, smem, s>>>(A, rows, LP, B, only_if);
 }
 
-void launch_gemm_tall_upper(double* A, int64_t rows, int LP, const double* B, cudaStream_t s, bool f64) {
+void launch_gemm_tall_upper(double* A, int64_t rows, int LP, const double* B, cudaStream_t s, bool f64,
+                            const int* only_if) {
   if (rows == 0) return;
   if (LP % 8 != 0 || LP > 8 * kUpperMaxQ) throw Error(-6, "triangular tall product: width must be a multiple of 8, at most 112");
   if (f64)
-    launch_gemm_tall_upper_t<true>(A, rows, LP, B, s);
+    launch_gemm_tall_upper_t<true>(A, rows, LP, B, s, only_if);
   else
-    launch_gemm_tall_upper_t<false>(A, rows, LP, B, s);
+    launch_gemm_tall_upper_t<false>(A, rows, LP, B, s, only_if);
   PCAONE_LAUNCH_CHECK();
 }
 
@@ -970,13 +1008,13 @@ void launch_to_f32(const double* a, float* b, int64_t n, cudaStream_t s) {
   PCAONE_LAUNCH_CHECK();
 }
 
-void launch_mult_small(const double* A, const double* B, double* C, int LP, cudaStream_t s) {
+void launch_mult_small(const double* A, const double* B, double* C, int LP, cudaStream_t s, const int* only_if) {
   static bool attr_set = false;
   if (!attr_set) {
     PCAONE_CUDA(cudaFuncSetAttribute(k_mult_small, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
     attr_set = true;
   }
-  k_mult_small<<<1, 512, sizeof(double) * 2 * LP * LP, s>>>(A, B, C, LP);
+  k_mult_small<<<1, 512, sizeof(double) * 2 * LP * LP, s>>>(A, B, C, LP, only_if);
   PCAONE_LAUNCH_CHECK();
 }
 
@@ -1004,6 +1042,11 @@ void launch_subspace_change(const double* X, const double* Y, int64_t rows, int 
   k_subspace_residual<<<ceil_div(rows * n, 256), 256, 0, s>>>(X, Y, k, n, M, rows, R);
   PCAONE_LAUNCH_CHECK();
   launch_cross(R, n, n, R, n, n, rows, 1, W, n, part, nblocks, s, true);
+}
+
+void launch_copy_if(const double* src, double* dst, int64_t n, const int* only_if, cudaStream_t s) {
+  k_copy_if<<<ceil_div(n, 256), 256, 0, s>>>(src, dst, n, only_if);
+  PCAONE_LAUNCH_CHECK();
 }
 
 void launch_em_fill(const int32_t* epos, const int32_t* sample, double* value, int64_t nnz, const int32_t* perm,

@@ -173,8 +173,9 @@ struct Context {
   size_t ev_used = 0;
   std::vector<std::pair<int, size_t>> ev_marks;  // (class, index of the start event)
   std::vector<std::pair<int, double>> ev_work;   // (class, flops of the launch)
-  double prof_ms[2] = {0, 0}, prof_flops[2] = {0, 0};
-  long long prof_launches[2] = {0, 0};
+  // classes: 0 G product, 1 H product (exact forms), 2 G, 3 H (E4M3 epochs)
+  double prof_ms[4] = {0, 0, 0, 0}, prof_flops[4] = {0, 0, 0, 0};
+  long long prof_launches[4] = {0, 0, 0, 0};
 
   BedView view() const { return BedView{bed.p, stride, M, N}; }
 
@@ -626,15 +627,8 @@ static void init_omg(Context& c) {
   c.w_slices = 0;
 }
 
-static int read_status(Context& c) {
-  int st = 0;
-  PCAONE_CUDA(cudaMemcpyAsync(&st, c.status.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
-  return st;
-}
-
 // a tensor-core tile that gave up a bounded wait leaves its partial sums
-// unwritten: report that (PCAONE_E_CUDA) before any numerical consequence
+// unwritten: PCAONE_E_CUDA, reported before any numerical consequence
 static void check_tc_err(Context& c) {
   if (!c.tc) return;
   int e = 0;
@@ -643,57 +637,53 @@ static void check_tc_err(Context& c) {
   if (e) throw Error(PCAONE_E_CUDA, "tensor-core pipeline: a bounded wait gave up (kernel aborted its tile)");
 }
 
+// Device status words: [0] CholeskyQR failures (OR of the factor kernels),
+// [1] small-SVD convergence, [2] whether the first Gram of the last CholeskyQR
+// needed the shift.  Read once per epoch (check_status), not per factor.
+static void clear_status(Context& c) { PCAONE_CUDA(cudaMemsetAsync(c.status.p, 0, 2 * sizeof(int), c.stream)); }
+
+static void check_status(Context& c) {
+  int st[2] = {0, 0};
+  PCAONE_CUDA(cudaMemcpyAsync(st, c.status.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  if (st[0]) {
+    check_tc_err(c);  // a tile that gave up leaves partial sums unwritten: report that first
+    throw Error(PCAONE_E_NUMERIC, "CholeskyQR: Gram matrix not positive definite, also after the shift");
+  }
+}
+
 // Orthonormal factor of A (rows x LP, in place) by CholeskyQR2, or shifted
 // CholeskyQR3 when the first Gram is not numerically positive definite
-// (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa 2020).  With need_r, Rt
-// holds R (upper, A_in = Q R) and Rti its inverse on return; the updates of
-// Omega only need Q.
+// (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa 2020): the first factor
+// retries with the shift on the device and raises a device flag, which the
+// third pass's kernels read, so no host round trip decides the path.  With
+// need_r, Rt holds R (upper, A_in = Q R) and Rti its inverse on return; the
+// updates of Omega only need Q.  Failures land in the device status word.
 static void cholqr(Context& c, double* A, int64_t rows, bool need_r) {
   const int L = c.L, LP = c.LP;
   const int nb = cross_blocks(rows);
+  int* failed = c.status.p;
+  int* shifted = c.status.p + 2;
   launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream, c.fp64);
-  launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R1.p, c.R1i.p, c.status.p, c.stream, c.fp64);
-  bool shifted = false;
-  if (read_status(c) != 0) {
-    // shift = 11 (m n + n (n + 1)) u ||A||_F^2
-    std::vector<double> w((size_t)LP * LP);
-    PCAONE_CUDA(cudaMemcpy(w.data(), c.W.p, w.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    double tr = 0;
-    for (int i = 0; i < L; ++i) tr += w[(size_t)i * LP + i];
-    const double shift = 11.0 * ((double)rows * L + (double)L * (L + 1)) * 1.1102230246251565e-16 * tr;
-    launch_chol_inv_shift(c.W.p, L, LP, shift, c.R1.p, c.R1i.p, c.status.p, c.stream, c.fp64);
-    if (read_status(c) != 0) {
-      check_tc_err(c);
-      throw Error(PCAONE_E_NUMERIC, "CholeskyQR: Gram matrix not positive definite");
-    }
-    shifted = true;
-  }
+  launch_chol_inv(c.W.p, L, LP, c.R1.p, c.R1i.p, failed, c.stream, c.fp64, rows, shifted);
   launch_gemm_tall_upper(A, rows, LP, c.R1i.p, c.stream, c.fp64);
   launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream, c.fp64);
-  launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R2.p, c.R2i.p, c.status.p, c.stream, c.fp64);
-  if (read_status(c) != 0) {
-    check_tc_err(c);
-    throw Error(PCAONE_E_NUMERIC, "CholeskyQR: second Gram not positive definite");
-  }
+  launch_chol_inv(c.W.p, L, LP, c.R2.p, c.R2i.p, failed, c.stream, c.fp64);
   launch_gemm_tall_upper(A, rows, LP, c.R2i.p, c.stream, c.fp64);
   if (need_r) {
     launch_mult_small(c.R2.p, c.R1.p, c.Rt.p, LP, c.stream);     // R = R2 R1
     launch_mult_small(c.R1i.p, c.R2i.p, c.Rti.p, LP, c.stream);  // R^-1 = R1^-1 R2^-1
   }
-  if (shifted) {
-    launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream, c.fp64);
-    launch_chol_inv_shift(c.W.p, L, LP, 0.0, c.R3.p, c.R3i.p, c.status.p, c.stream, c.fp64);
-    if (read_status(c) != 0) {
-      check_tc_err(c);
-      throw Error(PCAONE_E_NUMERIC, "CholeskyQR: third Gram not positive definite");
-    }
-    launch_gemm_tall_upper(A, rows, LP, c.R3i.p, c.stream, c.fp64);
-    if (need_r) {
-      launch_mult_small(c.R3.p, c.Rt.p, c.R1.p, LP, c.stream);
-      launch_mult_small(c.Rti.p, c.R3i.p, c.R1i.p, LP, c.stream);
-      PCAONE_CUDA(cudaMemcpyAsync(c.Rt.p, c.R1.p, (size_t)LP * LP * 8, cudaMemcpyDeviceToDevice, c.stream));
-      PCAONE_CUDA(cudaMemcpyAsync(c.Rti.p, c.R1i.p, (size_t)LP * LP * 8, cudaMemcpyDeviceToDevice, c.stream));
-    }
+  // the third pass of shifted CholeskyQR3, run by the device only when the
+  // first factor needed the shift
+  launch_cross(A, LP, L, A, LP, L, rows, 1, c.W.p, LP, c.red.p, nb, c.stream, c.fp64, shifted);
+  launch_chol_inv(c.W.p, L, LP, c.R3.p, c.R3i.p, failed, c.stream, c.fp64, -1, nullptr, shifted);
+  launch_gemm_tall_upper(A, rows, LP, c.R3i.p, c.stream, c.fp64, shifted);
+  if (need_r) {
+    launch_mult_small(c.R3.p, c.Rt.p, c.R1.p, LP, c.stream, shifted);    // R = R3 R2 R1
+    launch_mult_small(c.Rti.p, c.R3i.p, c.R1i.p, LP, c.stream, shifted); // R^-1 = R1^-1 R2^-1 R3^-1
+    launch_copy_if(c.R1.p, c.Rt.p, (int64_t)LP * LP, shifted, c.stream);
+    launch_copy_if(c.R1i.p, c.Rti.p, (int64_t)LP * LP, shifted, c.stream);
   }
 }
 
@@ -902,7 +892,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ga.dense = c.dense ? 1 : 0;
   ga.wait_cycles = c.wait_cycles;
   ga.fp8 = fp8 ? 1 : 0;
-  mark(0);
+  mark(fp8 ? 2 : 0);
   tc::launch_g(fp8 ? c.map_bed_g8 : c.map_bed_g, fp8 ? c.map_w8 : c.map_w, ga, c.stream);
   close_mark();
   if (any_miss) {
@@ -988,7 +978,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
     sg.out2 = c.hesum.p;
     launch_seg_gather(sg, c.stream);
   }
-  mark(1);
+  mark(fp8 ? 3 : 1);
   tc::launch_h(fp8 ? c.map_bed_h8 : c.map_bed_h, fp8 ? c.map_gt8 : c.map_gt, ha, c.stream);
   close_mark();
   tc::HFinishArgs hf{};
@@ -1182,6 +1172,7 @@ static void compute_g_and_h(Context& c, int pi) {
 static int compute_usv(Context& c, int p, double tol) {
   const int64_t M = c.M;
   if (c.tc) PCAONE_CUDA(cudaMemsetAsync(c.err.p, 0, sizeof(int), c.stream));  // a fresh abort flag per call
+  clear_status(c);
   const int N = c.N, L = c.L, LP = c.LP, k = c.k;
   int epochs = 0;
   bool done = false, ucur_in_upre = false;
@@ -1198,6 +1189,7 @@ static int compute_usv(Context& c, int p, double tol) {
     compute_g_and_h(c, pi);
     PCAONE_CUDA(cudaStreamSynchronize(c.stream));
     check_tc_err(c);
+    check_status(c);
     c.collect_events();
     auto t1 = clk::now();
     c.t_prod += secs(t0, t1);
@@ -1215,6 +1207,7 @@ static int compute_usv(Context& c, int p, double tol) {
       double mv = 0;
       PCAONE_CUDA(cudaMemcpyAsync(&mv, c.mevv.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
       PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+      check_status(c);  // the QR of G
       const double diff = 1.0 - mv;
       if (c.verbose && !c.P.emu) std::fprintf(stderr, "running of epoch = %d, diff = %g\n", pi, diff);
       if (diff < tol || pi == p) {
@@ -1248,6 +1241,7 @@ static int compute_usv(Context& c, int p, double tol) {
     if (done) break;
   }
   if (ucur_in_upre) std::swap(c.U.p, c.Upre.p);  // U = Ucur after the loop (Halko.cpp:96)
+  check_status(c);
   c.have_usv = true;
   return epochs;
 }
@@ -1588,7 +1582,7 @@ int pcaone_gpu_set_profiling(pcaone_gpu_ctx* ctx, int on) {
     PCAONE_CUDA(cudaStreamSynchronize(c.stream));
     c.collect_events();
     c.profiling = on != 0;
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < 4; ++i) {
       c.prof_ms[i] = 0;
       c.prof_flops[i] = 0;
       c.prof_launches[i] = 0;
@@ -1596,11 +1590,11 @@ int pcaone_gpu_set_profiling(pcaone_gpu_ctx* ctx, int on) {
   });
 }
 
-int pcaone_gpu_kernel_stats(pcaone_gpu_ctx* ctx, double ms[2], double flops[2], long long launches[2]) {
+int pcaone_gpu_kernel_stats(pcaone_gpu_ctx* ctx, double ms[4], double flops[4], long long launches[4]) {
   return guarded(ctx, [&](Context& c) {
     PCAONE_CUDA(cudaStreamSynchronize(c.stream));
     c.collect_events();
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < 4; ++i) {
       if (ms) ms[i] = c.prof_ms[i];
       if (flops) flops[i] = c.prof_flops[i];
       if (launches) launches[i] = c.prof_launches[i];
@@ -1738,7 +1732,9 @@ int pcaone_gpu_compute_g_and_h(pcaone_gpu_ctx* ctx, int pi, double* G, double* H
   return guarded(ctx, [&](Context& c) {
     pcaone::need_op(c);
     if (pi < 0) throw Error(PCAONE_E_ARG, "negative epoch");
+    pcaone::clear_status(c);
     pcaone::compute_g_and_h(c, pi);
+    pcaone::check_status(c);
     pcaone::copy_out(c, c.G.p, c.M, c.LP, c.L, G);
     pcaone::copy_out(c, c.H.p, c.N, c.LP, c.L, H);
     PCAONE_CUDA(cudaStreamSynchronize(c.stream));

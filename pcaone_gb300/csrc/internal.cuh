@@ -170,24 +170,34 @@ size_t cross_smem(int na, int nb, int sym);
 // W[i][j] (ld ldw) = sum_r A[r][i] * B[r][j], i < na, j < nb; sym: B = A
 // f64 (here and below): plain FP64 arithmetic instead of FP32 pairs (the
 // FP64-grade form)
+// only_if (here and below): a device flag; when given and 0 the kernels do
+// nothing (work decided on the device without a host round trip)
 void launch_cross(const double* A, int lda, int na, const double* B, int ldb, int nb, int64_t rows, int sym,
-                  double* W, int ldw, double* part, int nblocks, cudaStream_t s, bool f64 = false);
-// Cholesky of W + shift*I (leading L block) -> R (upper), Rinv; padding = identity
-void launch_chol_inv_shift(const double* W, int L, int LP, double shift, double* R, double* Rinv, int* status,
-                           cudaStream_t s, bool f64 = false);
+                  double* W, int ldw, double* part, int nblocks, cudaStream_t s, bool f64 = false,
+                  const int* only_if = nullptr);
+// Cholesky of W (leading L block) -> R (upper), Rinv; padding = identity.  A
+// failure ORs 1 into *status; with retry_rows >= 0 a failed factor is retaken
+// with the shift of shifted CholeskyQR3 for a tall matrix of that many rows,
+// and *shifted (when given) records whether it was
+void launch_chol_inv(const double* W, int L, int LP, double* R, double* Rinv, int* status, cudaStream_t s,
+                     bool f64 = false, int64_t retry_rows = -1, int* shifted = nullptr, const int* only_if = nullptr);
 // C (rows x n, ld ldc) = A (rows x LP) * B (LP x n, ld ldb); C may alias A
 void launch_gemm_tall(const double* A, int64_t rows, int LP, const double* B, int ldb, int n, double* C, int ldc,
                       cudaStream_t s, bool f64 = false);
 // A <- A * B in place for B upper triangular (LP x LP, LP a multiple of 8)
-void launch_gemm_tall_upper(double* A, int64_t rows, int LP, const double* B, cudaStream_t s, bool f64 = false);
+void launch_gemm_tall_upper(double* A, int64_t rows, int LP, const double* B, cudaStream_t s, bool f64 = false,
+                            const int* only_if = nullptr);
 // Q columns times the signs an Eigen / LAPACK Householder QR gives
 void launch_house_signs(double* Q, int64_t rows, int L, int LP, double* sgn, cudaStream_t s);
 int flip_blocks(int64_t rows);
 void launch_flip_omg(double* omg2, double* omg, int64_t rows, int L, int LP, double* part, double* sgn,
                      cudaStream_t s);
 void launch_add(const double* a, const double* b, double* c, int64_t n, cudaStream_t s);
+// dst = src (n doubles) when *only_if != 0
+void launch_copy_if(const double* src, double* dst, int64_t n, const int* only_if, cudaStream_t s);
 void launch_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
-void launch_mult_small(const double* A, const double* B, double* C, int LP, cudaStream_t s);
+void launch_mult_small(const double* A, const double* B, double* C, int LP, cudaStream_t s,
+                       const int* only_if = nullptr);
 void launch_usv_small(const double* Rinv, const double* Wh, int L, int LP, int k, double* UB, double* sigma,
                       double* T, double* tmp, int* status, cudaStream_t s);
 // W = R^T R with R = Y_n - X_n (X_n^T Y_n), the leading n columns of the

@@ -271,6 +271,10 @@ WORKLOADS = {
     # (1.56 GB packed) for profiling captures of single window launches
     "c2p": dict(nsamples=100_000, nsnps=62_500, npop=5, fst=[0.01, 0.02, 0.05, 0.1, 0.2],
                 anc="uniform", anc_range=(0.01, 0.5), mcar=0.005, k=20, p=20, maxp=6, bands=8),
+    # the c3 window shape (15,625 SNPs x 200,000 samples, k=40, p=10) as one
+    # single-pass window (0.78 GB packed) for profiling captures of single launches
+    "c3p": dict(nsamples=200_000, nsnps=15_625, npop=8, fst=0.05, anc="beta", anc_range=(0.01, 0.99),
+                admixed_frac=0.02, mcar=0.0, k=40, p=10, maxp=6, bands=64, svd=1, perm=0),
     # continuous dosages held as FP16 (FileBinary input, -C 0): c5 is 1M SNPs x 100k
     # samples (200 GB FP16, run without the shuffle: a shuffled copy would not
     # fit), c5s the same model at 100k SNPs (20 GB)
