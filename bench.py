@@ -135,7 +135,11 @@ class ClockSampler:
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # tensor-core window products, from one ncu capture of a window of the
 # workload's shape, keyed by (workload, product)
-NCU_TRAFFIC = {}
+NCU_TRAFFIC = {
+    # one capture of a window of the 1M-SNP workload (15,625 SNPs x 200,064 samples)
+    ("c3", "k_tc_h<e4m3>"): 787.7e6 + 184.1e6,
+    ("c3", "k_tc_g<e4m3>"): 827.2e6 + 119.3e6,
+}
 
 
 def workload_params(name: str, precision: str):
