@@ -531,6 +531,70 @@ def run_dense(args, wl, params, model, peaks, peak_kind, rank, ws, local):
     ctx.close()
 
 
+def host_mem_available():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return None
+
+
+def out_of_core_block(args, capi, local, pinned, M, N, params, in_core, in_core_perm):
+    """The out-of-core form (pcaone_gpu_load_bed_stream) on the same matrix:
+    the library's pinned host copy of the rows, two device slots of one window
+    each within a 4 GiB device budget; seconds per run with the rows in host
+    memory (CUDA events) and bytes streamed per run.  The window method's
+    shuffle follows the reference's out-of-core order (permute_plink), so the
+    PCs are compared with the in-core run's (its std::shuffle order) on the
+    well-separated components, loadings back in file order."""
+    from pcaone_gb300.accuracy import compare_pcs
+    import torch
+    stride = (N + 127) // 128 * 32
+    avail = host_mem_available()
+    if avail is not None and avail < 1.5 * M * stride:
+        return {"skipped": f"{avail / 1e9:.0f} GB of host memory available, the pinned copy needs "
+                           f"{M * stride / 1e9:.0f} GB"}
+    budget = 4 << 30
+    ctx = capi.Context(local)
+    try:
+        t0 = time.perf_counter()
+        ctx.load_bed_stream(pinned.data_ptr(), N, budget, nsnps=M)
+        load_s = time.perf_counter() - t0
+        ctx.run_halko(params)  # warm-up
+        ctx.stream_info()
+        times, fetched = [], []
+        for _ in range(max(1, min(args.steps, 3))):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            U, S, V, _ = ctx.run_halko(params)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            fetched.append(ctx.stream_info()[1])
+        t = sum(times) / len(times)
+        Vf = np.empty_like(V)
+        Vf[ctx.perm()] = V
+        Vi = np.empty_like(in_core[2])
+        Vi[in_core_perm] = in_core[2]
+        agree = compare_pcs(U, S, Vf, in_core[0], in_core[1], Vi)
+        svd = "window" if params.svd == capi.SVD_WINDOW else "single"
+        blk, nblk = capi.stream_plan(M, N, params.svd, params.bands, budget)
+        return {"value": t, "unit": "s", "device_budget_bytes": budget, "block_snps": blk, "blocks": nblk,
+                "method": svd, "load_s": load_s, "bytes_streamed_per_run": sum(fetched) / len(fetched),
+                "stream_gbs": sum(fetched) / len(fetched) / t / 1e9, "vs_in_core": agree,
+                "note": "rows in the library's pinned host copy (device row layout), windows in the reference's "
+                        "out-of-core order (permute_plink, --buffer 2); each window copied to a device slot by "
+                        "pitched copies on a second stream while the previous window's products run; load_s "
+                        "includes pinning the host copy"}
+    finally:
+        ctx.close()
+
+
 def run_ours(args):
     rank, ws, local = dist_init()
     import torch
@@ -623,6 +687,11 @@ def run_ours(args):
         etimes.append(e0.elapsed_time(e1) / 1e3)
     t_e2e = reduce_max(sum(etimes) / len(etimes), ws)
     h2d = M * bps + N * L * 8
+
+    # ---- out-of-core: the rows stay in pinned host memory, SNP blocks streamed ----
+    ooc = None
+    if rank == 0 and not args.no_out_of_core:
+        ooc = out_of_core_block(args, capi, local, pinned, M, N, params, (U, S, V), ctx.perm())
     d2h = (N + M) * wl["k"] * 8 + wl["k"] * 8
 
     # ---- roofline of the dominant kernel ----
@@ -687,6 +756,7 @@ def run_ours(args):
             "host_s": host_phases,
             "pcs": {"S_top": [float(x) for x in S[:5]]},
             "accuracy": accuracy,
+            "out_of_core": ooc,
         }
         if wl.get("emu"):
             line["em"] = {"iterations": em_iters[-1] if em_iters else None, "tolem": params.tolem,
@@ -707,6 +777,7 @@ def main():
     ap.add_argument("--precision", default="fp8", choices=["fp32", "bf16", "bf16x3", "fp8", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64-grade and FP32 reference runs")
+    ap.add_argument("--no-out-of-core", action="store_true", help="skip the streamed (out-of-core) runs")
     ap.add_argument("--warm-start", action="store_true", help="learned EM warm start (EM workloads)")
     ap.add_argument("--maxiter", type=int, default=None, help="EM iteration cap (EM workloads)")
     args = ap.parse_args()

@@ -1,7 +1,8 @@
 /*
  * pcaone_gpu.h -- C-ABI of the GB300 randomized-SVD hot path.
  *
- * The library replaces, for the in-core PLINK path, the reference's
+ * The library replaces, for the PLINK path (in core, or out of core with the
+ * rows in host memory) and FileBinary input, the reference's
  * RSVD operator interface (class RsvdOpData, src/Halko.hpp:6-42) and the data
  * it reads (class Data / FileBed, src/Data.hpp:9-59, src/FilePlink.hpp:7-47).
  * Every entry point takes plain pointers and sizes, returns 0 on success or a
@@ -209,6 +210,47 @@ int pcaone_gpu_load_synthetic(pcaone_gpu_ctx* ctx, uint64_t nsnps, uint32_t nsam
 /* Copies the resident packed genotypes back (nsnps rows of (nsamples+3)/4
  * bytes, the .bed body). */
 int pcaone_gpu_get_bed(pcaone_gpu_ctx* ctx, uint8_t* packed);
+
+/* ---- out-of-core: replaces the -m/--memory path ---------------------------
+ * FileBed::read_block_initial (src/FilePlink.cpp:122-218) with the block plan
+ * of Data::prepare (src/Data.cpp:40-84) and the block loops of computeGandH
+ * (src/Halko.cpp:130-153, 227-268).  The packed rows stay in host memory: the
+ * library keeps a pinned copy in its device row layout (nsnps x
+ * ceil(nsamples/128)*32 bytes), and each SNP block the window products need is
+ * copied into one of two device slots while the previous block's products run
+ * (in the shuffled order of the window method, a kernel gathers the block's
+ * rows over the host link).  device_budget bounds the two slots in bytes (0:
+ * no bound).  Without the window method's shuffle, results are bit-identical
+ * to those of the in-core load with the same parameters (the single-pass
+ * method's blocks are the in-core ones unless the budget asks for smaller).  Everything else reads the host copy directly
+ * (counts, missing-entry index, FP32 form, matvec, warm start).  Arguments and
+ * checks as pcaone_gpu_load_bed / _file_image.
+ * The window method's shuffle takes, as the reference's out-of-core mode
+ * does (src/Main.cpp:120-130), the order in which permute_plink rewrites the
+ * .bed (src/FilePlink.cpp:303-408; pcaone_gpu_ooc_order) instead of the
+ * in-core std::shuffle order; buffer_gb is its --buffer (0: 2, the
+ * reference's default); a kernel then gathers each window's rows over the
+ * host link, where unshuffled windows are one host-to-device copy each. */
+int pcaone_gpu_load_bed_stream(pcaone_gpu_ctx* ctx, const uint8_t* packed, uint64_t nsnps, uint32_t nsamples,
+                               uint64_t device_budget, uint32_t buffer_gb);
+int pcaone_gpu_load_bed_file_image_stream(pcaone_gpu_ctx* ctx, const uint8_t* image, uint64_t image_bytes,
+                                          uint64_t nsnps, uint32_t nsamples, uint64_t device_budget,
+                                          uint32_t buffer_gb);
+/* The out-of-core SNP order alone (no GPU needed): order[p] is the .bed row at
+ * working position p after permute_plink with --buffer buffer_gb (0: 2) and
+ * bands windows.  PCAONE_E_ARG when a buffer holds fewer SNPs than windows. */
+int pcaone_gpu_ooc_order(uint64_t nsnps, uint32_t nsamples, int bands, uint32_t buffer_gb, int32_t* order);
+/* The block plan alone (no GPU needed): SNPs per streamed block and the number
+ * of blocks for svd (PCAONE_SVD_*) and bands.  The window method streams its
+ * windows of ceil(nsnps/bands) SNPs, which two slots must hold (the reference
+ * cuts a window into bandFactor blocks instead, Data.cpp:66-77); the
+ * single-pass method uses blocks of at most 16384 SNPs, fewer when the budget
+ * asks, balanced.  PCAONE_E_LIMIT when the budget holds fewer than two blocks. */
+int pcaone_gpu_stream_plan(uint64_t nsnps, uint32_t nsamples, int svd, int bands, uint64_t device_budget,
+                           uint64_t* block_snps, uint64_t* nblocks);
+/* Whether the loaded rows are streamed, and the bytes copied into the device
+ * slots since the previous call (which resets the count). */
+int pcaone_gpu_stream_info(pcaone_gpu_ctx* ctx, int* streamed, double* bytes_fetched);
 
 /* ---- operator: replaces RsvdOpData and subclasses (src/Halko.hpp) ------- */
 /* Constructor of Normal/FancyRsvdOpData: draws Omega (initOmg, Halko.cpp:15-23). */

@@ -81,6 +81,37 @@ def shuffle_columns(n: int) -> np.ndarray:
     return out
 
 
+def permute_plink_order(nsnps: int, nsamples: int, bands: int, buffer_gb: int = 2) -> np.ndarray:
+    """The SNP order of the reference's out-of-core window method: order[p] is
+    the .bed row that permute_plink (src/FilePlink.cpp:303-408) writes at row
+    p of the rewritten file.  Restated from its index arithmetic (ia -> ib,
+    :383-393), without the file I/O: buffers of twoGB_snps SNPs (:311-314),
+    band starts bandidx (:328-341), a shorter last buffer (:365-374)."""
+    bps = (nsamples + 3) // 4
+    two_gb_snps = min(int(np.floor(1073741824.0 * buffer_gb / bps)), nsnps)
+    bufsize = two_gb_snps // bands
+    two_gb_snps = bufsize * bands
+    bufidx = bufsize
+    nblocks = (nsnps + two_gb_snps - 1) // two_gb_snps
+    modr2 = nsnps % two_gb_snps
+    modr, bandsize = nsnps % bands, (nsnps + bands - 1) // bands
+    bandidx = [i * bandsize if (modr == 0 or i < modr) else modr * bandsize + (bandsize - 1) * (i - modr)
+               for i in range(bands)]
+    order = np.full(nsnps, -1, dtype=np.int64)
+    for i in range(nblocks):
+        if i == nblocks - 1 and modr2 != 0:
+            snps2 = nsnps - (nblocks - 1) * two_gb_snps
+            bufsize = (snps2 + bands - 1) // bands
+            modr2 = snps2 % bands
+        for b in range(bands):
+            last = bufsize - 1
+            take_last = i != nblocks - 1 or b < modr2 or modr2 == 0
+            for j in range(last + (1 if take_last else 0)):
+                order[i * bufidx + bandidx[b] + j] = i * two_gb_snps + j * bands + b
+    assert (order >= 0).all() and len(set(order.tolist())) == nsnps
+    return order
+
+
 # ----------------------------------------------------------------------------
 # PLINK decode, counts, allele frequency (src/FilePlink.cpp:26-110)
 # ----------------------------------------------------------------------------

@@ -26,7 +26,10 @@
 // Outputs (numpy .npy, float64 column-major / int64):
 //   F.npy         allele frequencies after the AF pass (src/FilePlink.cpp:33-62; PLINK only)
 //   U.npy S.npy V.npy   final operator state (src/Halko.cpp:46-97)
-//   perm.npy      the in-core column permutation (src/RSVD.hpp:61-78), if any
+//   perm.npy      the column permutation, if any: in core that of
+//                 src/RSVD.hpp:61-78; out of core (-m with the window
+//                 method's shuffle) that of permute_plink
+//                 (src/FilePlink.cpp:303-408, as src/Main.cpp:120-130 runs it)
 //   Omg0.npy      the initial random test matrix (src/Halko.cpp:15-23)
 //   G0.npy        optional (--dump-g0 as first option): the decoded, centred
 //                 matrix before standardisation (N x M), small inputs only
@@ -131,7 +134,14 @@ int main(int argc, char** argv) {
   }
   using clk = std::chrono::steady_clock;
   const auto t0 = clk::now();
+  // out-of-core (-m) with the window method's shuffle: the reference rewrites
+  // the .bed in its structured order first and runs on that file
+  // (src/Main.cpp:120-130); the rewritten files go to OUTDIR/ooc.perm.*
+  const bool ooc_permutation = params.perm && params.out_of_core && params.file_t == FileType::PLINK;
+  PermMat ooc_perm;
+  if (ooc_permutation) ooc_perm = permute_plink(params.filein, outdir + "/ooc", params.buffer, params.bands);
   Data* data = params.file_t == FileType::PLINK ? (Data*)new FileBed(params) : (Data*)new FileBin(params);
+  if (ooc_permutation) data->perm = ooc_perm;
   data->prepare();
   const auto t1 = clk::now();
   if (timing) dump_g0 = false;

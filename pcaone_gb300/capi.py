@@ -34,6 +34,8 @@ EXPORTS = [
     "pcaone_gpu_mlp_stats", "pcaone_gpu_mlp_forward_backward", "pcaone_gpu_load_dense",
     "pcaone_gpu_load_binary_file_image", "pcaone_gpu_load_synthetic_dense", "pcaone_gpu_project",
     "pcaone_gpu_random_omega", "pcaone_gpu_shuffle_order", "pcaone_gpu_set_wait_limit",
+    "pcaone_gpu_load_bed_stream", "pcaone_gpu_load_bed_file_image_stream", "pcaone_gpu_stream_plan",
+    "pcaone_gpu_stream_info", "pcaone_gpu_ooc_order",
 ]
 MLP_PARAMS, MLP_INPUTS = 82689, 64
 
@@ -114,6 +116,12 @@ def load(path: str = LIBPATH) -> ctypes.CDLL:
     lib.pcaone_gpu_random_omega.argtypes = [c_int, c_int, c_uint64, c_uint32, c_void_p]
     lib.pcaone_gpu_shuffle_order.argtypes = [c_uint64, c_void_p]
     lib.pcaone_gpu_set_wait_limit.argtypes = [c_void_p, ctypes.c_longlong]
+    lib.pcaone_gpu_load_bed_stream.argtypes = [c_void_p, c_void_p, c_uint64, c_uint32, c_uint64, c_uint32]
+    lib.pcaone_gpu_load_bed_file_image_stream.argtypes = [c_void_p, c_void_p, c_uint64, c_uint64, c_uint32,
+                                                          c_uint64, c_uint32]
+    lib.pcaone_gpu_ooc_order.argtypes = [c_uint64, c_uint32, c_int, c_uint32, c_void_p]
+    lib.pcaone_gpu_stream_plan.argtypes = [c_uint64, c_uint32, c_int, c_int, c_uint64, P(c_uint64), P(c_uint64)]
+    lib.pcaone_gpu_stream_info.argtypes = [c_void_p, P(c_int), P(c_double)]
     for name in EXPORTS:
         if name not in ("pcaone_gpu_default_params", "pcaone_gpu_last_error", "pcaone_gpu_mlp_default_params"):
             getattr(lib, name).restype = c_int
@@ -137,6 +145,26 @@ def shuffle_order(n: int) -> np.ndarray:
     rc = load().pcaone_gpu_shuffle_order(n, out.ctypes.data)
     if rc != PCAONE_OK:
         raise PcaoneError(rc, "pcaone_gpu_shuffle_order failed")
+    return out
+
+
+def stream_plan(nsnps: int, nsamples: int, svd: int, bands: int, device_budget: int):
+    """The out-of-core block plan (pcaone_gpu_stream_plan): (SNPs per block,
+    blocks).  Host only; PcaoneError(PCAONE_E_LIMIT) when the budget holds
+    fewer than two blocks."""
+    b, nb = c_uint64(0), c_uint64(0)
+    rc = load().pcaone_gpu_stream_plan(nsnps, nsamples, svd, bands, device_budget, ctypes.byref(b), ctypes.byref(nb))
+    if rc != PCAONE_OK:
+        raise PcaoneError(rc, "pcaone_gpu_stream_plan failed")
+    return int(b.value), int(nb.value)
+
+
+def ooc_order(nsnps: int, nsamples: int, bands: int, buffer_gb: int = 2) -> np.ndarray:
+    """The out-of-core SNP order (pcaone_gpu_ooc_order): host only."""
+    out = np.empty(nsnps, dtype=np.int32)
+    rc = load().pcaone_gpu_ooc_order(nsnps, nsamples, bands, buffer_gb, out.ctypes.data)
+    if rc != PCAONE_OK:
+        raise PcaoneError(rc, "pcaone_gpu_ooc_order failed")
     return out
 
 
@@ -230,6 +258,32 @@ class Context:
         buf = np.frombuffer(image, dtype=np.uint8)
         self._check(self.lib.pcaone_gpu_load_bed_file_image(self.h, _ptr(buf), buf.size, nsnps, nsamples))
         self.nsamples, self.nsnps = int(nsamples), int(nsnps)
+
+    def load_bed_stream(self, packed, nsamples: int, device_budget: int = 0, nsnps: int | None = None,
+                        buffer_gb: int = 2):
+        """Out-of-core load (pcaone_gpu_load_bed_stream): ``packed`` is a
+        numpy array of rows or an address of host memory (then give nsnps)."""
+        if isinstance(packed, np.ndarray):
+            packed = np.ascontiguousarray(packed, dtype=np.uint8)
+            ptr, nsnps = _ptr(packed), packed.shape[0]
+        else:
+            ptr = c_void_p(int(packed))
+        self._check(self.lib.pcaone_gpu_load_bed_stream(self.h, ptr, int(nsnps), nsamples, int(device_budget),
+                                                        int(buffer_gb)))
+        self.nsamples, self.nsnps = int(nsamples), int(nsnps)
+
+    def load_bed_file_image_stream(self, image: bytes, nsnps: int, nsamples: int, device_budget: int = 0,
+                                   buffer_gb: int = 2):
+        buf = np.frombuffer(image, dtype=np.uint8)
+        self._check(self.lib.pcaone_gpu_load_bed_file_image_stream(self.h, _ptr(buf), buf.size, nsnps, nsamples,
+                                                                   int(device_budget), int(buffer_gb)))
+        self.nsamples, self.nsnps = int(nsamples), int(nsnps)
+
+    def stream_info(self):
+        """(streamed, bytes copied into the device slots since the last call)."""
+        on, nbytes = c_int(0), c_double(0)
+        self._check(self.lib.pcaone_gpu_stream_info(self.h, ctypes.byref(on), ctypes.byref(nbytes)))
+        return bool(on.value), float(nbytes.value)
 
     def load_bed_device(self, dev_ptr: int, pitch: int, nsnps: int, nsamples: int):
         self._check(self.lib.pcaone_gpu_load_bed_device(self.h, c_void_p(dev_ptr), pitch, nsnps, nsamples))

@@ -6,6 +6,7 @@
 // g/2 scale):  00 two copies of A1, 01 missing, 10 one copy, 11 no copy.
 #include <cuda_fp16.h>
 
+#include "../../include/pcaone_gpu.h"
 #include "internal.cuh"
 
 namespace pcaone {
@@ -147,7 +148,49 @@ __global__ void k_synth(uint8_t* __restrict__ bed, int64_t stride, int64_t snp0,
   bed[jl * stride + q] = (uint8_t)byte;
 }
 
+// Rows perm[0 .. nrows) of src into consecutive rows of dst (stride bytes
+// each, a multiple of 16), for sources across the host link (pinned host
+// memory mapped into the device address space), whose latency wants many
+// loads in flight: the rows' 16-byte chunks are strided over the grid, and
+// every thread issues kGatherDepth loads before it stores them.  Consecutive
+// threads take consecutive chunks of a row (coalesced).
+constexpr int kGatherDepth = 8;
+__global__ void __launch_bounds__(256) k_gather_rows_deep(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
+                                                          int64_t stride, const int32_t* __restrict__ perm,
+                                                          int64_t nrows) {
+  const int64_t cpr = stride >> 4;
+  const int64_t total = nrows * cpr;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q0 < total; q0 += step * kGatherDepth) {
+    uint4 v[kGatherDepth];
+    int64_t d[kGatherDepth];
+#pragma unroll
+    for (int u = 0; u < kGatherDepth; ++u) {
+      const int64_t q = q0 + u * step;
+      d[u] = -1;
+      if (q < total) {
+        const int64_t r = q / cpr, c = q - r * cpr;
+        const int64_t srow = perm ? (int64_t)perm[r] : r;
+        v[u] = *reinterpret_cast<const uint4*>(src + srow * stride + (c << 4));
+        d[u] = r * stride + (c << 4);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kGatherDepth; ++u)
+      if (d[u] >= 0) *reinterpret_cast<uint4*>(dst + d[u]) = v[u];
+  }
+}
+
 }  // namespace
+
+void launch_gather_rows_deep(const uint8_t* src, uint8_t* dst, int64_t stride, const int32_t* perm, int64_t nrows,
+                             int ctas, cudaStream_t s) {
+  if (nrows <= 0) return;
+  if ((stride & 15) != 0 || ((uintptr_t)src & 15u) != 0 || ((uintptr_t)dst & 15u) != 0)
+    throw Error(PCAONE_E_ARG, "internal: row gather needs 16-byte aligned rows");
+  k_gather_rows_deep<<<ctas, 256, 0, s>>>(src, dst, stride, perm, nrows);
+  PCAONE_LAUNCH_CHECK();
+}
 
 void launch_repitch(const uint8_t* src, int64_t src_pitch, uint8_t* dst, int64_t dst_pitch, int64_t nrows, int64_t bps,
                     cudaStream_t s) {

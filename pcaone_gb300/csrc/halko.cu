@@ -177,17 +177,64 @@ struct Context {
   double prof_ms[4] = {0, 0, 0, 0}, prof_flops[4] = {0, 0, 0, 0};
   long long prof_launches[4] = {0, 0, 0, 0};
 
-  BedView view() const { return BedView{bed.p, stride, M, N}; }
+  // Out-of-core streaming (load_bed_stream; FileBed::read_block_initial,
+  // src/FilePlink.cpp:122-218): the packed rows stay in pinned host memory in
+  // the device row layout, mapped into the device address space, where the
+  // kernels that read the matrix once per call (counts, missing-entry index,
+  // matvec, projection, the FP32 form's products) read them over the host
+  // link.  The tensor-core window products read each SNP block from one of two
+  // device slots, filled on fetch_stream while the previous block's products
+  // run (block plan: stream_block_size).
+  struct Slot {
+    DBuf<uint8_t> buf;
+    int64_t pos0 = -1, n = 0, rows = 0;  // block held (working positions), capacity in rows
+    cudaEvent_t ready = nullptr;         // the fill of the block has landed
+    cudaEvent_t idle = nullptr;          // the last product reading the slot has run
+    CUtensorMap g{}, h{}, g8{}, h8{};
+  };
+  bool streamed = false;
+  int sm_count = 152;
+  uint8_t* hbed = nullptr;      // pinned host rows, M x stride bytes
+  uint8_t* hbed_dev = nullptr;  // their device address
+  size_t hbed_bytes = 0;
+  uint64_t stream_budget = 0;   // device bytes for the two slots (0: no bound)
+  unsigned stream_buffer_gb = 2;  // --buffer of the out-of-core shuffle (src/Cmd.hpp:52)
+  Slot slots[2];
+  int slot_cur = -1;
+  cudaStream_t fetch_stream = nullptr;
+  double stream_bytes = 0;      // bytes fetched into the slots since the last query
+  const uint8_t* rows_ptr() const { return streamed ? hbed_dev : bed.p; }
+  uint8_t* rows_mut() { return streamed ? hbed_dev : bed.p; }
+  BedView view() const { return BedView{rows_ptr(), stride, M, N}; }
+  void invalidate_slots() {
+    for (auto& s : slots) s.pos0 = -1, s.n = 0;
+    slot_cur = -1;
+  }
+  void free_host_rows() {
+    if (fetch_stream) cudaStreamSynchronize(fetch_stream);
+    if (hbed) cudaFreeHost(hbed);
+    hbed = hbed_dev = nullptr;
+    hbed_bytes = 0;
+    for (auto& s : slots) s.buf.release();
+    invalidate_slots();
+  }
 
   // host loads (load_bed_host): a copy stream, two staging buffers and their
   // events; ev_free[2] marks where the context's stream stood when a load began
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[3] = {nullptr, nullptr, nullptr};
   DBuf<uint8_t> stage;
+  // out-of-core loads: padded chunks go back to the pinned host copy on a
+  // third stream (ev_ready: chunk prepared; ev_back: chunk copied back)
+  cudaStream_t back_stream = nullptr;
+  cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_back[2] = {nullptr, nullptr};
+  DBuf<uint8_t> stage2;
   void ensure_copy_stream() {
     if (!copy_stream) {
       PCAONE_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
-      for (auto* e : {&ev_copied[0], &ev_copied[1], &ev_free[0], &ev_free[1], &ev_free[2]})
+      PCAONE_CUDA(cudaStreamCreateWithFlags(&back_stream, cudaStreamNonBlocking));
+      for (auto* e : {&ev_copied[0], &ev_copied[1], &ev_free[0], &ev_free[1], &ev_free[2], &ev_ready[0],
+                      &ev_ready[1], &ev_back[0], &ev_back[1]})
         PCAONE_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
     PCAONE_CUDA(cudaEventRecord(ev_free[2], stream));
@@ -215,11 +262,20 @@ struct Context {
     ev_used = 0;
   }
   ~Context() {
+    free_host_rows();
+    for (auto& s : slots)
+      for (auto e : {s.ready, s.idle})
+        if (e) cudaEventDestroy(e);
+    if (fetch_stream) cudaStreamDestroy(fetch_stream);
     for (auto e : ev_pool) cudaEventDestroy(e);
     if (copy_stream) {
       cudaStreamSynchronize(copy_stream);
+      cudaStreamSynchronize(back_stream);
       cudaStreamDestroy(copy_stream);
-      for (auto e : {ev_copied[0], ev_copied[1], ev_free[0], ev_free[1], ev_free[2]}) cudaEventDestroy(e);
+      cudaStreamDestroy(back_stream);
+      for (auto e : {ev_copied[0], ev_copied[1], ev_free[0], ev_free[1], ev_free[2], ev_ready[0], ev_ready[1],
+                     ev_back[0], ev_back[1]})
+        cudaEventDestroy(e);
     }
   }
 };
@@ -230,7 +286,7 @@ struct Context {
 // bytes of one staging buffer of the host loads
 constexpr size_t kStageBytes = (size_t)512 << 20;
 
-static void load_common(Context& c, uint64_t nsnps, uint32_t nsamples, bool dense = false) {
+static void load_common(Context& c, uint64_t nsnps, uint32_t nsamples, bool dense = false, bool stream = false) {
   if (nsamples == 0 || nsnps == 0) throw Error(PCAONE_E_ARG, "empty genotype matrix");
   if (nsnps > 0x7fffffffull) throw Error(PCAONE_E_LIMIT, "more than 2^31-1 SNPs");
   if (nsamples > 0x7fffff00u) throw Error(PCAONE_E_LIMIT, "too many samples");
@@ -239,7 +295,32 @@ static void load_common(Context& c, uint64_t nsnps, uint32_t nsamples, bool dens
   c.npad = round_up(c.N, 128);
   c.dense = dense;
   c.stride = dense ? (int64_t)c.npad * 2 : c.npad / 4;
-  c.bed.ensure((size_t)c.M * c.stride, c.stream, true);
+  c.invalidate_slots();
+  c.stream_bytes = 0;
+  if (stream) {
+    // the rows go to pinned, mapped host memory; no device copy of the matrix
+    c.bed.release();
+    c.bedp.release();
+    const size_t bytes = (size_t)c.M * c.stride;
+    if (bytes != c.hbed_bytes) {
+      c.free_host_rows();
+      void* h = nullptr;
+      if (cudaHostAlloc(&h, bytes, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess) {
+        cudaGetLastError();
+        throw Error(PCAONE_E_NOMEM, "out-of-core load: cannot pin " + std::to_string(bytes) + " bytes of host memory");
+      }
+      c.hbed = static_cast<uint8_t*>(h);
+      c.hbed_bytes = bytes;
+      void* d = nullptr;
+      PCAONE_CUDA(cudaHostGetDevicePointer(&d, h, 0));
+      c.hbed_dev = static_cast<uint8_t*>(d);
+    }
+    c.streamed = true;
+  } else {
+    c.free_host_rows();
+    c.streamed = false;
+    c.bed.ensure((size_t)c.M * c.stride, c.stream, true);
+  }
   c.counts.ensure((size_t)c.M * 4, c.stream, false);
   c.F.ensure((size_t)c.M, c.stream, false);
   c.have_data = false;
@@ -252,7 +333,7 @@ static void load_common(Context& c, uint64_t nsnps, uint32_t nsamples, bool dens
 }
 
 static void finish_load(Context& c) {
-  launch_sanitize_padding(c.bed.p, c.stride, c.M, c.N, c.stream);
+  launch_sanitize_padding(c.rows_mut(), c.stride, c.M, c.N, c.stream);
   launch_counts(c.view(), c.counts.p, c.F.p, c.stream);
   c.counts_total_missing = -1;
   c.have_data = true;
@@ -273,9 +354,18 @@ static void ensure_missing_total(Context& c) {
 // into two staging buffers on a second stream (large linear copies run at the
 // host link's rate, where one pitched copy of short rows does not) while the
 // context's stream re-pitches the previous chunk into the padded rows.
-static void load_bed_host(Context& c, const uint8_t* packed, uint64_t nsnps, uint32_t nsamples) {
-  load_common(c, nsnps, nsamples);
+//
+// Out-of-core (stream): the same pipeline with the re-pitch writing the padded
+// rows into the pinned host copy through its device address.
+static void load_rows_to_host_copy(Context& c, const uint8_t* packed, int64_t bps);
+
+static void load_bed_host(Context& c, const uint8_t* packed, uint64_t nsnps, uint32_t nsamples, bool stream = false) {
+  load_common(c, nsnps, nsamples, false, stream);
   const int64_t bps = ((int64_t)nsamples + 3) / 4;
+  if (stream) {
+    load_rows_to_host_copy(c, packed, bps);
+    return;
+  }
   if (bps == c.stride) {
     PCAONE_CUDA(cudaMemcpyAsync(c.bed.p, packed, (size_t)c.M * bps, cudaMemcpyHostToDevice, c.stream));
     finish_load(c);
@@ -295,10 +385,46 @@ static void load_bed_host(Context& c, const uint8_t* packed, uint64_t nsnps, uin
                                 c.copy_stream));
     PCAONE_CUDA(cudaEventRecord(c.ev_copied[b], c.copy_stream));
     PCAONE_CUDA(cudaStreamWaitEvent(c.stream, c.ev_copied[b], 0));
-    launch_repitch(buf, bps, c.bed.p + (size_t)j0 * c.stride, c.stride, n, bps, c.stream);
+    launch_repitch(buf, bps, c.rows_mut() + (size_t)j0 * c.stride, c.stride, n, bps, c.stream);
     PCAONE_CUDA(cudaEventRecord(c.ev_free[b], c.stream));
   }
   finish_load(c);
+}
+
+// Out-of-core load: chunks of whole rows pass through the device (copied in,
+// re-pitched into padded rows, padding bits cleared, counted) and go back to
+// the pinned host copy; both copies run on copy engines, in opposite
+// directions, while the context's stream prepares the previous chunk.
+static void load_rows_to_host_copy(Context& c, const uint8_t* packed, int64_t bps) {
+  c.ensure_copy_stream();
+  const int64_t rows = std::max<int64_t>(1, std::min<int64_t>(c.M, (int64_t)(kStageBytes / c.stride)));
+  c.stage.ensure((size_t)(2 * rows * bps), c.stream, false);
+  c.stage2.ensure((size_t)(2 * rows * c.stride), c.stream, false);
+  for (int64_t j0 = 0, q = 0; j0 < c.M; j0 += rows, ++q) {
+    const int b = (int)(q & 1);
+    const int64_t n = std::min<int64_t>(rows, c.M - j0);
+    uint8_t* in = c.stage.p + (size_t)b * rows * bps;
+    uint8_t* out = c.stage2.p + (size_t)b * rows * c.stride;
+    // `in` is free once the chunk two back was re-pitched; `out` once it was copied back
+    PCAONE_CUDA(cudaStreamWaitEvent(c.copy_stream, q >= 2 ? c.ev_ready[b] : c.ev_free[2], 0));
+    PCAONE_CUDA(cudaMemcpyAsync(in, packed + (size_t)j0 * bps, (size_t)n * bps, cudaMemcpyHostToDevice,
+                                c.copy_stream));
+    PCAONE_CUDA(cudaEventRecord(c.ev_copied[b], c.copy_stream));
+    PCAONE_CUDA(cudaStreamWaitEvent(c.stream, c.ev_copied[b], 0));
+    if (q >= 2) PCAONE_CUDA(cudaStreamWaitEvent(c.stream, c.ev_back[b], 0));
+    launch_repitch(in, bps, out, c.stride, n, bps, c.stream);
+    launch_sanitize_padding(out, c.stride, n, c.N, c.stream);
+    launch_counts(BedView{out, c.stride, n, c.N}, c.counts.p + (size_t)j0 * 4, c.F.p + j0, c.stream);
+    PCAONE_CUDA(cudaEventRecord(c.ev_ready[b], c.stream));
+    PCAONE_CUDA(cudaStreamWaitEvent(c.back_stream, c.ev_ready[b], 0));
+    PCAONE_CUDA(cudaMemcpyAsync(c.hbed + (size_t)j0 * c.stride, out, (size_t)n * c.stride, cudaMemcpyDeviceToHost,
+                                c.back_stream));
+    PCAONE_CUDA(cudaEventRecord(c.ev_back[b], c.back_stream));
+  }
+  // readers of the host copy (the context's stream) start after the last copy back
+  for (int b = 0; b < 2; ++b) PCAONE_CUDA(cudaStreamWaitEvent(c.stream, c.ev_back[b], 0));
+  c.counts_total_missing = -1;
+  c.have_data = true;
 }
 
 static void load_bed_device(Context& c, const void* src, uint64_t pitch, uint64_t nsnps, uint32_t nsamples) {
@@ -403,27 +529,26 @@ static void upload_omega0(Context& c) {
   PCAONE_CUDA(cudaStreamSynchronize(c.stream));
 }
 
-// tensor-core buffers, launch shapes and TMA descriptors for windows of up to
-// `win` SNPs
-static void tc_make_bed_maps(Context& c) {
+// TMA descriptors of the packed rows (or FP16 rows) the tensor-core products
+// read: `rows` rows from `base` (the whole matrix, or a streaming slot)
+static void make_bed_maps(const Context& c, const uint8_t* base, int64_t rows, CUtensorMap& g, CUtensorMap& h,
+                          CUtensorMap& g8, CUtensorMap& h8) {
   if (c.dense) {
     // FP16 rows: G tiles of 64 samples x 128 SNPs (128-byte swizzle), H tiles
     // of 128 samples x 64 SNPs
-    tc::make_map_2d(&c.map_bed_g, c.bed_work, tc::kMapF16, (uint64_t)c.npad, (uint64_t)c.M, (uint64_t)c.stride, 64,
-                    128, true);
-    tc::make_map_2d(&c.map_bed_h, c.bed_work, tc::kMapF16, (uint64_t)c.npad, (uint64_t)c.M, (uint64_t)c.stride, 128,
-                    64, false);
+    tc::make_map_2d(&g, base, tc::kMapF16, (uint64_t)c.npad, (uint64_t)rows, (uint64_t)c.stride, 64, 128, true);
+    tc::make_map_2d(&h, base, tc::kMapF16, (uint64_t)c.npad, (uint64_t)rows, (uint64_t)c.stride, 128, 64, false);
     return;
   }
-  tc::make_map_2d(&c.map_bed_g, c.bed_work, tc::kMapU8, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 16,
-                  128, false);
-  tc::make_map_2d(&c.map_bed_h, c.bed_work, tc::kMapU8, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 32,
-                  64, false);
+  tc::make_map_2d(&g, base, tc::kMapU8, (uint64_t)c.stride, (uint64_t)rows, (uint64_t)c.stride, 16, 128, false);
+  tc::make_map_2d(&h, base, tc::kMapU8, (uint64_t)c.stride, (uint64_t)rows, (uint64_t)c.stride, 32, 64, false);
   // E4M3 form: 128 samples (32 bytes) per G stage, 128 SNP rows per H stage
-  tc::make_map_2d(&c.map_bed_g8, c.bed_work, tc::kMapU8, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 32,
-                  128, false);
-  tc::make_map_2d(&c.map_bed_h8, c.bed_work, tc::kMapU8, (uint64_t)c.stride, (uint64_t)c.M, (uint64_t)c.stride, 32,
-                  128, false);
+  tc::make_map_2d(&g8, base, tc::kMapU8, (uint64_t)c.stride, (uint64_t)rows, (uint64_t)c.stride, 32, 128, false);
+  tc::make_map_2d(&h8, base, tc::kMapU8, (uint64_t)c.stride, (uint64_t)rows, (uint64_t)c.stride, 32, 128, false);
+}
+
+static void tc_make_bed_maps(Context& c) {
+  make_bed_maps(c, c.bed_work, c.M, c.map_bed_g, c.map_bed_h, c.map_bed_g8, c.map_bed_h8);
 }
 
 // launch shapes of one window's tensor-core products: G tiles of 128 SNPs x
@@ -447,6 +572,90 @@ static void tc_shapes(const Context& c, int win, int S, bool fp8, int& chunk, in
   }
   nchunks = ceil_div(c.npad, chunk);
   nsplit = ceil_div(win, per_split);
+}
+
+// Out-of-core block plan (Data::prepare, src/Data.cpp:40-84): SNPs per block
+// when two device slots of stride-byte rows share `budget` bytes (0: no
+// bound).  The window method streams its own windows (ceil(M / bands) SNPs,
+// the blocks the products use in core too), which two slots must hold: the
+// reference instead cuts each window into bandFactor blocks (Data.cpp:66-77),
+// which the products here do not need.  The single-pass method uses the in-core
+// blocks of at most 16384 SNPs, smaller when the budget asks, balanced over
+// the blocks.  Returns 0 when the budget cannot hold two blocks.
+int64_t stream_block_size(int64_t M, int64_t stride, int svd, int bands, uint64_t budget) {
+  if (M <= 0 || stride <= 0) return 0;
+  const uint64_t per_slot = budget / 2;
+  if (svd == PCAONE_SVD_WINDOW) {
+    if (bands <= 0) return 0;
+    const int64_t win = (M + bands - 1) / bands;
+    return budget == 0 || (uint64_t)win * (uint64_t)stride <= per_slot ? win : 0;
+  }
+  int64_t cap = 16384;
+  if (budget) cap = std::min<int64_t>(cap, (int64_t)(per_slot / (uint64_t)stride));
+  if (cap <= 0) return 0;
+  const int64_t nblk = (M + cap - 1) / cap;
+  return (M + nblk - 1) / nblk;
+}
+
+// The SNP order of the reference's out-of-core window method, whose
+// permute_plink (src/FilePlink.cpp:303-408) rewrites the .bed before the run:
+// the file is read in buffers of per_buf consecutive SNPs (as many as
+// buffer_gb GiB of rows hold, cut to a multiple of the bands), and band b takes
+// from each buffer the SNPs at offsets b, b + bands, b + 2 bands, ...; in the
+// rewritten file band b starts where ceil(M / bands)-SNP bands would (the
+// first M mod bands bands) or hold one SNP fewer, and buffer i's share of a
+// band sits at i * (per_buf / bands) within it.  A last, shorter buffer gives
+// its first (count mod bands) bands one SNP more than the others.
+// order[p] = the file row at working position p.  Returns false when a buffer
+// holds fewer SNPs than there are bands.
+bool host_ooc_order(int64_t M, int64_t bps, unsigned buffer_gb, int bands, int32_t* order) {
+  int64_t per_buf = (int64_t)std::floor(1073741824.0 * (double)buffer_gb / (double)bps);
+  per_buf = std::min(per_buf, M);
+  const int64_t per_band0 = per_buf / bands;
+  if (per_band0 == 0) return false;
+  per_buf = per_band0 * bands;
+  const int64_t big = (M + bands - 1) / bands, rem = M % bands;
+  const int64_t nbuf = (M + per_buf - 1) / per_buf, tail = M % per_buf;
+  for (int64_t i = 0; i < nbuf; ++i) {
+    const bool short_buf = i == nbuf - 1 && tail != 0;
+    const int64_t per_band = short_buf ? (tail + bands - 1) / bands : per_band0;
+    const int64_t full_bands = short_buf ? tail % bands : 0;  // 0: every band takes per_band
+    for (int64_t b = 0; b < bands; ++b) {
+      const int64_t start = rem == 0 || b < rem ? b * big : rem * big + (big - 1) * (b - rem);
+      const int64_t nj = full_bands != 0 && b >= full_bands ? per_band - 1 : per_band;
+      for (int64_t j = 0; j < nj; ++j) order[start + i * per_band0 + j] = (int32_t)(i * per_buf + j * bands + b);
+    }
+  }
+  return true;
+}
+
+// positions per SNP window of the current operator: the winSVD band blocks
+// (src/Halko.cpp:169-172) or the sSVD blocks of at most 16384 SNPs (the
+// out-of-core block plan when the rows are streamed)
+static int64_t window_size(const Context& c) {
+  if (c.streamed) return stream_block_size(c.M, c.stride, c.P.svd, c.P.bands, c.stream_budget);
+  if (c.P.svd == PCAONE_SVD_WINDOW) return (c.M + c.P.bands - 1) / c.P.bands;
+  const int64_t nwin = (c.M + 16383) / 16384;
+  return (c.M + nwin - 1) / nwin;
+}
+
+// two device slots of `rows` packed rows, their events and TMA descriptors
+static void setup_slots(Context& c, int64_t rows) {
+  if (c.fetch_stream) PCAONE_CUDA(cudaStreamSynchronize(c.fetch_stream));  // no fill in flight into a slot
+  if (!c.fetch_stream) {
+    int lo = 0, hi = 0;
+    PCAONE_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    PCAONE_CUDA(cudaStreamCreateWithPriority(&c.fetch_stream, cudaStreamNonBlocking, hi));
+  }
+  for (auto& sl : c.slots) {
+    if (!sl.ready) PCAONE_CUDA(cudaEventCreateWithFlags(&sl.ready, cudaEventDisableTiming));
+    if (!sl.idle) PCAONE_CUDA(cudaEventCreateWithFlags(&sl.idle, cudaEventDisableTiming));
+    sl.buf.ensure((size_t)rows * c.stride, c.stream, false);
+    sl.rows = rows;
+    make_bed_maps(c, sl.buf.p, rows, sl.g, sl.h, sl.g8, sl.h8);
+    PCAONE_CUDA(cudaEventRecord(sl.idle, c.stream));
+  }
+  c.invalidate_slots();
 }
 
 static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
@@ -490,8 +699,13 @@ static void tc_setup(Context& c, int win, const std::vector<int64_t>& lens) {
   c.cr_cnt.ensure(1, c.stream, true);
   c.tpart.ensure(need_part, c.stream, false);
   c.thpart.ensure(need_hpart, c.stream, false);
-  c.bed_work = c.bed.p;
-  tc_make_bed_maps(c);
+  if (c.streamed) {
+    c.bed_work = nullptr;
+    setup_slots(c, win);
+  } else {
+    c.bed_work = c.bed.p;
+    tc_make_bed_maps(c);
+  }
   const int sl = c.dense ? tc::kMapF16 : tc::kMapBF16;  // slice digits: FP16 for dense input, else BF16
   tc::make_map_2d(&c.map_w, c.wsl.p, sl, (uint64_t)c.npad, (uint64_t)smax * LP, (uint64_t)c.npad * 2, 64, LP, true);
   tc::make_map_2d(&c.map_gt, c.gt.p, sl, (uint64_t)c.ldg, (uint64_t)smax * LP, (uint64_t)c.ldg * 2, 64, LP, true);
@@ -571,8 +785,10 @@ static void op_init(Context& c, const pcaone_gpu_params& p) {
   c.V.ensure((size_t)c.M * c.k, c.stream);
   c.Vpre.ensure((size_t)c.M * c.k, c.stream);
   // window scratch: the largest need over the distinct window lengths of the schedule
-  const int64_t win = p.svd == PCAONE_SVD_WINDOW ? (c.M + p.bands - 1) / p.bands
-                                                   : (c.M + (c.M + 16383) / 16384 - 1) / ((c.M + 16383) / 16384);
+  const int64_t win = window_size(c);
+  if (win <= 0)
+    throw Error(PCAONE_E_LIMIT, "out-of-core: the device budget of " + std::to_string(c.stream_budget) +
+                                    " bytes does not hold two SNP blocks (raise it, or the number of windows)");
   std::vector<int64_t> lens = {win, c.M % std::max<int64_t>(1, win)};
   size_t need_part = 1, need_hpart = 1;
   for (int64_t n : lens) {
@@ -743,13 +959,6 @@ static void fit_with_pi(Context& c) {
   c.t_em += secs(t0, clk::now());
 }
 
-// positions per SNP window of the current operator: the winSVD band blocks
-// (src/Halko.cpp:169-172) or the in-core sSVD blocks of at most 16384 SNPs
-static int64_t window_size(const Context& c) {
-  if (c.P.svd == PCAONE_SVD_WINDOW) return (c.M + c.P.bands - 1) / c.P.bands;
-  const int64_t nwin = (c.M + 16383) / 16384;
-  return (c.M + nwin - 1) / nwin;
-}
 
 // missing entries grouped by (window, sample), in working order: a count pass
 // over the packed rows, an exclusive scan, and a fill pass
@@ -823,16 +1032,22 @@ static void prepare_epoch0(Context& c, bool window) {
     c.bandsize = 1;
     c.blocksize = (c.M + c.P.bands - 1) / c.P.bands;
     if (c.P.perm && !(c.update && c.P.emu) && !c.permuted) {
-      // PCAone::permute_matrix (src/RSVD.hpp:61-70): column i <- column perm[i]
+      // PCAone::permute_matrix (src/RSVD.hpp:61-70): column i <- column perm[i];
+      // out of core, the order permute_plink gives the rewritten file
+      // (src/Main.cpp:120-130)
       c.perm_host.resize((size_t)c.M);
-      host_shuffle_columns(c.M, c.perm_host.data());
+      if (!c.streamed)
+        host_shuffle_columns(c.M, c.perm_host.data());
+      else if (!host_ooc_order(c.M, ((int64_t)c.N + 3) / 4, c.stream_buffer_gb, c.P.bands, c.perm_host.data()))
+        throw Error(PCAONE_E_ARG, "out-of-core shuffle: a buffer of the --buffer size holds fewer SNPs than windows");
       PCAONE_CUDA(cudaMemcpyAsync(c.perm.p, c.perm_host.data(), c.M * sizeof(int32_t), cudaMemcpyHostToDevice,
                                   c.stream));
       PCAONE_CUDA(cudaStreamSynchronize(c.stream));
       c.permuted = true;
       c.miss_valid = false;
       c.bk_valid = false;
-      if (c.tc) {
+      c.invalidate_slots();  // streamed blocks are gathered through the order
+      if (c.tc && !c.streamed) {
         c.bedp.ensure((size_t)c.M * c.stride, c.stream, false);
         tc::launch_gather_rows(c.bed.p, c.bedp.p, c.stride, c.perm.p, c.M, c.stream);
         c.bed_work = c.bedp.p;
@@ -842,6 +1057,65 @@ static void prepare_epoch0(Context& c, bool window) {
   }
   prepare_missing(c);
 }
+
+// ---- out-of-core streaming of SNP blocks (Halko.cpp:130-153, 227-268) ----
+
+// the slot holding the block [pos0, pos0 + n) of the working order, or -1
+static int find_slot(const Context& c, int64_t pos0, int64_t n) {
+  for (int s = 0; s < 2; ++s)
+    if (c.slots[s].pos0 == pos0 && c.slots[s].n == n) return s;
+  return -1;
+}
+
+// fills slot s with the block [pos0, pos0 + n) on the fetch stream once the
+// products that last read the slot have run: one host-to-device copy of the
+// contiguous rows, or, in a shuffled order, a gather kernel that reads the
+// rows through their device address
+static void fetch_block(Context& c, int s, int64_t pos0, int64_t n) {
+  Context::Slot& sl = c.slots[s];
+  if (n > sl.rows) throw Error(PCAONE_E_ARG, "internal: streamed block larger than its slot");
+  PCAONE_CUDA(cudaStreamWaitEvent(c.fetch_stream, sl.idle, 0));
+  if (!c.permuted) {
+    PCAONE_CUDA(cudaMemcpyAsync(sl.buf.p, c.hbed + (size_t)pos0 * c.stride, (size_t)n * c.stride,
+                                cudaMemcpyHostToDevice, c.fetch_stream));
+  } else {
+    // shuffled windows: a gather kernel reads the block's rows through their
+    // device address (scattered rows cross the host link at about 110 GB/s on
+    // this system whether a kernel or pitched copies move them; contiguous
+    // windows copy at about 170 GB/s)
+    launch_gather_rows_deep(c.hbed_dev, sl.buf.p, c.stride, c.perm.p + pos0, n, 4 * c.sm_count, c.fetch_stream);
+  }
+  PCAONE_CUDA(cudaEventRecord(sl.ready, c.fetch_stream));
+  sl.pos0 = pos0;
+  sl.n = n;
+  c.stream_bytes += (double)n * (double)c.stride;
+}
+
+// makes the block [pos0, pos0 + n) readable by the products on the context's
+// stream and points the TMA descriptors at its slot, then prefetches the block
+// that follows in schedule order (the next window, the first after the last)
+// into the other slot.  Returns the first position the slot holds.
+static int64_t acquire_block(Context& c, int64_t pos0, int64_t n) {
+  int s = find_slot(c, pos0, n);
+  if (s < 0) {
+    s = c.slot_cur == 0 ? 1 : 0;
+    fetch_block(c, s, pos0, n);
+  }
+  PCAONE_CUDA(cudaStreamWaitEvent(c.stream, c.slots[s].ready, 0));
+  c.slot_cur = s;
+  const Context::Slot& sl = c.slots[s];
+  c.map_bed_g = sl.g;
+  c.map_bed_h = sl.h;
+  c.map_bed_g8 = sl.g8;
+  c.map_bed_h8 = sl.h8;
+  const int64_t next = pos0 + n < c.M ? pos0 + n : 0;
+  const int64_t nn = std::min(window_size(c), c.M - next);
+  if (nn > 0 && find_slot(c, next, nn) < 0) fetch_block(c, 1 - s, next, nn);
+  return sl.pos0;
+}
+
+// the products of the current block are queued: its slot may be refilled after them
+static void release_block(Context& c) { PCAONE_CUDA(cudaEventRecord(c.slots[c.slot_cur].idle, c.stream)); }
 
 // tensor-core form of one window (prod_tc.cu)
 static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
@@ -876,8 +1150,11 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   auto close_mark = [&]() {
     if (c.profiling) PCAONE_CUDA(cudaEventRecord(c.ev_pool[c.ev_marks.back().second + 1], c.stream));
   };
+  // rows of the packed matrix the products read: the whole matrix in HBM, or
+  // the streamed block's slot
+  const int64_t row_base = c.streamed ? acquire_block(c, pos0, n) : 0;
   tc::GArgs ga{};
-  ga.pos0 = pos0;
+  ga.pos0 = pos0 - row_base;
   ga.nsnp = (int)n;
   ga.LP = LP;
   ga.nslice = S;
@@ -944,7 +1221,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   tc::launch_g_finish(fa, c.hexp.p, c.hunit.p, c.gmunit.p, c.cvec.p, tc::ColRedScratch{c.cr_part.p, c.cr_cnt.p},
                       c.stream);
   tc::HArgs ha{};
-  ha.pos0 = pos0;
+  ha.pos0 = pos0 - row_base;
   ha.nsnp = (int)n;
   ha.L = c.L;
   ha.LP = LP;
@@ -981,6 +1258,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   mark(fp8 ? 3 : 1);
   tc::launch_h(fp8 ? c.map_bed_h8 : c.map_bed_h, fp8 ? c.map_gt8 : c.map_gt, ha, c.stream);
   close_mark();
+  if (c.streamed) release_block(c);
   tc::HFinishArgs hf{};
   hf.nsamples = c.N;
   hf.npad = c.npad;
@@ -1284,7 +1562,7 @@ static void warm_start(Context& c) {
   const int32_t* perm = c.permuted ? c.perm.p : nullptr;
   c.smiss.ensure(c.N, c.stream, false);
   mlp::sample_missing(c.bk_ptr.p, c.bk_nwin, c.N, c.M, c.smiss.p, c.stream);
-  mlp::FeatureArgs fa{c.bed.p, c.stride, c.M, c.N, perm, c.F.p, c.U.p, c.V.p, c.smiss.p, c.counts.p, c.k,
+  mlp::FeatureArgs fa{c.rows_ptr(), c.stride, c.M, c.N, perm, c.F.p, c.U.p, c.V.p, c.smiss.p, c.counts.p, c.k,
                       std::min(c.k, 14), std::sqrt((double)c.N), std::sqrt((double)c.M)};
   const int T = (w.train_entries / w.batch) * w.batch, Hn = w.holdout_entries;
   if (T <= 0) throw Error(PCAONE_E_ARG, "warm start: fewer training genotypes than one batch");
@@ -1501,6 +1779,16 @@ static int guarded(pcaone_gpu_ctx* ctx, F&& fn) {
   }
 }
 
+static void check_bed_image(const uint8_t* image, uint64_t image_bytes, uint64_t nsnps, uint32_t nsamples) {
+  if (!image || image_bytes < 3) throw Error(PCAONE_E_FORMAT, "truncated .bed image");
+  if (image[0] != 0x6c || image[1] != 0x1b || image[2] != 0x01)
+    throw Error(PCAONE_E_FORMAT, "Incorrect magic number in plink bed file.");
+  const uint64_t need = 3 + nsnps * (((uint64_t)nsamples + 3) / 4);
+  if (image_bytes < need)
+    throw Error(PCAONE_E_FORMAT, "truncated .bed: " + std::to_string(image_bytes) + " bytes, expected " +
+                                     std::to_string(need));
+}
+
 extern "C" {
 
 void pcaone_gpu_default_params(pcaone_gpu_params* p) {
@@ -1551,6 +1839,8 @@ int pcaone_gpu_open(const pcaone_gpu_desc* desc, pcaone_gpu_ctx** out) {
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PCAONE_E_CUDA;
   if (ctx->c.device < 0 || ctx->c.device >= ndev) return PCAONE_E_ARG;
   if (cudaSetDevice(ctx->c.device) != cudaSuccess) return PCAONE_E_CUDA;
+  if (cudaDeviceGetAttribute(&ctx->c.sm_count, cudaDevAttrMultiProcessorCount, ctx->c.device) != cudaSuccess)
+    return PCAONE_E_CUDA;
   if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) return PCAONE_E_CUDA;
   *out = ctx.release();
   return PCAONE_OK;
@@ -1624,15 +1914,61 @@ int pcaone_gpu_load_bed(pcaone_gpu_ctx* ctx, const uint8_t* packed, uint64_t nsn
 int pcaone_gpu_load_bed_file_image(pcaone_gpu_ctx* ctx, const uint8_t* image, uint64_t image_bytes,
                                    uint64_t nsnps, uint32_t nsamples) {
   return guarded(ctx, [&](Context& c) {
-    if (!image || image_bytes < 3) throw Error(PCAONE_E_FORMAT, "truncated .bed image");
-    if (image[0] != 0x6c || image[1] != 0x1b || image[2] != 0x01)
-      throw Error(PCAONE_E_FORMAT, "Incorrect magic number in plink bed file.");
-    const uint64_t need = 3 + nsnps * (((uint64_t)nsamples + 3) / 4);
-    if (image_bytes < need)
-      throw Error(PCAONE_E_FORMAT, "truncated .bed: " + std::to_string(image_bytes) + " bytes, expected " +
-                                       std::to_string(need));
+    check_bed_image(image, image_bytes, nsnps, nsamples);
     pcaone::load_bed_host(c, image + 3, nsnps, nsamples);
     PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_load_bed_stream(pcaone_gpu_ctx* ctx, const uint8_t* packed, uint64_t nsnps, uint32_t nsamples,
+                               uint64_t device_budget, uint32_t buffer_gb) {
+  return guarded(ctx, [&](Context& c) {
+    if (!packed) throw Error(PCAONE_E_ARG, "null buffer");
+    c.stream_budget = device_budget;
+    c.stream_buffer_gb = buffer_gb ? buffer_gb : 2;
+    pcaone::load_bed_host(c, packed, nsnps, nsamples, true);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_load_bed_file_image_stream(pcaone_gpu_ctx* ctx, const uint8_t* image, uint64_t image_bytes,
+                                          uint64_t nsnps, uint32_t nsamples, uint64_t device_budget,
+                                          uint32_t buffer_gb) {
+  return guarded(ctx, [&](Context& c) {
+    check_bed_image(image, image_bytes, nsnps, nsamples);
+    c.stream_budget = device_budget;
+    c.stream_buffer_gb = buffer_gb ? buffer_gb : 2;
+    pcaone::load_bed_host(c, image + 3, nsnps, nsamples, true);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_stream_plan(uint64_t nsnps, uint32_t nsamples, int svd, int bands, uint64_t device_budget,
+                           uint64_t* block_snps, uint64_t* nblocks) {
+  if (nsnps == 0 || nsamples == 0 || nsnps > 0x7fffffffull || nsamples > 0x7fffff00u) return PCAONE_E_ARG;
+  if (svd != PCAONE_SVD_SINGLE && svd != PCAONE_SVD_WINDOW) return PCAONE_E_ARG;
+  if (svd == PCAONE_SVD_WINDOW && (bands < 4 || (bands & (bands - 1)) != 0)) return PCAONE_E_ARG;
+  const int64_t stride = (((int64_t)nsamples + 127) / 128) * 32;
+  const int64_t b = pcaone::stream_block_size((int64_t)nsnps, stride, svd, bands, device_budget);
+  if (b <= 0) return PCAONE_E_LIMIT;
+  if (block_snps) *block_snps = (uint64_t)b;
+  if (nblocks) *nblocks = (nsnps + (uint64_t)b - 1) / (uint64_t)b;
+  return PCAONE_OK;
+}
+
+int pcaone_gpu_ooc_order(uint64_t nsnps, uint32_t nsamples, int bands, uint32_t buffer_gb, int32_t* order) {
+  if (!order || nsnps == 0 || nsamples == 0 || nsnps > 0x7fffffffull || nsamples > 0x7fffff00u) return PCAONE_E_ARG;
+  if (bands < 4 || (bands & (bands - 1)) != 0) return PCAONE_E_ARG;
+  return pcaone::host_ooc_order((int64_t)nsnps, ((int64_t)nsamples + 3) / 4, buffer_gb ? buffer_gb : 2, bands, order)
+             ? PCAONE_OK
+             : PCAONE_E_ARG;
+}
+
+int pcaone_gpu_stream_info(pcaone_gpu_ctx* ctx, int* streamed, double* bytes_fetched) {
+  return guarded(ctx, [&](Context& c) {
+    if (streamed) *streamed = c.streamed ? 1 : 0;
+    if (bytes_fetched) *bytes_fetched = c.stream_bytes;
+    c.stream_bytes = 0;
   });
 }
 
@@ -1691,7 +2027,7 @@ int pcaone_gpu_get_bed(pcaone_gpu_ctx* ctx, uint8_t* packed) {
     pcaone::need_plink(c);
     if (!packed) throw Error(PCAONE_E_ARG, "null buffer");
     const size_t bps = ((size_t)c.N + 3) / 4;
-    PCAONE_CUDA(cudaMemcpy2DAsync(packed, bps, c.bed.p, c.stride, bps, c.M, cudaMemcpyDeviceToHost, c.stream));
+    PCAONE_CUDA(cudaMemcpy2DAsync(packed, bps, c.rows_ptr(), c.stride, bps, c.M, cudaMemcpyDefault, c.stream));
     PCAONE_CUDA(cudaStreamSynchronize(c.stream));
   });
 }

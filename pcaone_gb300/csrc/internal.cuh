@@ -124,6 +124,11 @@ void launch_sanitize_padding(uint8_t* bed, int64_t stride, int64_t nsnps, int ns
 void launch_repitch(const uint8_t* src, int64_t src_pitch, uint8_t* dst, int64_t dst_pitch, int64_t nrows, int64_t bps,
                     cudaStream_t s);
 void launch_counts(const BedView& v, int32_t* counts, double* F, cudaStream_t s);
+// rows perm[0 .. nrows) (identity when perm is null) of src into consecutive
+// rows of dst, many 16-byte loads in flight per thread (sources across the
+// host link); ctas thread blocks of 256
+void launch_gather_rows_deep(const uint8_t* src, uint8_t* dst, int64_t stride, const int32_t* perm, int64_t nrows,
+                             int ctas, cudaStream_t s);
 // per-SNP decode table: lut[j] = {x(00), x(01), x(10), x(11)} with x(c) =
 // scale_j * (BED2GENO[c] - F_j), x(01) = 0; lut64 likewise in double.
 void launch_lut(const double* F, int64_t nsnps, int standardize, int ploidy, float4* lut32, double* lut64,

@@ -23,11 +23,21 @@ from .synthetic import read_bed
 
 
 class FileBed:
-    """PLINK fileset resident on the GPU (src/FilePlink.hpp:7-47, FilePlink.cpp:26-120)."""
+    """PLINK fileset on the GPU (src/FilePlink.hpp:7-47, FilePlink.cpp:26-120).
+
+    ``memory`` (GB of device memory for the streamed blocks, the -m/--memory
+    option, src/Cmd.cpp) selects the out-of-core form (FilePlink.cpp:122-218):
+    the rows stay in pinned host memory and SNP blocks are streamed to the GPU;
+    the window method's shuffle then follows permute_plink with ``buffer`` GB
+    (the --buffer option) as the reference's out-of-core mode does.
+    """
 
     def __init__(self, prefix: Optional[str] = None, *, packed: Optional[np.ndarray] = None,
-                 nsamples: Optional[int] = None, device: int = 0, verbose: int = 0):
+                 nsamples: Optional[int] = None, device: int = 0, verbose: int = 0,
+                 memory: Optional[float] = None, buffer: int = 2):
         self.ctx = capi.Context(device, verbose)
+        self.out_of_core = memory is not None
+        budget = int(memory * (1 << 30)) if memory is not None else 0
         if prefix is not None:
             fam = prefix + ".fam"
             bim = prefix + ".bim"
@@ -37,9 +47,15 @@ class FileBed:
                 m = sum(1 for _ in f)
             with open(prefix + ".bed", "rb") as f:
                 image = f.read()
-            self.ctx.load_bed_file_image(image, m, n)
+            if self.out_of_core:
+                self.ctx.load_bed_file_image_stream(image, m, n, budget, buffer)
+            else:
+                self.ctx.load_bed_file_image(image, m, n)
         elif packed is not None and nsamples is not None:
-            self.ctx.load_bed(packed, nsamples)
+            if self.out_of_core:
+                self.ctx.load_bed_stream(packed, nsamples, budget, buffer_gb=buffer)
+            else:
+                self.ctx.load_bed(packed, nsamples)
         else:
             raise ValueError("give a PLINK prefix or packed genotypes with nsamples")
         self.nsamples = self.ctx.nsamples

@@ -29,6 +29,7 @@ class RunOptions:
     tolem: float = 1e-5
     noshuffle: bool = False
     scale: int = -9
+    memory: float = 0.0  # -m GB: out-of-core (src/Cmd.cpp:218)
     extra: dict = field(default_factory=dict)
 
     @property
@@ -72,6 +73,8 @@ def parse_options(opts) -> RunOptions:
             o.scale = int(next(it))
         elif a in ("-b", "-B"):
             next(it)
+        elif a in ("-m", "--memory"):
+            o.memory = float(next(it))
         else:
             raise ValueError(f"option {a} not handled")
     o.oversamples = max(o.oversamples, o.k)
@@ -90,14 +93,17 @@ class GoldenCase:
     ref: dict
 
 
-def golden_cases():
-    """PLINK fixtures (packed genotypes)."""
+def golden_cases(out_of_core: bool = False):
+    """PLINK fixtures (packed genotypes): the in-core runs, or with
+    out_of_core the reference's -m runs."""
     out = []
     for path in sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz"))):
         z = np.load(path)
         if "packed" not in z.files:
             continue
         opts = parse_options(json.loads(str(z["options"])))
+        if (opts.memory > 0) != out_of_core:
+            continue
         ref = {k: z[k] for k in z.files if k not in ("packed", "options")}
         meta = ref["meta"]
         out.append(GoldenCase(os.path.basename(path)[:-4], z["packed"], int(meta[0]), int(meta[1]), opts, ref))
@@ -129,7 +135,7 @@ def binary_cases():
 
 
 def golden_case(name: str) -> GoldenCase:
-    for c in golden_cases():
+    for c in golden_cases() + golden_cases(out_of_core=True):
         if c.name == name:
             return c
     raise KeyError(name)

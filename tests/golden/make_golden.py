@@ -6,6 +6,7 @@ tests never run this):
     make -C oracle ref REF=<reference tree>   # builds oracle/_ref/ref_driver
     python tests/golden/make_golden.py         # all fixtures
     python tests/golden/make_golden.py --eigs-only   # only tests/golden/eigs/
+    python tests/golden/make_golden.py --ooc-only    # only the out-of-core (-m) cases
 
 Each case draws a seeded synthetic PLINK fileset (pcaone_gb300.synthetic),
 runs the reference's RSVD operators through oracle/_ref/ref_driver with the
@@ -55,6 +56,44 @@ CASES = {
     "em_ssvd": (dict(nsamples=160, nsnps=1200, npop=3, fst=0.1, seed=7, mcar=0.08),
                 ["-d", "1", "--emu", "--maxiter", "5", "--maxp", "3", "-k", "2"]),
 }
+
+# Out-of-core runs (-m GB): the reference streams blocks from the .bed file;
+# with the window method's shuffle it first rewrites the file in the band
+# interleave of permute_plink (src/FilePlink.cpp:303-408, --buffer 2 GB).  The
+# budgets give 3 to 5 blocks, which Data::prepare then aligns with the windows.
+OOC_CASES = {
+    # M a multiple of the windows: each window is one band of the interleave
+    "ooc_wsvd_n301": (dict(nsamples=301, nsnps=2400, npop=3, fst=0.1, seed=11, mcar=0.01, pad_garbage=True),
+                      ["-d", "2", "-k", "4", "--maxp", "6", "-w", "16", "-m", "0.002"]),
+    # M = 1500 over 16 windows: bands of 94 and 93 SNPs, windows of 94 (a last
+    # window of 90), and a second buffer block of 12 SNPs in the interleave
+    "ooc_em_wsvd_n203": (dict(nsamples=203, nsnps=1500, npop=3, fst=0.1, seed=5, mcar=0.05, pad_garbage=True),
+                         ["-d", "2", "--emu", "--maxiter", "8", "--maxp", "6", "-k", "3", "-w", "16", "-m",
+                          "0.0015"]),
+    "ooc_ssvd_n203": (dict(nsamples=203, nsnps=1500, npop=3, fst=0.1, seed=5, mcar=0.05, pad_garbage=True),
+                      ["-d", "1", "-k", "3", "--maxp", "4", "-m", "0.0015"]),
+}
+
+
+def run_ooc_case(name: str, model_kw: dict, opts: list) -> dict:
+    kw = dict(model_kw)
+    pad_garbage = kw.pop("pad_garbage", False)
+    model = synthetic.draw_population_model(**kw)
+    packed = synthetic.sample_packed_bed(model, pad_garbage=pad_garbage)
+    with tempfile.TemporaryDirectory() as td:
+        prefix = os.path.join(td, name)
+        synthetic.write_plink(prefix, packed, model.nsamples)
+        out = os.path.join(td, "out")
+        os.makedirs(out)
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        subprocess.check_call([DRIVER, out, "-b", prefix] + opts, env=env)
+        res = {k: np.load(os.path.join(out, k + ".npy")) for k in ("U", "S", "V", "Omg0", "meta")}
+        if os.path.exists(os.path.join(out, "perm.npy")):
+            res["perm"] = np.load(os.path.join(out, "perm.npy"))
+    res["packed"] = packed
+    res["options"] = np.array(json.dumps(opts))
+    return res
+
 
 # FileBinary input (-B; per-SNP mean centring only, -C 0): continuous dosages
 # stored as float16 (synthetic.sample_dosages), written as the float32 matrix
@@ -181,6 +220,12 @@ def main() -> None:
         for name in EIGS_CASES:
             run_eigs_case(name)
         return
+    if "--ooc-only" in sys.argv:
+        for name, (mkw, opts) in OOC_CASES.items():
+            res = run_ooc_case(name, mkw, opts)
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+            print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"])
+        return
     for name, (mkw, opts) in CASES.items():
         res = run_case(name, mkw, opts)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
@@ -193,6 +238,10 @@ def main() -> None:
         res = run_projection_case(name, mkw, nb, opts)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
         print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"], "P2[0]=", res["P2"][0])
+    for name, (mkw, opts) in OOC_CASES.items():
+        res = run_ooc_case(name, mkw, opts)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+        print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"])
     for name in EIGS_CASES:
         run_eigs_case(name)
 

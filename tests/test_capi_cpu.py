@@ -80,3 +80,29 @@ def test_header_is_plain_c_and_links_from_c(tmp_path, lib):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, (out.returncode, out.stdout, out.stderr)
     assert "c caller ok" in out.stdout
+
+
+def test_stream_plan(lib):
+    """The out-of-core block plan (Data::prepare, src/Data.cpp:40-84), host only."""
+    stride = lambda n: (n + 127) // 128 * 32  # noqa: E731  device row bytes
+    M, N = 1_000_000, 200_000
+    # window method: the windows themselves, ceil(M / bands)
+    assert capi.stream_plan(M, N, capi.SVD_WINDOW, 64, 0) == (15_625, 64)
+    assert capi.stream_plan(M, N, capi.SVD_WINDOW, 64, 2 * 15_625 * stride(N)) == (15_625, 64)
+    with pytest.raises(capi.PcaoneError) as e:
+        capi.stream_plan(M, N, capi.SVD_WINDOW, 64, 2 * 15_625 * stride(N) - 1)
+    assert e.value.code == -6
+    assert capi.stream_plan(1001, 16, capi.SVD_WINDOW, 4, 0) == (251, 4)
+    # single pass: the in-core blocks of at most 16384 SNPs, balanced ...
+    assert capi.stream_plan(M, N, capi.SVD_SINGLE, 64, 0) == (16_130, 62)
+    assert capi.stream_plan(16384, N, capi.SVD_SINGLE, 64, 0) == (16_384, 1)
+    # ... fewer when two slots of the budget hold fewer rows
+    b, nb = capi.stream_plan(M, N, capi.SVD_SINGLE, 64, 2 * 1000 * stride(N))
+    assert b <= 1000 and nb == -(-M // 1000) and b == -(-M // nb)
+    with pytest.raises(capi.PcaoneError) as e:
+        capi.stream_plan(M, N, capi.SVD_SINGLE, 64, stride(N))  # less than a row per slot
+    assert e.value.code == -6
+    for bad in [(0, N, 1, 64, 0), (M, 0, 1, 64, 0), (M, N, 3, 64, 0), (M, N, 2, 6, 0), (M, N, 2, 2, 0)]:
+        with pytest.raises(capi.PcaoneError) as e:
+            capi.stream_plan(*bad)
+        assert e.value.code == -1

@@ -137,3 +137,47 @@ def test_projection_matches_reference(case):
     for mode, key in ((1, "P1"), (2, "P2")):
         P = H.project(case.ref["packed_new"], n_new, case.ref["F"], V, S, mode)
         assert np.max(np.abs(P - case.ref[key])) <= 1e-10 * max(1.0, np.max(np.abs(case.ref[key]))), mode
+
+
+# ---- out-of-core (-m) runs of the reference -------------------------------
+OOC_CASES = golden_cases(out_of_core=True)
+OOC_IDS = [c.name for c in OOC_CASES]
+
+
+@pytest.mark.parametrize("case", OOC_CASES, ids=OOC_IDS)
+def test_out_of_core_order(case):
+    """The order permute_plink gives the rewritten .bed (src/FilePlink.cpp:303-408),
+    restated by the oracle and by the library (pcaone_gpu_ooc_order), against the
+    reference's own permutation; the single-pass method does not shuffle."""
+    if not case.opts.perm:
+        assert "perm" not in case.ref
+        return
+    order = H.permute_plink_order(case.nsnps, case.nsamples, case.opts.bands)
+    assert np.array_equal(order, case.ref["perm"])
+    from pcaone_gb300 import build as B
+    from pcaone_gb300 import capi
+    import os
+    if not os.path.exists(capi.LIBPATH):
+        B.build()
+    assert np.array_equal(capi.ooc_order(case.nsnps, case.nsamples, case.opts.bands), case.ref["perm"])
+
+
+@pytest.mark.parametrize("case", OOC_CASES, ids=OOC_IDS)
+def test_out_of_core_rsvd_matches_reference(case):
+    """The reference's out-of-core run equals the in-core computation on the
+    rewritten matrix without the in-core shuffle: its windows are the in-core
+    ones when Data::prepare aligns the blocks with them (bandFactor 1,
+    src/Data.cpp:66-77), and the file's own allele frequencies keep the EM fill
+    consistent.  The restatement on the rows in permute_plink order agrees to
+    rounding."""
+    o = case.opts
+    packed = case.packed[case.ref["perm"]] if "perm" in case.ref else case.packed
+    d = H.OracleData(packed, case.nsamples, emu=o.emu, perm=False, seed=o.seed, bands=o.bands, rand=o.rand,
+                     svd_t=o.svd, omega0=case.ref["Omg0"])
+    op = H.run_pca_with_halko(d, o.k, o.oversamples, maxp=o.maxp, tol=o.tol, maxiter=o.maxiter, tolem=o.tolem)
+    if o.emu:
+        assert op.em_iters == int(case.ref["meta"][2])
+    S = case.ref["S"]
+    assert np.max(np.abs(op.S ** 2 - S ** 2) / S ** 2) < 1e-9
+    assert np.max(np.abs(align_signs(op.U, case.ref["U"]) - case.ref["U"])) < 1e-8
+    assert np.max(np.abs(align_signs(op.V, case.ref["V"]) - case.ref["V"])) < 1e-8
