@@ -277,19 +277,24 @@ __device__ __forceinline__ void lut_init(uint32_t* lut, int tid, int nthreads) {
   }
 }
 
-// The FP8 form's table: the two E4M3 dosages of a 4-bit pair of codes (low
-// byte from the code in bits 0-1): 00 -> 2.0 (0x40), 10 -> 1.0 (0x38), 01
-// (missing) and 11 -> 0; 32 copies laid out as lut_init's.  dec8 turns a
-// packed byte (four codes) into four E4M3 dosages, first code in the low byte.
-__device__ __forceinline__ uint32_t e4m3_dosage(uint32_t code) { return code == 0u ? 0x40u : code == 2u ? 0x38u : 0u; }
-__device__ __forceinline__ void lut_init8(uint32_t* lut, int tid, int nthreads) {
-  for (int i = tid; i < kLutWords; i += nthreads) {
-    const uint32_t n = (uint32_t)i >> 5;
-    lut[i] = e4m3_dosage(n & 3u) | (e4m3_dosage((n >> 2) & 3u) << 8);
+// The FP8 form's decode, in registers: four E4M3 words (four dosages each,
+// first code in the low byte) from the 16 2-bit codes of w (code i in bits
+// 2i .. 2i+1).  Each half-word's eight codes are spread to one per nibble
+// (a byte permute and two shift-and-mask steps), and every nibble selects a
+// byte of the table {0x40 (00: 2.0), 0x00 (01: missing), 0x38 (10: 1.0),
+// 0x00 (11)} in a second byte permute: four integer operations per word and
+// no shared-memory lookup (a table in shared memory cost two lookups and about
+// eight operations per word).
+__device__ __forceinline__ void e4m3_x16(uint32_t w, uint32_t* out) {
+  constexpr uint32_t kTab = 0x00380040u;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    uint32_t x = __byte_perm(w, 0u, h ? 0x4342u : 0x4140u);  // bytes 2h, 2h+1 -> bytes 0, 2
+    x = (x | (x << 4)) & 0x0F0F0F0Fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    out[2 * h] = __byte_perm(kTab, 0u, x);  // selectors: the low four nibbles
+    out[2 * h + 1] = __byte_perm(kTab, 0u, x >> 16);
   }
-}
-__device__ __forceinline__ uint32_t dec8(const uint32_t* lut_l, uint32_t byte) {
-  return lut_l[(byte & 15u) << 5] | (lut_l[((byte >> 4) & 15u) << 5] << 16);
 }
 
 // One stage of a warp transpose of a 32 x 32 matrix of 2-bit codes held as
@@ -360,23 +365,39 @@ constexpr int kMaxNTmemA = 256;
 // bytes of K.
 constexpr int kModeGeno = 0, kModeDense = 1, kModeGeno8 = 2;
 
-// a_addr: TMEM address of the A operand (!kASmem) or its shared-memory
-// address (kASmem)
+// The MMAs of one pipeline stage: four K steps of 32 bytes over the slices
+// concatenated along N, cut into MMAs of at most 256 columns.  The issuing
+// thread shares its SM sub-partition with decoder warps, so every instruction
+// it needs costs several cycles: the shared-memory descriptors are advanced by
+// adding offsets to precomputed ones (their address field counts 16-byte
+// units; 32 bytes of K = 2, 256 B rows = 2048), and the instruction
+// descriptors of the two column chunks come precomputed.  a_tmem: the stage's
+// A operand in TMEM (!kASmem), a_desc: its shared-memory descriptor (kASmem).
 template <int kMode, bool kASmem>
-__device__ __forceinline__ void mma_cat(uint32_t tmem_col0, uint32_t a_addr, uint32_t b_addr, int ncols,
-                                        uint32_t accumulate) {
-  for (int n0 = 0; n0 < ncols; n0 += kMaxNTmemA) {
-    const int n = min(kMaxNTmemA, ncols - n0);
-    if constexpr (kMode == kModeGeno8) {
-      mma_e4m3_ta(tmem_col0 + n0, a_addr, desc_sw128(b_addr + n0 * 128), idesc_e4m3(128, n), accumulate);
-    } else {
-      const uint32_t id = kMode == kModeDense ? idesc_f16(128, n) : idesc_bf16(128, n);
-      if constexpr (kASmem)
-        mma_bf16_ss(tmem_col0 + n0, desc_sw128(a_addr), desc_sw128(b_addr + n0 * 128), id, accumulate);
+__device__ __forceinline__ void mma_stage(uint32_t tmem_d, uint32_t a_tmem, uint64_t a_desc, uint64_t b_desc,
+                                          int ncat, uint32_t id0, uint32_t id1, bool first) {
+#pragma unroll
+  for (int kk = 0; kk < 4; ++kk) {
+    const uint32_t acc = (first && kk == 0) ? 0u : 1u;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      if (c == 1 && ncat <= kMaxNTmemA) break;
+      const uint64_t bd = b_desc + (uint64_t)(2 * kk + c * (kMaxNTmemA * 128 / 16));
+      const uint32_t id = c ? id1 : id0;
+      const uint32_t d = tmem_d + (uint32_t)(c * kMaxNTmemA);
+      if constexpr (kMode == kModeGeno8)
+        mma_e4m3_ta(d, a_tmem + kk * 8, bd, id, acc);
+      else if constexpr (kASmem)
+        mma_bf16_ss(d, a_desc + (uint64_t)(2 * kk), bd, id, acc);
       else
-        mma_bf16_ta(tmem_col0 + n0, a_addr, desc_sw128(b_addr + n0 * 128), id, accumulate);
+        mma_bf16_ta(d, a_tmem + kk * 8, bd, id, acc);
     }
   }
+}
+
+template <int kMode>
+__host__ __device__ constexpr uint32_t idesc_of(int n) {
+  return kMode == kModeGeno8 ? idesc_e4m3(128, n) : kMode == kModeDense ? idesc_f16(128, n) : idesc_bf16(128, n);
 }
 
 // Warp roles of both kernels (320 threads): warp 0 lane 0 issues the TMA
@@ -511,15 +532,12 @@ __global__ void __launch_bounds__(kThreads, 2)
   __shared__ uint32_t tmem_sh;
   __shared__ volatile int abort_sh;
   __shared__ float unit[3 * 112];
-  __shared__ uint32_t lut[kDense ? 1 : kLutWords];
+  __shared__ uint32_t lut[kDense || kFp8 ? 1 : kLutWords];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int LP = a.LP, S = a.nslice;
   const SmemLayout lay = layout_for(LP, S, kTileBytes, kASmem);
   const int row0 = blockIdx.x * 128;
-  if (kFp8)
-    lut_init8(lut, tid, kThreads);
-  else if (!kDense)
-    lut_init(lut, tid, kThreads);
+  if (!kDense && !kFp8) lut_init(lut, tid, kThreads);
   const int kbeg = blockIdx.y * a.chunk;
   const int kend = min(kbeg + a.chunk, a.npad);
   const int nk = (kend - kbeg + kK - 1) / kK;
@@ -556,41 +574,44 @@ __global__ void __launch_bounds__(kThreads, 2)
       int issued = 0;
       for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
         tma_prefetch_2d(&map_bed, (kbeg + kb * kK) >> kdiv, (int)(a.pos0 + row0));
+      const int prow = (int)(a.pos0 + row0);
+      int st = 0, round = 0;
       for (int kb = 0; kb < nk; ++kb) {
-        const int st = kb % nst;
-        if (kb + kPrefetchSteps < nk)
-          tma_prefetch_2d(&map_bed, (kbeg + (kb + kPrefetchSteps) * kK) >> kdiv, (int)(a.pos0 + row0));
-        if (kb >= nst && !role_wait(&empty_bar[st], (uint32_t)(kb / nst - 1) & 1u, &abort_sh, wlim)) break;
-        uint8_t* base = smem + st * lay.stage_bytes;
         const int k0 = kbeg + kb * kK;
+        if (kb + kPrefetchSteps < nk) tma_prefetch_2d(&map_bed, (k0 + kPrefetchSteps * kK) >> kdiv, prow);
+        if (round > 0 && !role_wait(&empty_bar[st], (uint32_t)(round - 1) & 1u, &abort_sh, wlim)) break;
+        uint8_t* base = smem + st * lay.stage_bytes;
         mbar_expect_tx(&full_bar[st], tx_bytes);
-        tma_load_2d(base + lay.p, &map_bed, k0 >> kdiv, (int)(a.pos0 + row0), &full_bar[st]);
+        tma_load_2d(base + lay.p, &map_bed, k0 >> kdiv, prow, &full_bar[st]);
         for (int s = 0; s < S; ++s) tma_load_2d(base + lay.b + s * LP * 128, &map_w, k0, s * LP, &full_bar[st]);
         issued = kb + 1;
+        if (++st == nst) {
+          st = 0;
+          ++round;
+        }
       }
       if (abort_sh) drain_copies(full_bar, issued, nst);
     }
   } else if (warp == 1) {
     // ---- MMA issuer ----
     if (lane == 0) {
+      const uint32_t id0 = idesc_of<kMode>(min(ncat, kMaxNTmemA));
+      const uint32_t id1 = idesc_of<kMode>(ncat > kMaxNTmemA ? ncat - kMaxNTmemA : 16);
+      const uint64_t b_desc0 = desc_sw128(smem_u32(smem + lay.b));
+      const uint64_t a_desc0 = desc_sw128(smem_u32(smem + lay.a));
+      const uint64_t stage_units = lay.stage_bytes >> 4;
+      int st = 0, round = 0;
       for (int kb = 0; kb < nk; ++kb) {
-        const int st = kb % nst;
-        if (!role_wait(&dec_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh, wlim)) break;
+        if (!role_wait(&dec_bar[st], (uint32_t)round & 1u, &abort_sh, wlim)) break;
         tc_fence_after();
-        uint8_t* base = smem + st * lay.stage_bytes;
-        const uint32_t bb = smem_u32(base + lay.b);
-        if constexpr (kASmem) {
-          const uint32_t aa = smem_u32(base + lay.a);
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            mma_cat<kMode, true>(tmem, aa + kk * 32, bb + kk * 32, ncat, (kb | kk) != 0);
-        } else {
-          const uint32_t ad = tmem + a_col0 + st * 32;
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            mma_cat<kMode, false>(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
-        }
+        const uint64_t so = (uint64_t)st * stage_units;
+        mma_stage<kMode, kASmem>(tmem, tmem + a_col0 + (uint32_t)st * 32u, a_desc0 + so, b_desc0 + so, ncat, id0, id1,
+                                 kb == 0);
         mma_commit(&empty_bar[st]);
+        if (++st == nst) {
+          st = 0;
+          ++round;
+        }
       }
       mma_commit(&acc_bar);  // arrives once every MMA above has completed
     }
@@ -602,9 +623,9 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int q4 = warp & 3, ch = (warp - kDecodeWarp0) >> 2;
     const int r = q4 * 32 + lane;
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
+    int st = 0, round = 0;
     for (int kb = 0; kb < nk; ++kb) {
-      const int st = kb % nst;
-      if (!role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh, wlim)) break;
+      if (!role_wait(&full_bar[st], (uint32_t)round & 1u, &abort_sh, wlim)) break;
       uint8_t* base = smem + st * lay.stage_bytes;
       uint32_t wd[16];
       if (kDense) {
@@ -623,10 +644,10 @@ __global__ void __launch_bounds__(kThreads, 2)
       } else if (kFp8) {
         // samples 64ch .. 64ch+63 of the step: 16 packed bytes, one per word
         const uint4 pk = *reinterpret_cast<const uint4*>(base + lay.p + r * 32 + ch * 16);
-        const uint32_t pw[4] = {pk.x, pk.y, pk.z, pk.w};
-        const uint32_t* lut_l = lut + lane;
-#pragma unroll
-        for (int e = 0; e < 16; ++e) wd[e] = dec8(lut_l, pw[e >> 2] >> (8 * (e & 3)));
+        e4m3_x16(pk.x, wd);
+        e4m3_x16(pk.y, wd + 4);
+        e4m3_x16(pk.z, wd + 8);
+        e4m3_x16(pk.w, wd + 12);
       } else {
         const uint2 pk = *reinterpret_cast<const uint2*>(base + lay.p + r * 16 + ch * 8);
         const uint32_t* lut_l = lut + lane;
@@ -646,6 +667,10 @@ __global__ void __launch_bounds__(kThreads, 2)
         tc_fence_before();
       }
       mbar_arrive(&dec_bar[st]);
+      if (++st == nst) {
+        st = 0;
+        ++round;
+      }
     }
     // ---- epilogue ----
     const bool ok = nk > 0 && role_wait(&acc_bar, 0u, &abort_sh, wlim);
@@ -702,12 +727,9 @@ __global__ void __launch_bounds__(kThreads, 2)
   __shared__ uint32_t tmem_sh;
   __shared__ volatile int abort_sh;
   __shared__ float unit[3 * 112];
-  __shared__ uint32_t lut[kDense ? 1 : kLutWords];
+  __shared__ uint32_t lut[kDense || kFp8 ? 1 : kLutWords];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  if (kFp8)
-    lut_init8(lut, tid, kThreads);
-  else if (!kDense)
-    lut_init(lut, tid, kThreads);
+  if (!kDense && !kFp8) lut_init(lut, tid, kThreads);
   const int LP = a.LP, S = a.nslice;
   const SmemLayout lay = layout_for(LP, S, kTileBytes, kASmem);
   const int samp0 = blockIdx.x * 128;
@@ -746,40 +768,42 @@ __global__ void __launch_bounds__(kThreads, 2)
       int issued = 0;
       for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
         tma_prefetch_2d(&map_bed, scol, (int)(a.pos0 + jb + kb * kK));
+      int st = 0, round = 0;
       for (int kb = 0; kb < nk; ++kb) {
-        const int st = kb % nst;
-        if (kb + kPrefetchSteps < nk)
-          tma_prefetch_2d(&map_bed, scol, (int)(a.pos0 + jb + (kb + kPrefetchSteps) * kK));
-        if (kb >= nst && !role_wait(&empty_bar[st], (uint32_t)(kb / nst - 1) & 1u, &abort_sh, wlim)) break;
-        uint8_t* base = smem + st * lay.stage_bytes;
         const int j0 = jb + kb * kK;
+        if (kb + kPrefetchSteps < nk) tma_prefetch_2d(&map_bed, scol, (int)(a.pos0 + j0 + kPrefetchSteps * kK));
+        if (round > 0 && !role_wait(&empty_bar[st], (uint32_t)(round - 1) & 1u, &abort_sh, wlim)) break;
+        uint8_t* base = smem + st * lay.stage_bytes;
         mbar_expect_tx(&full_bar[st], tx_bytes);
         tma_load_2d(base + lay.p, &map_bed, scol, (int)(a.pos0 + j0), &full_bar[st]);
         for (int r = 0; r < S; ++r) tma_load_2d(base + lay.b + r * LP * 128, &map_g, j0, r * LP, &full_bar[st]);
         issued = kb + 1;
+        if (++st == nst) {
+          st = 0;
+          ++round;
+        }
       }
       if (abort_sh) drain_copies(full_bar, issued, nst);
     }
   } else if (warp == 1) {
     if (lane == 0) {
+      const uint32_t id0 = idesc_of<kMode>(min(ncat, kMaxNTmemA));
+      const uint32_t id1 = idesc_of<kMode>(ncat > kMaxNTmemA ? ncat - kMaxNTmemA : 16);
+      const uint64_t b_desc0 = desc_sw128(smem_u32(smem + lay.b));
+      const uint64_t a_desc0 = desc_sw128(smem_u32(smem + lay.a));
+      const uint64_t stage_units = lay.stage_bytes >> 4;
+      int st = 0, round = 0;
       for (int kb = 0; kb < nk; ++kb) {
-        const int st = kb % nst;
-        if (!role_wait(&dec_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh, wlim)) break;
+        if (!role_wait(&dec_bar[st], (uint32_t)round & 1u, &abort_sh, wlim)) break;
         tc_fence_after();
-        uint8_t* base = smem + st * lay.stage_bytes;
-        const uint32_t bb = smem_u32(base + lay.b);
-        if constexpr (kASmem) {
-          const uint32_t aa = smem_u32(base + lay.a);
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            mma_cat<kMode, true>(tmem, aa + kk * 32, bb + kk * 32, ncat, (kb | kk) != 0);
-        } else {
-          const uint32_t ad = tmem + a_col0 + st * 32;
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            mma_cat<kMode, false>(tmem, ad + kk * 8, bb + kk * 32, ncat, (kb | kk) != 0);
-        }
+        const uint64_t so = (uint64_t)st * stage_units;
+        mma_stage<kMode, kASmem>(tmem, tmem + a_col0 + (uint32_t)st * 32u, a_desc0 + so, b_desc0 + so, ncat, id0, id1,
+                                 kb == 0);
         mma_commit(&empty_bar[st]);
+        if (++st == nst) {
+          st = 0;
+          ++round;
+        }
       }
       mma_commit(&acc_bar);
     }
@@ -791,10 +815,10 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int q4 = warp & 3, ch = (warp - kDecodeWarp0) >> 2;
     const int r = q4 * 32 + lane;
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
+    int st = 0, round = 0;
     for (int kb = 0; kb < nk; ++kb) {
-      const int st = kb % nst;
       // warp-uniform outcome: the genotype decode below shuffles across the warp
-      if (!__all_sync(0xffffffffu, role_wait(&full_bar[st], (uint32_t)(kb / nst) & 1u, &abort_sh, wlim))) break;
+      if (!__all_sync(0xffffffffu, role_wait(&full_bar[st], (uint32_t)round & 1u, &abort_sh, wlim))) break;
       uint8_t* base = smem + st * lay.stage_bytes;
       uint32_t wd[16];
       if (kDense) {
@@ -811,14 +835,13 @@ __global__ void __launch_bounds__(kThreads, 2)
         // row 64ch + 32t + l of the warp's 32 samples; after the transpose lane
         // r holds sample r's 32 codes, byte q of lo / hi = rows 4q .. 4q+3 /
         // 16+4q .. 16+4q+3, one E4M3 word each
-        const uint32_t* lut_l = lut + lane;
 #pragma unroll
         for (int t = 0; t < 2; ++t) {
           const uint2 rowv = *reinterpret_cast<const uint2*>(base + lay.p + (ch * 64 + t * 32 + lane) * 32 + q4 * 8);
           uint32_t lo = rowv.x, hi = rowv.y;
           xpose2_warp(lo, hi, lane);
-#pragma unroll
-          for (int e = 0; e < 8; ++e) wd[8 * t + e] = dec8(lut_l, (e < 4 ? lo : hi) >> (8 * (e & 3)));
+          e4m3_x16(lo, wd + 8 * t);
+          e4m3_x16(hi, wd + 8 * t + 4);
         }
       } else {
         // lane l loads SNP row 32ch + l of the warp's 32 samples (8 bytes); the
@@ -843,6 +866,10 @@ __global__ void __launch_bounds__(kThreads, 2)
         tc_fence_before();
       }
       mbar_arrive(&dec_bar[st]);
+      if (++st == nst) {
+        st = 0;
+        ++round;
+      }
     }
     const bool ok = nk > 0 && role_wait(&acc_bar, 0u, &abort_sh, wlim);
     tc_fence_after();
