@@ -13,6 +13,8 @@
 #pragma once
 
 #include <cmath>
+#include <cstdint>
+#include <cstring>
 
 #ifdef __CUDA_ARCH__
 #define PCAONE_DD_ADD(a, b) __fadd_rn((a), (b))
@@ -29,6 +31,92 @@ namespace pcaone {
 struct dd {
   float hi, lo;
 };
+
+// Bit casts usable on host and device.
+__host__ __device__ inline uint64_t dd_bits(double v) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(v);
+#else
+  uint64_t b;
+  std::memcpy(&b, &v, 8);
+  return b;
+#endif
+}
+__host__ __device__ inline double dd_double_of(uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double v;
+  std::memcpy(&v, &b, 8);
+  return v;
+#endif
+}
+__host__ __device__ inline float dd_float_of(uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(b);
+#else
+  float v;
+  std::memcpy(&v, &b, 4);
+  return v;
+#endif
+}
+__host__ __device__ inline uint32_t dd_fbits(float v) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(v);
+#else
+  uint32_t b;
+  std::memcpy(&b, &v, 4);
+  return b;
+#endif
+}
+__host__ __device__ inline int dd_clz32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+  return __clz((int)x);
+#else
+  return x ? __builtin_clz(x) : 32;
+#endif
+}
+
+// hi + lo = v with integer operations only: this GPU runs FP64 arithmetic and
+// the FP64 <-> FP32 conversions at a small fraction of its FP32 rate, and the
+// tall products of CholeskyQR split every element they read.  hi is v with its
+// 52-bit mantissa cut to the top 23 bits (exact as a float), lo the remaining
+// 29 bits cut to a float's 24 (lo rounds toward zero), so |hi + lo - v| <
+// 2^-46 |v| for 2^-74 <= |v| < 2^128.  Below 2^-74 lo underflows (24 bits
+// remain), below 2^-126 both are zero, and 2^128 is out of range; the tall
+// matrices of CholeskyQR (sketch columns, their Q factors, inverse Cholesky
+// factors) lie far inside.
+__host__ __device__ inline void dd_split_bits(double v, float& hi, float& lo) {
+  const uint64_t b = dd_bits(v);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7FFu) - 1023;
+  if (e < -126) {
+    hi = lo = 0.f;
+    return;
+  }
+  hi = dd_float_of(sign | ((uint32_t)(e + 127) << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu));
+  const uint32_t m = (uint32_t)b & 0x1FFFFFFFu;  // value m * 2^(e - 52)
+  const int k = 31 - dd_clz32(m);                // leading bit of m (m > 0)
+  const int el = e - 52 + k;                     // exponent of lo
+  if (m == 0u || el < -126) {
+    lo = 0.f;
+    return;
+  }
+  const uint32_t mant = k >= 23 ? (m >> (k - 23)) : (m << (23 - k));
+  lo = dd_float_of(sign | ((uint32_t)(el + 127) << 23) | (mant & 0x7FFFFFu));
+}
+
+// (double)hi + (double)lo with the two conversions done on the bits (exact
+// for normal floats; zero and subnormal floats count as zero), leaving one FP64
+// addition.
+__host__ __device__ inline double dd_double_of_float(float f) {
+  const uint32_t b = dd_fbits(f);
+  const uint32_t e = (b >> 23) & 0xFFu;
+  if (e == 0u) return 0.0;
+  return dd_double_of(((uint64_t)(b & 0x80000000u) << 32) | ((uint64_t)(e - 127 + 1023) << 52) |
+                      ((uint64_t)(b & 0x7FFFFFu) << 29));
+}
+__host__ __device__ inline double dd_merge_bits(float hi, float lo) { return dd_double_of_float(hi) + dd_double_of_float(lo); }
 
 __host__ __device__ inline dd dd_from_double(double v) {
   const float h = (float)v;

@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict_
       if constexpr (F64)
         Ad[e] = v;
       else
-        fp_split(v, Ah[e], Al[e]);
+        dd_split_bits(v, Ah[e], Al[e]);
     }
     if (!sym)
       for (int e = tid; e < kRowsTile * nb; e += blockDim.x) {
@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict_
         if constexpr (F64)
           Bd[e] = v;
         else
-          fp_split(v, Bh[e], Bl[e]);
+          dd_split_bits(v, Bh[e], Bl[e]);
       }
     __syncthreads();
     const int ldt = sym ? na : nb;
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(256) k_cross_partial(const double* __restrict_
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int e = tid + q * 256;
-    if (e < nent) out[pi[e] * nb + pj[e]] = F64 ? accd[q] : fp_value(acc[q]);
+    if (e < nent) out[pi[e] * nb + pj[e]] = F64 ? accd[q] : dd_merge_bits(acc[q].hi, acc[q].lo);
   }
 }
 
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows
     if constexpr (F64)
       Bd[e] = v;
     else
-      fp_split(v, Bh[e], Bl[e]);
+      dd_split_bits(v, Bh[e], Bl[e]);
   }
   const int r = 2 * (tid >> 4), cg = tid & 15;
   for (int64_t rt = (int64_t)blockIdx.x * kRowsTile; rt < rows; rt += (int64_t)gridDim.x * kRowsTile) {
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows
       if constexpr (F64)
         Ad[rr * las + cc] = v;
       else
-        fp_split(v, Ah[rr * las + cc], Al[rr * las + cc]);
+        dd_split_bits(v, Ah[rr * las + cc], Al[rr * las + cc]);
     }
     __syncthreads();
     const int64_t row0 = rt + r;
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(256) k_gemm_tall(const double* A, int64_t rows
 #pragma unroll
           for (int q = 0; q < 3; ++q) {
             const int c = c0 + cg + 16 * q;
-            if (c < n) C[(row0 + h) * ldc + c] = F64 ? sd[h][q] : fp_value(s[h][q]);
+            if (c < n) C[(row0 + h) * ldc + c] = F64 ? sd[h][q] : dd_merge_bits(s[h][q].hi, s[h][q].lo);
           }
         }
       }
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(256) k_gemm_tall_upper(double* A, int64_t rows
     if constexpr (F64)
       Bd[e] = B[e];
     else
-      fp_split(B[e], Bh[e], Bl[e]);
+      dd_split_bits(B[e], Bh[e], Bl[e]);
   }
   int cmax = -1;
 #pragma unroll
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(256) k_gemm_tall_upper(double* A, int64_t rows
       if constexpr (F64)
         Ad[rr * las + cc] = v;
       else
-        fp_split(v, Ah[rr * las + cc], Al[rr * las + cc]);
+        dd_split_bits(v, Ah[rr * las + cc], Al[rr * las + cc]);
     }
     __syncthreads();
     FloatPair s[kUpperMaxQ];
@@ -438,8 +438,84 @@ __global__ void __launch_bounds__(256) k_gemm_tall_upper(double* A, int64_t rows
 #pragma unroll
       for (int q = 0; q < kUpperMaxQ; ++q) {
         const int c = 16 * (q >> 1) + ((q & 1) ? 15 - warp : warp);
-        if (c < LP) A[row * LP + c] = F64 ? sd[q] : fp_value(s[q]);
+        if (c < LP) A[row * LP + c] = F64 ? sd[q] : dd_merge_bits(s[q].hi, s[q].lo);
       }
+    }
+  }
+}
+
+// The same product in FP32 pairs, register-blocked: a CTA takes 64-row tiles
+// of A (read once, split into float pairs in shared memory from the doubles'
+// bits, no FP64 arithmetic), thread (rg, cg) forms rows 4rg .. 4rg+3 and
+// columns cg, cg+16, ... (LP/16 of them), so each float pair it loads from
+// shared memory serves four (A) or up to seven (B) products.  Column block j
+// (columns 16j .. 16j+15) needs the rows t < 16(j+1) of B only; within the
+// diagonal block the terms t > column are exact zeros of B and are skipped by
+// a predicate.  Every output accumulates the same terms in the same order
+// (t increasing) as k_gemm_tall_upper.
+constexpr int kUpRows = 64;
+constexpr int kUpMaxJ = 7;  // LP / 16 with LP <= 112
+__global__ void __launch_bounds__(256) k_gemm_tall_upper_rb(double* A, int64_t rows, int LP,
+                                                            const double* __restrict__ B,
+                                                            const int* __restrict__ only_if) {
+  if (only_if && *only_if == 0) return;
+  extern __shared__ float2 smp[];
+  float2* Bs = smp;                    // LP x LP (hi, lo)
+  float2* As = Bs + LP * LP;           // kUpRows x (LP + 1): odd row stride
+  const int las = LP + 1;
+  const int tid = threadIdx.x, rg = tid >> 4, cg = tid & 15;
+  const int J = LP >> 4;
+  for (int e = tid; e < LP * LP; e += blockDim.x) {
+    float h, l;
+    dd_split_bits(B[e], h, l);
+    Bs[e] = make_float2(h, l);
+  }
+  for (int64_t rt = (int64_t)blockIdx.x * kUpRows; rt < rows; rt += (int64_t)gridDim.x * kUpRows) {
+    __syncthreads();
+    // element e = rr * LP + cc of the tile, stepped by the block size without a division
+    for (int e = tid, rr = tid / LP, cc = tid % LP; e < kUpRows * LP; e += blockDim.x) {
+      const int64_t row = rt + rr;
+      float h = 0.f, l = 0.f;
+      if (row < rows) dd_split_bits(A[row * LP + cc], h, l);
+      As[rr * las + cc] = make_float2(h, l);
+      cc += blockDim.x;
+      while (cc >= LP) {
+        cc -= LP;
+        ++rr;
+      }
+    }
+    __syncthreads();
+    FloatPair acc[4][kUpMaxJ];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < kUpMaxJ; ++j) acc[i][j] = FloatPair{};
+    const float2* a0 = As + (4 * rg) * las;
+    for (int tb = 0; tb < J; ++tb) {
+      for (int tt = 0; tt < 16; ++tt) {
+        const int t = 16 * tb + tt;
+        const float2 x0 = a0[t], x1 = a0[las + t], x2 = a0[2 * las + t], x3 = a0[3 * las + t];
+        const float2* brow = Bs + t * LP + cg;
+#pragma unroll
+        for (int j = 0; j < kUpMaxJ; ++j) {
+          // column cg + 16j: rows t <= cg + 16j of B; blocks j < tb hold only zeros at row t
+          if (j < J && j >= tb && (j > tb || tt <= cg)) {
+            const float2 y = brow[16 * j];
+            fp_add_prod2(acc[0][j], x0.x, x0.y, y.x, y.y);
+            fp_add_prod2(acc[1][j], x1.x, x1.y, y.x, y.y);
+            fp_add_prod2(acc[2][j], x2.x, x2.y, y.x, y.y);
+            fp_add_prod2(acc[3][j], x3.x, x3.y, y.x, y.y);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int64_t row = rt + 4 * rg + i;
+      if (row >= rows) continue;
+#pragma unroll
+      for (int j = 0; j < kUpMaxJ; ++j)
+        if (j < J) A[row * LP + cg + 16 * j] = dd_merge_bits(acc[i][j].hi, acc[i][j].lo);
     }
   }
 }
@@ -944,6 +1020,24 @@ void launch_gemm_tall(const double* A, int64_t rows, int LP, const double* B, in
   PCAONE_LAUNCH_CHECK();
 }
 
+void launch_gemm_tall_upper_rb(double* A, int64_t rows, int LP, const double* B, cudaStream_t s, const int* only_if) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    PCAONE_CUDA(cudaFuncSetAttribute(k_gemm_tall_upper_rb, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set = true;
+  }
+  const size_t smem = sizeof(float2) * ((size_t)LP * LP + (size_t)kUpRows * (LP + 1));
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    PCAONE_CUDA(cudaGetDevice(&dev));
+    PCAONE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const int per_sm = std::max(1, std::min(4, (int)((200 * 1024) / smem)));
+  const int grid = (int)std::min<int64_t>((rows + kUpRows - 1) / kUpRows, (int64_t)sms * per_sm);
+  k_gemm_tall_upper_rb<<<grid, 256, smem, s>>>(A, rows, LP, B, only_if);
+}
+
 template <bool F64>
 void launch_gemm_tall_upper_t(double* A, int64_t rows, int LP, const double* B, cudaStream_t s, const int* only_if) {
   static bool attr_set = false;
@@ -963,6 +1057,8 @@ void launch_gemm_tall_upper(double* A, int64_t rows, int LP, const double* B, cu
   if (LP % 8 != 0 || LP > 8 * kUpperMaxQ) throw Error(-6, "triangular tall product: width must be a multiple of 8, at most 112");
   if (f64)
     launch_gemm_tall_upper_t<true>(A, rows, LP, B, s, only_if);
+  else if (LP % 16 == 0)
+    launch_gemm_tall_upper_rb(A, rows, LP, B, s, only_if);
   else
     launch_gemm_tall_upper_t<false>(A, rows, LP, B, s, only_if);
   PCAONE_LAUNCH_CHECK();

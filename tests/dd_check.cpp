@@ -31,6 +31,23 @@ int main() {
     e_add = std::fmax(e_add, (double)(fabsl(ld(dd_add(a, b)) - (X + Y)) / (fabsl(X) + fabsl(Y))));
   }
   std::printf("op_mul %.3e\nop_div %.3e\nop_sqrt %.3e\nop_add %.3e\n", e_mul, e_div, e_sqrt, e_add);
+  // the integer split and merge of the tall products: values over 2^-70 .. 2^100
+  double e_split = 0, e_merge = 0, e_zero = 0;
+  for (int t = 0; t < 400000; ++t) {
+    const double x = nd(g) * std::ldexp(1.0, (int)(g() % 170) - 70);
+    float h, l;
+    dd_split_bits(x, h, l);
+    e_split = std::fmax(e_split, (double)(fabsl((long double)h + (long double)l - (long double)x) / fabsl(x)));
+    if (std::fabs(l) > std::ldexp(std::fabs((double)h), -22)) e_split = 1.0;  // lo below ulp(hi)
+    // merge: exactly (double)h + (double)l
+    e_merge = std::fmax(e_merge, std::fabs(dd_merge_bits(h, l) - ((double)h + (double)l)));
+  }
+  float h0, l0;
+  dd_split_bits(0.0, h0, l0);
+  e_zero = std::fabs(h0) + std::fabs(l0) + std::fabs(dd_merge_bits(0.f, 0.f));
+  dd_split_bits(-1.0, h0, l0);
+  e_zero += std::fabs(h0 + 1.0f) + std::fabs(l0);
+  std::printf("split %.3e\nmerge %.3e\nsplit_exact %.3e\n", e_split, e_merge, e_zero);
   for (int L : {1, 2, 5, 40, 48, 64, 112}) {
     const int rows = 3 * L + 7;
     std::vector<double> A((size_t)rows * L), W((size_t)L * L);

@@ -36,3 +36,12 @@ def test_cholesky_and_inverse(dd_results, L):
     # R^T R reproduces the Gram matrix and X R = I to ~48-bit accuracy
     assert dd_results[f"chol_L{L}"] < 2e-14
     assert dd_results[f"inv_L{L}"] < 2e-14
+
+
+def test_integer_split_and_merge(dd_results):
+    """The tall products' split of a double into a float pair from its bits
+    (no FP64 arithmetic) keeps 46 bits; the merge equals (double)hi +
+    (double)lo; zero and exact values split exactly."""
+    assert dd_results["split"] < 2.0 ** -46
+    assert dd_results["merge"] == 0.0
+    assert dd_results["split_exact"] == 0.0
