@@ -143,6 +143,13 @@ struct Context {
   // tensor-core form (prod_tc.cu)
   bool tc = false;
   DBuf<uint8_t> bedp;                 // packed rows in working order (shuffled window method)
+  // sample-major copy of the working-order rows, one block of bt_ldw
+  // positions per window (tc::launch_transpose_codes): the H products run the
+  // G kernel on it, whose tiles decode without transposes
+  DBuf<uint8_t> bedT;
+  bool bt_valid = false, bt_off = false;
+  int64_t bt_ws = 0, bt_ldw = 0, bt_pitch = 0;
+  CUtensorMap map_bt{}, map_bt8{};
   const uint8_t* bed_work = nullptr;  // packed rows the tensor-core kernels read
   DBuf<__nv_bfloat16> wsl, gt;        // W slices (3*LP x npad), Gh slices (3*LP x ldg)
   DBuf<double> colsum, cpart, cvec, wunit, hunit, ghbuf, wrep;
@@ -297,6 +304,7 @@ static void load_common(Context& c, uint64_t nsnps, uint32_t nsamples, bool dens
   c.stride = dense ? (int64_t)c.npad * 2 : c.npad / 4;
   c.invalidate_slots();
   c.stream_bytes = 0;
+  c.bt_valid = false;
   if (stream) {
     // the rows go to pinned, mapped host memory; no device copy of the matrix
     c.bed.release();
@@ -1047,6 +1055,7 @@ static void prepare_epoch0(Context& c, bool window) {
       c.miss_valid = false;
       c.bk_valid = false;
       c.invalidate_slots();  // streamed blocks are gathered through the order
+      c.bt_valid = false;
       if (c.tc && !c.streamed) {
         c.bedp.ensure((size_t)c.M * c.stride, c.stream, false);
         tc::launch_gather_rows(c.bed.p, c.bedp.p, c.stride, c.perm.p, c.M, c.stream);
@@ -1116,6 +1125,36 @@ static int64_t acquire_block(Context& c, int64_t pos0, int64_t n) {
 
 // the products of the current block are queued: its slot may be refilled after them
 static void release_block(Context& c) { PCAONE_CUDA(cudaEventRecord(c.slots[c.slot_cur].idle, c.stream)); }
+
+// The sample-major copy for the H products of genotype windows in HBM, built
+// once per working order; false (and the transposing H kernel instead) for
+// streamed rows, dense input, or when the copy does not fit in device memory.
+static bool ensure_sample_major(Context& c) {
+  if (c.dense || c.streamed || c.bt_off) return false;
+  const int64_t ws = window_size(c);
+  if (c.bt_valid && c.bt_ws == ws) return true;
+  const int64_t ldw = (ws + 127) / 128 * 128;
+  const int64_t nwin = (c.M + ws - 1) / ws;
+  const int64_t pitch = nwin * (ldw / 4);
+  try {
+    c.bedT.ensure((size_t)c.npad * (size_t)pitch, c.stream, false);
+  } catch (const Error&) {
+    cudaGetLastError();
+    c.bedT.release();
+    c.bt_off = true;  // the H products keep the transposing kernel
+    return false;
+  }
+  tc::launch_transpose_codes(c.bed_work, c.stride, c.M, ws, ldw, (int)nwin, c.npad, c.bedT.p, pitch, c.stream);
+  tc::make_map_2d(&c.map_bt, c.bedT.p, tc::kMapU8, (uint64_t)pitch, (uint64_t)c.npad, (uint64_t)pitch, 16, 128,
+                  false);
+  tc::make_map_2d(&c.map_bt8, c.bedT.p, tc::kMapU8, (uint64_t)pitch, (uint64_t)c.npad, (uint64_t)pitch, 32, 128,
+                  false);
+  c.bt_ws = ws;
+  c.bt_ldw = ldw;
+  c.bt_pitch = pitch;
+  c.bt_valid = true;
+  return true;
+}
 
 // tensor-core form of one window (prod_tc.cu)
 static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
@@ -1255,9 +1294,34 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
     sg.out2 = c.hesum.p;
     launch_seg_gather(sg, c.stream);
   }
-  mark(fp8 ? 3 : 1);
-  tc::launch_h(fp8 ? c.map_bed_h8 : c.map_bed_h, fp8 ? c.map_gt8 : c.map_gt, ha, c.stream);
-  close_mark();
+  if (ensure_sample_major(c)) {
+    // H = X_w^T Gh as a G product on the sample-major copy: rows = samples,
+    // K = the window's positions (column block pos0 / ws), B = the Gh slices
+    tc::GArgs ta{};
+    ta.pos0 = 0;
+    ta.kofs = pos0 / c.bt_ws * c.bt_ldw;
+    ta.nsnp = c.npad;
+    ta.LP = LP;
+    ta.nslice = S;
+    ta.chunk = per;
+    ta.npad = (int)round_up64(n, fp8 ? 128 : 64);
+    ta.nchunks = nsp;
+    ta.nstages = tc::stages_for(LP, S, tc::g_tile_bytes(false, fp8), false);
+    ta.tmem_cols = tc::tmem_cols_for(tc::tmem_cols_needed(LP, S, ta.nstages, false));
+    ta.wscale = nullptr;
+    ta.part = c.thpart.p;
+    ta.err = c.err.p;
+    ta.dense = 0;
+    ta.wait_cycles = c.wait_cycles;
+    ta.fp8 = fp8 ? 1 : 0;
+    mark(fp8 ? 3 : 1);
+    tc::launch_g(fp8 ? c.map_bt8 : c.map_bt, fp8 ? c.map_gt8 : c.map_gt, ta, c.stream);
+    close_mark();
+  } else {
+    mark(fp8 ? 3 : 1);
+    tc::launch_h(fp8 ? c.map_bed_h8 : c.map_bed_h, fp8 ? c.map_gt8 : c.map_gt, ha, c.stream);
+    close_mark();
+  }
   if (c.streamed) release_block(c);
   tc::HFinishArgs hf{};
   hf.nsamples = c.N;

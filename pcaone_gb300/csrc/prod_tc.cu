@@ -572,17 +572,18 @@ __global__ void __launch_bounds__(kThreads, 2)
       const uint32_t tx_bytes = kTileBytes + (uint32_t)(ncat * 128);
       const int kdiv = kDense ? 0 : 2;  // inner TMA coordinate: samples, or packed bytes
       int issued = 0;
-      for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
-        tma_prefetch_2d(&map_bed, (kbeg + kb * kK) >> kdiv, (int)(a.pos0 + row0));
       const int prow = (int)(a.pos0 + row0);
+      const int kofs = (int)a.kofs;
+      for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
+        tma_prefetch_2d(&map_bed, (kofs + kbeg + kb * kK) >> kdiv, prow);
       int st = 0, round = 0;
       for (int kb = 0; kb < nk; ++kb) {
         const int k0 = kbeg + kb * kK;
-        if (kb + kPrefetchSteps < nk) tma_prefetch_2d(&map_bed, (k0 + kPrefetchSteps * kK) >> kdiv, prow);
+        if (kb + kPrefetchSteps < nk) tma_prefetch_2d(&map_bed, (kofs + k0 + kPrefetchSteps * kK) >> kdiv, prow);
         if (round > 0 && !role_wait(&empty_bar[st], (uint32_t)(round - 1) & 1u, &abort_sh, wlim)) break;
         uint8_t* base = smem + st * lay.stage_bytes;
         mbar_expect_tx(&full_bar[st], tx_bytes);
-        tma_load_2d(base + lay.p, &map_bed, k0 >> kdiv, prow, &full_bar[st]);
+        tma_load_2d(base + lay.p, &map_bed, (kofs + k0) >> kdiv, prow, &full_bar[st]);
         for (int s = 0; s < S; ++s) tma_load_2d(base + lay.b + s * LP * 128, &map_w, k0, s * LP, &full_bar[st]);
         issued = kb + 1;
         if (++st == nst) {
@@ -1205,6 +1206,56 @@ __global__ void k_gather_rows(const uint8_t* __restrict__ src, uint8_t* __restri
   for (int64_t q = threadIdx.x; q < stride / 16; q += blockDim.x) d[q] = s[q];
 }
 
+// Sample-major copy of the packed rows (launch_transpose_codes): sample row i,
+// block w holds the codes of window w's positions w*ws + j (j < ldw, four per
+// byte, position j in bits 2(j%4) of byte j/4), as a .bed would with samples
+// and SNPs swapped, so that an H tile (128 samples x 128 positions) is read and
+// decoded like a G tile.  Positions past the window or the matrix hold code
+// 00 (their Gh rows are zero).  A CTA iteration reads a 128-position x
+// 256-sample tile (64-byte row pieces in 16-byte loads), then
+// warp v transposes the 32-sample block v in four 32 x 32 code blocks with
+// the shuffle transpose of the H decoder and writes each of its samples' 128
+// positions as one 32-byte piece.
+constexpr int kXposeSamples = 256;
+__global__ void __launch_bounds__(256) k_transpose_codes(const uint8_t* __restrict__ bed, int64_t stride, int64_t M,
+                                                         int64_t ws, int64_t ldw, int npad, uint8_t* __restrict__ bt,
+                                                         int64_t tpitch) {
+  __shared__ __align__(16) uint8_t tile[128][kXposeSamples / 4];  // positions x packed samples
+  const int jt = blockIdx.x, w = blockIdx.z;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t p0 = (int64_t)w * ws + (int64_t)jt * 128;
+  const int64_t jlim = min((int64_t)128, min(ws - (int64_t)jt * 128, M - p0));  // positions of this tile
+  const int nbytes = npad / 4;
+  for (int b0 = blockIdx.y * (kXposeSamples / 4); b0 < nbytes; b0 += gridDim.y * (kXposeSamples / 4)) {
+    const int cb = min(kXposeSamples / 4, nbytes - b0);  // packed bytes of this tile (a multiple of 32)
+    __syncthreads();
+    // 128 rows x 64 bytes: four 16-byte pieces per row, 512 pieces over 256 threads
+    for (int e = tid; e < 128 * 4; e += blockDim.x) {
+      const int j = e >> 2, q = e & 3;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (j < jlim && q * 16 < cb) v = *reinterpret_cast<const uint4*>(bed + (p0 + j) * stride + b0 + q * 16);
+      *reinterpret_cast<uint4*>(&tile[j][q * 16]) = v;
+    }
+    __syncthreads();
+    // warp v: samples 32v .. 32v+31 of the tile (packed bytes 8v .. 8v+7)
+    if (warp * 8 < cb) {
+      uint32_t out[8];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const uint2 r = *reinterpret_cast<const uint2*>(&tile[32 * t + lane][8 * warp]);
+        uint32_t lo = r.x, hi = r.y;
+        xpose2_warp(lo, hi, lane);  // lane = sample; lo / hi = positions 32t .. +15 / +16 .. +31
+        out[2 * t] = lo;
+        out[2 * t + 1] = hi;
+      }
+      const int64_t row = (int64_t)b0 * 4 + 32 * warp + lane;
+      uint4* dst = reinterpret_cast<uint4*>(bt + row * tpitch + (int64_t)w * (ldw >> 2) + jt * 32);
+      dst[0] = make_uint4(out[0], out[1], out[2], out[3]);
+      dst[1] = make_uint4(out[4], out[5], out[6], out[7]);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -1424,6 +1475,19 @@ void launch_g_finish(const GFinishArgs& a, int* Eh, double* hunit, double* gmuni
 void launch_h_finish(const HFinishArgs& a, cudaStream_t s) {
   const int64_t n = (int64_t)a.nsamples * a.LP;
   k_tc_h_finish<<<ceil_div(n, 256), 256, 0, s>>>(a);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_transpose_codes(const uint8_t* bed, int64_t stride, int64_t M, int64_t ws, int64_t ldw, int nwin,
+                            int npad, uint8_t* bt, int64_t tpitch, cudaStream_t s) {
+  if (M == 0 || nwin == 0) return;
+  if (ldw % 128 != 0 || ldw < ws || npad % 128 != 0 || (int64_t)npad / 4 > stride || tpitch < nwin * (ldw / 4))
+    throw Error(-1, "internal: sample-major copy layout");
+  if (stride % 16 != 0 || tpitch % 16 != 0 || ((uintptr_t)bed & 15u) != 0 || ((uintptr_t)bt & 15u) != 0)
+    throw Error(-1, "internal: sample-major copy alignment");
+  const int ytiles = std::max(1, std::min(ceil_div(npad, kXposeSamples), 4));
+  dim3 grid((unsigned)(ldw / 128), (unsigned)ytiles, (unsigned)nwin);
+  k_transpose_codes<<<grid, 256, 0, s>>>(bed, stride, M, ws, ldw, npad, bt, tpitch);
   PCAONE_LAUNCH_CHECK();
 }
 

@@ -12,6 +12,9 @@ namespace tc {
 // G = X_w * W for one SNP window (see prod_tc.cu)
 struct GArgs {
   int64_t pos0;           // first position of the window (row of the packed matrix)
+  int64_t kofs;           // K elements before the first of this product in the operand's rows (0 for G;
+                          // the window's column offset when the kernel runs an H product on the
+                          // sample-major copy)
   int nsnp;               // SNPs in the window
   int LP;                 // padded sketch width (multiple of 16, <= 112)
   int nslice;             // BF16 slices of W (1..3)
@@ -28,6 +31,12 @@ struct GArgs {
   long long wait_cycles;  // limit of the pipeline waits in SM cycles (0: about 2 s)
   int fp8;                // 1: E4M3 operands (128 samples per pipeline stage)
 };
+
+// Sample-major copy of the packed rows for the H products (k_tc_g then runs
+// H on it): block w of every sample row holds window w's codes, ldw positions
+// per block (a multiple of 128), tpitch bytes per sample row.
+void launch_transpose_codes(const uint8_t* bed, int64_t stride, int64_t M, int64_t ws, int64_t ldw, int nwin,
+                            int npad, uint8_t* bt, int64_t tpitch, cudaStream_t s);
 
 // H += X_w^T * Gh for one SNP window (dosage part; k_tc_h_finish adds the
 // missing-entry sums gathered by k_seg_gather)
