@@ -134,11 +134,13 @@ class ClockSampler:
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # tensor-core window products, from one ncu capture of a window of the
-# workload's shape, keyed by (workload, product)
+# workload's shape, keyed by (workload, product class of kernel_stats)
 NCU_TRAFFIC = {
-    # one capture of a window of the 1M-SNP workload (15,625 SNPs x 200,064 samples)
-    ("c3", "k_tc_h<e4m3>"): 787.7e6 + 184.1e6,
-    ("c3", "k_tc_g<e4m3>"): 827.2e6 + 119.3e6,
+    # one capture of a window of the 1M-SNP workload (15,625 SNPs x 200,064
+    # samples); the E4M3 G and H products both run k_tc_g<2> (H on the
+    # sample-major copy)
+    ("c3", "g_product_e4m3"): 821.3e6 + 118.8e6,
+    ("c3", "h_product_e4m3"): 841.3e6 + 182.0e6,
 }
 
 
@@ -694,33 +696,42 @@ def run_ours(args):
         ooc = out_of_core_block(args, capi, local, pinned, M, N, params, (U, S, V), ctx.perm())
     d2h = (N + M) * wl["k"] * 8 + wl["k"] * 8
 
-    # ---- roofline of the dominant kernel ----
-    dom = max(kstats, key=lambda k: kstats[k]["ms"])
-    ks = kstats[dom]
-    e4m3 = dom.endswith("_e4m3")
-    achieved = ks["flops"] / (ks["ms"] / 1e3) / 1e12 if ks["ms"] > 0 else 0.0
+    # ---- roofline of the dominant kernel (and of every product class) ----
     bf16_peak = peaks.get("bf16_tflops", PEAKS_FALLBACK["bf16_tflops"])
-    # the dense E4M3 rate is twice the BF16 one on this tensor core (4.5 vs 2.25
-    # PFLOP/s nominal); no FP8 GEMM is measured, so its peak is 2x the measured BF16
-    peak = 2.0 * bf16_peak if e4m3 else bf16_peak
     tc = args.precision != "fp32"
     LPtc = (L + 15) // 16 * 16
-    nslices = 2 if e4m3 else 6 if args.precision == "fp64" else 3
-    executed = achieved * (nslices * LPtc / L) if tc else achieved
-    per_launch_s = ks["ms"] / 1e3 / max(1, ks["launches"])
-    kname = ("k_tc_" + dom[0] + ("<e4m3>" if e4m3 else "")) if tc else f"k_window_{dom[0]}"
-    traffic = NCU_TRAFFIC.get((args.workload, kname)) if tc else None
-    roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": traffic, "kernel": kname,
-            "executed_tflops": executed, "executed_frac": executed / peak,
-            "hbm_gbs": (traffic / per_launch_s / 1e9) if traffic else None,
-            "note": (f"{args.precision} form; {ks['launches']} launches, {ks['ms']:.1f} ms of "
-                     f"{sum(times) * 1e3:.1f} ms; achieved = algorithmic 2*N*SNPs*L per launch / event time; "
-                     f"peak = {'2x ' if e4m3 else ''}{peak_kind} bf16 dense"
-                     f"{' (E4M3 dense rate)' if e4m3 else ''}; executed counts {nslices} integer slices of "
-                     f"{LPtc} columns; traffic per launch from ncu of the same window shape")}
-    if not tc:
-        roof["note"] += "; the FP32 form runs on CUDA cores, not the tensor pipe"
+
+    def roofline_of(cls):
+        ks = kstats[cls]
+        e4m3 = cls.endswith("_e4m3")
+        achieved = ks["flops"] / (ks["ms"] / 1e3) / 1e12 if ks["ms"] > 0 else 0.0
+        # the dense E4M3 rate is twice the BF16 one on this tensor core (4.5 vs
+        # 2.25 PFLOP/s nominal); no FP8 GEMM is measured, so its peak is 2x the
+        # measured BF16
+        peak = 2.0 * bf16_peak if e4m3 else bf16_peak
+        nslices = 2 if e4m3 else 6 if args.precision == "fp64" else 3
+        executed = achieved * (nslices * LPtc / L) if tc else achieved
+        per_launch_s = ks["ms"] / 1e3 / max(1, ks["launches"])
+        # both tensor-core products run k_tc_g (mode 2: E4M3, 0: BF16 digits); H
+        # reads the sample-major copy of the rows
+        kname = (f"k_tc_g<{2 if e4m3 else 0}> ({cls[0].upper()} product)") if tc else f"k_window_{cls[0]}"
+        traffic = NCU_TRAFFIC.get((args.workload, cls)) if tc else None
+        r = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+             "frac": achieved / peak, "traffic": traffic, "kernel": kname,
+             "executed_tflops": executed, "executed_frac": executed / peak,
+             "hbm_gbs": (traffic / per_launch_s / 1e9) if traffic else None,
+             "note": (f"{args.precision} form; {ks['launches']} launches, {ks['ms']:.1f} ms of "
+                      f"{sum(times) * 1e3:.1f} ms; achieved = algorithmic 2*N*SNPs*L per launch / event time; "
+                      f"peak = {'2x ' if e4m3 else ''}{peak_kind} bf16 dense"
+                      f"{' (E4M3 dense rate)' if e4m3 else ''}; executed counts {nslices} integer slices of "
+                      f"{LPtc} columns; traffic per launch from ncu of the same window shape (null: not captured)")}
+        if not tc:
+            r["note"] += "; the FP32 form runs on CUDA cores, not the tensor pipe"
+        return r
+
+    dom = max(kstats, key=lambda k: kstats[k]["ms"])
+    roof = roofline_of(dom)
+    roof_by_class = {cls: roofline_of(cls) for cls in kstats if kstats[cls]["launches"] > 0}
 
     # ---- accuracy against the FP64-grade form; the FP32 CUDA-core form ----
     accuracy = None
@@ -751,6 +762,7 @@ def run_ours(args):
                     "load_gbs": M * bps / statistics.median(load_s[1:]) / 1e9 if len(load_s) > 1 else None},
             "gpu_launches": int(launches),
             "roofline": roof,
+            "roofline_by_class": roof_by_class,
             "cpu_baseline": cpu,
             "kernels": kstats,
             "host_s": host_phases,
