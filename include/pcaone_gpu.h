@@ -211,6 +211,32 @@ int pcaone_gpu_load_synthetic(pcaone_gpu_ctx* ctx, uint64_t nsnps, uint32_t nsam
  * bytes, the .bed body). */
 int pcaone_gpu_get_bed(pcaone_gpu_ctx* ctx, uint8_t* packed);
 
+/* ---- PLINK2 input: replaces FilePgen (src/FilePgen.hpp, FilePgen.cpp:27-86) -
+ * Hard calls only: ALT allele counts 0/1/2 (3 = missing), the values FilePgen
+ * takes from pgenlib's ReadHardcalls, dosage v / 2 (FilePgen.cpp:16-21); they
+ * become PLINK 1 codes with A1 = ALT on the device, so counts, allele
+ * frequencies and every product equal those of the same genotypes in a .bed.
+ * The reference uses .pgen dosages when the file has them unless --hardcall
+ * is given; this library reads hard calls in both cases.
+ *
+ * genovecs: nsnps rows of hard calls, 2 bits per sample (the layout of
+ * pgenlib's genovec, sample i in bits 2(i%4) of byte i/4), row_pitch bytes
+ * apart (>= ceil(nsamples/4); 0 = packed). */
+int pcaone_gpu_load_pgen_genovecs(pcaone_gpu_ctx* ctx, const uint8_t* genovecs, uint64_t row_pitch, uint64_t nsnps,
+                                  uint32_t nsamples);
+/* A whole .pgen file image in a storage mode this library reads itself:
+ * 0x01 (PLINK 1 variant-major rows; nsamples from the .psam), or the
+ * fixed-width 0x02 / 0x03 / 0x04 (12-byte header with the variant and sample
+ * counts, nsamples from the .psam checked against it when nonzero).
+ * Variable-width (compressed) files return PCAONE_E_FORMAT: pgenlib decodes
+ * those on the host, for pcaone_gpu_load_pgen_genovecs. */
+int pcaone_gpu_load_pgen_file_image(pcaone_gpu_ctx* ctx, const uint8_t* image, uint64_t image_bytes,
+                                    uint32_t nsamples);
+/* The layout pcaone_gpu_load_pgen_file_image reads (no GPU needed): storage
+ * mode, counts, offset of the first record and bytes per record. */
+int pcaone_gpu_pgen_layout(const uint8_t* image, uint64_t image_bytes, uint32_t nsamples, int* mode, uint64_t* nsnps,
+                           uint32_t* nsamples_out, uint64_t* offset, uint64_t* record_bytes);
+
 /* ---- out-of-core: replaces the -m/--memory path ---------------------------
  * FileBed::read_block_initial (src/FilePlink.cpp:122-218) with the block plan
  * of Data::prepare (src/Data.cpp:40-84) and the block loops of computeGandH

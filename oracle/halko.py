@@ -81,6 +81,19 @@ def shuffle_columns(n: int) -> np.ndarray:
     return out
 
 
+def genovec_to_bed(genovec: np.ndarray, nsamples: int) -> np.ndarray:
+    """PLINK 2 hard calls (2-bit ALT allele counts, 3 = missing: what pgenlib's
+    ReadHardcalls reports as 0, 1, 2, -3) as PLINK 1 codes with A1 = ALT, so
+    that BED2GENO gives the dosage FilePgen uses, v / 2 (src/FilePgen.cpp:16-21):
+    2 -> 00 (1.0), 1 -> 10 (0.5), 0 -> 11 (0.0), 3 -> 01 (missing)."""
+    g = np.asarray(genovec, dtype=np.uint8)
+    lut = np.array([3, 2, 0, 1], dtype=np.uint8)
+    out = np.zeros_like(g)
+    for s in range(4):
+        out |= lut[(g >> (2 * s)) & 3] << (2 * s)
+    return out
+
+
 def permute_plink_order(nsnps: int, nsamples: int, bands: int, buffer_gb: int = 2) -> np.ndarray:
     """The SNP order of the reference's out-of-core window method: order[p] is
     the .bed row that permute_plink (src/FilePlink.cpp:303-408) writes at row

@@ -5,7 +5,8 @@
 // (the reference's text writers keep 6 significant digits, src/Data.cpp:215).
 //
 // usage: ref_driver OUTDIR [driver options] <PCAone command-line options,
-//        e.g. -b prefix -k 10 -d 2> (PLINK -b input, or FileBinary -B input with -C 0)
+//        e.g. -b prefix -k 10 -d 2> (PLINK -b input, PLINK2 -p input read by the
+//        reference's pgenlib, or FileBinary -B input with -C 0)
 //
 // Driver options:
 //   --dump-g0             also write G0.npy (below)
@@ -51,6 +52,7 @@
 #include <vector>
 
 #include "FileBinary.hpp"
+#include "FilePgen.hpp"
 #include "FilePlink.hpp"
 #include "Halko.hpp"
 #include "Projection.hpp"
@@ -128,8 +130,8 @@ int main(int argc, char** argv) {
   if (force_os >= 0) params.oversamples = force_os;
   cao.cao.open(outdir + "/ref.log");
   cao.is_screen = false;
-  if (params.file_t != FileType::PLINK && params.file_t != FileType::BINARY) {
-    std::fprintf(stderr, "only PLINK and binary input are driven here\n");
+  if (params.file_t != FileType::PLINK && params.file_t != FileType::BINARY && params.file_t != FileType::PGEN) {
+    std::fprintf(stderr, "only PLINK, PGEN and binary input are driven here\n");
     return 2;
   }
   using clk = std::chrono::steady_clock;
@@ -140,12 +142,14 @@ int main(int argc, char** argv) {
   const bool ooc_permutation = params.perm && params.out_of_core && params.file_t == FileType::PLINK;
   PermMat ooc_perm;
   if (ooc_permutation) ooc_perm = permute_plink(params.filein, outdir + "/ooc", params.buffer, params.bands);
-  Data* data = params.file_t == FileType::PLINK ? (Data*)new FileBed(params) : (Data*)new FileBin(params);
+  Data* data = params.file_t == FileType::PLINK  ? (Data*)new FileBed(params)
+               : params.file_t == FileType::PGEN ? (Data*)new FilePgen(params)
+                                                 : (Data*)new FileBin(params);
   if (ooc_permutation) data->perm = ooc_perm;
   data->prepare();
   const auto t1 = clk::now();
   if (timing) dump_g0 = false;
-  if (params.file_t == FileType::PLINK && !timing) dump1(outdir, "F", data->F);
+  if ((params.file_t == FileType::PLINK || params.file_t == FileType::PGEN) && !timing) dump1(outdir, "F", data->F);
   if (dump_g0) dump(outdir, "G0", data->G);
 
   // operator selection and call sequence of run_pca_with_halko (src/Halko.cpp:271-320)

@@ -35,7 +35,8 @@ EXPORTS = [
     "pcaone_gpu_load_binary_file_image", "pcaone_gpu_load_synthetic_dense", "pcaone_gpu_project",
     "pcaone_gpu_random_omega", "pcaone_gpu_shuffle_order", "pcaone_gpu_set_wait_limit",
     "pcaone_gpu_load_bed_stream", "pcaone_gpu_load_bed_file_image_stream", "pcaone_gpu_stream_plan",
-    "pcaone_gpu_stream_info", "pcaone_gpu_ooc_order",
+    "pcaone_gpu_stream_info", "pcaone_gpu_ooc_order", "pcaone_gpu_load_pgen_genovecs",
+    "pcaone_gpu_load_pgen_file_image", "pcaone_gpu_pgen_layout",
 ]
 MLP_PARAMS, MLP_INPUTS = 82689, 64
 
@@ -120,6 +121,10 @@ def load(path: str = LIBPATH) -> ctypes.CDLL:
     lib.pcaone_gpu_load_bed_file_image_stream.argtypes = [c_void_p, c_void_p, c_uint64, c_uint64, c_uint32,
                                                           c_uint64, c_uint32]
     lib.pcaone_gpu_ooc_order.argtypes = [c_uint64, c_uint32, c_int, c_uint32, c_void_p]
+    lib.pcaone_gpu_load_pgen_genovecs.argtypes = [c_void_p, c_void_p, c_uint64, c_uint64, c_uint32]
+    lib.pcaone_gpu_load_pgen_file_image.argtypes = [c_void_p, c_void_p, c_uint64, c_uint32]
+    lib.pcaone_gpu_pgen_layout.argtypes = [c_void_p, c_uint64, c_uint32, P(c_int), P(c_uint64), P(c_uint32),
+                                           P(c_uint64), P(c_uint64)]
     lib.pcaone_gpu_stream_plan.argtypes = [c_uint64, c_uint32, c_int, c_int, c_uint64, P(c_uint64), P(c_uint64)]
     lib.pcaone_gpu_stream_info.argtypes = [c_void_p, P(c_int), P(c_double)]
     for name in EXPORTS:
@@ -157,6 +162,17 @@ def stream_plan(nsnps: int, nsamples: int, svd: int, bands: int, device_budget: 
     if rc != PCAONE_OK:
         raise PcaoneError(rc, "pcaone_gpu_stream_plan failed")
     return int(b.value), int(nb.value)
+
+
+def pgen_layout(image: bytes, nsamples: int = 0) -> dict:
+    """The storage layout of a .pgen image (pcaone_gpu_pgen_layout): host only."""
+    buf = np.frombuffer(image, dtype=np.uint8)
+    mode, m, n, off, rec = c_int(0), c_uint64(0), c_uint32(0), c_uint64(0), c_uint64(0)
+    rc = load().pcaone_gpu_pgen_layout(_ptr(buf), buf.size, nsamples, ctypes.byref(mode), ctypes.byref(m),
+                                       ctypes.byref(n), ctypes.byref(off), ctypes.byref(rec))
+    if rc != PCAONE_OK:
+        raise PcaoneError(rc, "pcaone_gpu_pgen_layout failed")
+    return {"mode": mode.value, "nsnps": m.value, "nsamples": n.value, "offset": off.value, "record_bytes": rec.value}
 
 
 def ooc_order(nsnps: int, nsamples: int, bands: int, buffer_gb: int = 2) -> np.ndarray:
@@ -278,6 +294,19 @@ class Context:
         self._check(self.lib.pcaone_gpu_load_bed_file_image_stream(self.h, _ptr(buf), buf.size, nsnps, nsamples,
                                                                    int(device_budget), int(buffer_gb)))
         self.nsamples, self.nsnps = int(nsamples), int(nsnps)
+
+    def load_pgen_genovecs(self, genovecs: np.ndarray, nsamples: int):
+        """PLINK 2 hard calls (pcaone_gpu_load_pgen_genovecs): rows of 2-bit ALT
+        counts, 3 = missing."""
+        g = np.ascontiguousarray(genovecs, dtype=np.uint8)
+        self._check(self.lib.pcaone_gpu_load_pgen_genovecs(self.h, _ptr(g), g.shape[1], g.shape[0], nsamples))
+        self.nsamples, self.nsnps = int(nsamples), int(g.shape[0])
+
+    def load_pgen_file_image(self, image: bytes, nsamples: int = 0):
+        buf = np.frombuffer(image, dtype=np.uint8)
+        lay = pgen_layout(image, nsamples)
+        self._check(self.lib.pcaone_gpu_load_pgen_file_image(self.h, _ptr(buf), buf.size, nsamples))
+        self.nsamples, self.nsnps = int(lay["nsamples"]), int(lay["nsnps"])
 
     def stream_info(self):
         """(streamed, bytes copied into the device slots since the last call)."""

@@ -148,6 +148,22 @@ __global__ void k_synth(uint8_t* __restrict__ bed, int64_t stride, int64_t snp0,
   bed[jl * stride + q] = (uint8_t)byte;
 }
 
+// PLINK 2 hard calls (2-bit ALT allele counts, 3 = missing) to PLINK 1 codes
+// with A1 = ALT, in place over a byte range: with a = b1 b0 the code is
+// (NOT b1, NOT (b1 XOR b0)): 2 -> 00, 1 -> 10, 0 -> 11, 3 -> 01.  Four bytes
+// per thread; padding lanes of the last byte of a row are cleared afterwards
+// by the sanitation pass.
+__global__ void k_genovec_to_bed(uint8_t* __restrict__ bytes, int64_t nbytes) {
+  const int64_t i0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * 4;
+  if (i0 >= nbytes) return;
+  const int cnt = nbytes - i0 < 4 ? (int)(nbytes - i0) : 4;
+  uint32_t w = 0;
+  for (int k = 0; k < cnt; ++k) w |= (uint32_t)bytes[i0 + k] << (8 * k);
+  const uint32_t lo = w & 0x55555555u, hi = (w >> 1) & 0x55555555u;
+  w = ((~hi & 0x55555555u) << 1) | (~(hi ^ lo) & 0x55555555u);
+  for (int k = 0; k < cnt; ++k) bytes[i0 + k] = (uint8_t)(w >> (8 * k));
+}
+
 // Rows perm[0 .. nrows) of src into consecutive rows of dst (stride bytes
 // each, a multiple of 16), for sources across the host link (pinned host
 // memory mapped into the device address space), whose latency wants many
@@ -189,6 +205,12 @@ void launch_gather_rows_deep(const uint8_t* src, uint8_t* dst, int64_t stride, c
   if ((stride & 15) != 0 || ((uintptr_t)src & 15u) != 0 || ((uintptr_t)dst & 15u) != 0)
     throw Error(PCAONE_E_ARG, "internal: row gather needs 16-byte aligned rows");
   k_gather_rows_deep<<<ctas, 256, 0, s>>>(src, dst, stride, perm, nrows);
+  PCAONE_LAUNCH_CHECK();
+}
+
+void launch_genovec_to_bed(uint8_t* bytes, int64_t nbytes, cudaStream_t s) {
+  if (nbytes <= 0) return;
+  k_genovec_to_bed<<<ceil_div(ceil_div(nbytes, 4), 256), 256, 0, s>>>(bytes, nbytes);
   PCAONE_LAUNCH_CHECK();
 }
 

@@ -367,15 +367,24 @@ static void ensure_missing_total(Context& c) {
 // rows into the pinned host copy through its device address.
 static void load_rows_to_host_copy(Context& c, const uint8_t* packed, int64_t bps);
 
-static void load_bed_host(Context& c, const uint8_t* packed, uint64_t nsnps, uint32_t nsamples, bool stream = false) {
+//
+// PLINK 2 hard calls (hardcalls: rows of 2-bit ALT allele counts, 3 =
+// missing, src_pitch bytes apart) are translated to PLINK 1 codes on the
+// device before the re-pitch.
+static void load_bed_host(Context& c, const uint8_t* packed, uint64_t nsnps, uint32_t nsamples, bool stream = false,
+                          bool hardcalls = false, int64_t src_pitch = 0) {
   load_common(c, nsnps, nsamples, false, stream);
   const int64_t bps = ((int64_t)nsamples + 3) / 4;
+  if (src_pitch == 0) src_pitch = bps;
+  if (src_pitch < bps) throw Error(PCAONE_E_ARG, "row pitch shorter than a row");
   if (stream) {
+    if (hardcalls || src_pitch != bps) throw Error(PCAONE_E_ARG, "the out-of-core load takes PLINK 1 rows");
     load_rows_to_host_copy(c, packed, bps);
     return;
   }
-  if (bps == c.stride) {
+  if (bps == c.stride && src_pitch == bps) {
     PCAONE_CUDA(cudaMemcpyAsync(c.bed.p, packed, (size_t)c.M * bps, cudaMemcpyHostToDevice, c.stream));
+    if (hardcalls) launch_genovec_to_bed(c.bed.p, c.M * bps, c.stream);
     finish_load(c);
     return;
   }
@@ -389,10 +398,15 @@ static void load_bed_host(Context& c, const uint8_t* packed, uint64_t nsnps, uin
     // the buffer is free once the re-pitch that last read it has run (for the
     // first two chunks: once the context's stream reached this load)
     PCAONE_CUDA(cudaStreamWaitEvent(c.copy_stream, q >= 2 ? c.ev_free[b] : c.ev_free[2], 0));
-    PCAONE_CUDA(cudaMemcpyAsync(buf, packed + (size_t)j0 * bps, (size_t)n * bps, cudaMemcpyHostToDevice,
-                                c.copy_stream));
+    if (src_pitch == bps)
+      PCAONE_CUDA(cudaMemcpyAsync(buf, packed + (size_t)j0 * bps, (size_t)n * bps, cudaMemcpyHostToDevice,
+                                  c.copy_stream));
+    else
+      PCAONE_CUDA(cudaMemcpy2DAsync(buf, (size_t)bps, packed + (size_t)j0 * src_pitch, (size_t)src_pitch, (size_t)bps,
+                                    (size_t)n, cudaMemcpyHostToDevice, c.copy_stream));
     PCAONE_CUDA(cudaEventRecord(c.ev_copied[b], c.copy_stream));
     PCAONE_CUDA(cudaStreamWaitEvent(c.stream, c.ev_copied[b], 0));
+    if (hardcalls) launch_genovec_to_bed(buf, n * bps, c.stream);
     launch_repitch(buf, bps, c.rows_mut() + (size_t)j0 * c.stride, c.stride, n, bps, c.stream);
     PCAONE_CUDA(cudaEventRecord(c.ev_free[b], c.stream));
   }
@@ -1843,6 +1857,64 @@ static int guarded(pcaone_gpu_ctx* ctx, F&& fn) {
   }
 }
 
+namespace pcaone {
+// Layout of a .pgen image this library reads itself (FilePgen, src/FilePgen.hpp:13-40,
+// reads every .pgen through pgenlib): PLINK 1 variant-major rows (storage mode
+// 0x01: the 3 magic bytes, then ceil(N/4)-byte rows, the sample count from the
+// caller's .psam), or the fixed-width PLINK 2 modes 0x02 (2-bit hard calls),
+// 0x03 (hard calls, then 2 N bytes of dosages per record) and 0x04 (then 4 N
+// bytes of dosages and phased dosages): magic, mode, variant and sample counts
+// (little-endian uint32), and a control byte whose low six bits are zero and
+// whose top two say where the non-reference flags are (3: one bit per variant
+// right after the 12 header bytes).  Only the hard calls are read.
+// Variable-width files (compressed records) are decoded by pgenlib on the host,
+// whose hard calls pcaone_gpu_load_pgen_genovecs takes.
+struct PgenLayout {
+  int mode = 0;
+  uint64_t nsnps = 0, offset = 0, pitch = 0;
+  uint32_t nsamples = 0;
+};
+
+static uint32_t le32(const uint8_t* p) {
+  return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+}
+
+PgenLayout pgen_layout(const uint8_t* img, uint64_t bytes, uint32_t nsamples_psam) {
+  if (!img || bytes < 3 || img[0] != 0x6c || img[1] != 0x1b) throw Error(PCAONE_E_FORMAT, "not a .pgen file (magic)");
+  PgenLayout l;
+  l.mode = img[2];
+  if (l.mode == 0x01) {
+    if (nsamples_psam == 0) throw Error(PCAONE_E_ARG, "a PLINK 1 mode .pgen needs the sample count of its .psam");
+    l.nsamples = nsamples_psam;
+    l.pitch = ((uint64_t)l.nsamples + 3) / 4;
+    l.offset = 3;
+    if ((bytes - 3) % l.pitch != 0) throw Error(PCAONE_E_FORMAT, "PLINK 1 mode .pgen: size is not a whole number of rows");
+    l.nsnps = (bytes - 3) / l.pitch;
+    return l;
+  }
+  if (l.mode == 0x00) throw Error(PCAONE_E_FORMAT, "sample-major PLINK 1 data");
+  if (l.mode >= 0x10)
+    throw Error(PCAONE_E_FORMAT, "variable-width .pgen (compressed records): decode the records with pgenlib and pass "
+                                 "the hard calls to pcaone_gpu_load_pgen_genovecs");
+  if (l.mode > 0x04) throw Error(PCAONE_E_FORMAT, "unknown .pgen storage mode");
+  if (bytes < 12) throw Error(PCAONE_E_FORMAT, "truncated .pgen header");
+  l.nsnps = le32(img + 3);
+  l.nsamples = le32(img + 7);
+  const uint8_t ctrl = img[11];
+  if (ctrl & 63) throw Error(PCAONE_E_FORMAT, "fixed-width .pgen with a variable-width control byte");
+  if (l.nsnps == 0 || l.nsamples == 0) throw Error(PCAONE_E_FORMAT, ".pgen with no variants or samples");
+  if (nsamples_psam != 0 && nsamples_psam != l.nsamples)
+    throw Error(PCAONE_E_ARG, ".pgen sample count differs from the .psam: " + std::to_string(l.nsamples) + " vs " +
+                                  std::to_string(nsamples_psam));
+  l.offset = 12 + ((ctrl >> 6) == 3 ? (l.nsnps + 7) / 8 : 0);
+  l.pitch = ((uint64_t)l.nsamples + 3) / 4 + (l.mode == 0x03 ? 2ull : l.mode == 0x04 ? 4ull : 0ull) * l.nsamples;
+  if (bytes != l.offset + l.nsnps * l.pitch)
+    throw Error(PCAONE_E_FORMAT, ".pgen size " + std::to_string(bytes) + " bytes, expected " +
+                                     std::to_string(l.offset + l.nsnps * l.pitch));
+  return l;
+}
+}  // namespace pcaone
+
 static void check_bed_image(const uint8_t* image, uint64_t image_bytes, uint64_t nsnps, uint32_t nsamples) {
   if (!image || image_bytes < 3) throw Error(PCAONE_E_FORMAT, "truncated .bed image");
   if (image[0] != 0x6c || image[1] != 0x1b || image[2] != 0x01)
@@ -2033,6 +2105,38 @@ int pcaone_gpu_stream_info(pcaone_gpu_ctx* ctx, int* streamed, double* bytes_fet
     if (streamed) *streamed = c.streamed ? 1 : 0;
     if (bytes_fetched) *bytes_fetched = c.stream_bytes;
     c.stream_bytes = 0;
+  });
+}
+
+int pcaone_gpu_pgen_layout(const uint8_t* image, uint64_t image_bytes, uint32_t nsamples, int* mode, uint64_t* nsnps,
+                           uint32_t* nsamples_out, uint64_t* offset, uint64_t* record_bytes) {
+  try {
+    const pcaone::PgenLayout l = pcaone::pgen_layout(image, image_bytes, nsamples);
+    if (mode) *mode = l.mode;
+    if (nsnps) *nsnps = l.nsnps;
+    if (nsamples_out) *nsamples_out = l.nsamples;
+    if (offset) *offset = l.offset;
+    if (record_bytes) *record_bytes = l.pitch;
+    return PCAONE_OK;
+  } catch (const Error& e) {
+    return e.code;
+  }
+}
+
+int pcaone_gpu_load_pgen_file_image(pcaone_gpu_ctx* ctx, const uint8_t* image, uint64_t image_bytes, uint32_t nsamples) {
+  return guarded(ctx, [&](Context& c) {
+    const pcaone::PgenLayout l = pcaone::pgen_layout(image, image_bytes, nsamples);
+    pcaone::load_bed_host(c, image + l.offset, l.nsnps, l.nsamples, false, l.mode != 0x01, (int64_t)l.pitch);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_load_pgen_genovecs(pcaone_gpu_ctx* ctx, const uint8_t* genovecs, uint64_t row_pitch, uint64_t nsnps,
+                                  uint32_t nsamples) {
+  return guarded(ctx, [&](Context& c) {
+    if (!genovecs) throw Error(PCAONE_E_ARG, "null buffer");
+    pcaone::load_bed_host(c, genovecs, nsnps, nsamples, false, true, (int64_t)row_pitch);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
   });
 }
 

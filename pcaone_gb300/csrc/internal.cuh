@@ -124,6 +124,9 @@ void launch_sanitize_padding(uint8_t* bed, int64_t stride, int64_t nsnps, int ns
 void launch_repitch(const uint8_t* src, int64_t src_pitch, uint8_t* dst, int64_t dst_pitch, int64_t nrows, int64_t bps,
                     cudaStream_t s);
 void launch_counts(const BedView& v, int32_t* counts, double* F, cudaStream_t s);
+// PLINK 2 hard calls (ALT counts, 3 = missing) -> PLINK 1 codes (A1 = ALT), in
+// place over nbytes bytes
+void launch_genovec_to_bed(uint8_t* bytes, int64_t nbytes, cudaStream_t s);
 // rows perm[0 .. nrows) (identity when perm is null) of src into consecutive
 // rows of dst, many 16-byte loads in flight per thread (sources across the
 // host link); ctas thread blocks of 256

@@ -79,6 +79,31 @@ class FileBed:
         self.ctx.close()
 
 
+class FilePgen(FileBed):
+    """PLINK2 fileset on the GPU (src/FilePgen.hpp:13-40): the sample count from
+    the .psam (lines not starting with '#'), hard calls from the .pgen (storage
+    modes 0x01-0x04; variable-width files are decoded by pgenlib on the host and
+    given as ``genovecs``, rows of 2-bit ALT counts with 3 = missing)."""
+
+    def __init__(self, prefix: Optional[str] = None, *, genovecs: Optional[np.ndarray] = None,
+                 nsamples: Optional[int] = None, device: int = 0, verbose: int = 0):
+        self.ctx = capi.Context(device, verbose)
+        self.out_of_core = False
+        if prefix is not None:
+            with open(prefix + ".psam") as f:
+                n = sum(1 for line in f if line.strip() and not line.startswith("#"))
+            with open(prefix + ".pgen", "rb") as f:
+                image = f.read()
+            self.ctx.load_pgen_file_image(image, n)
+        elif genovecs is not None and nsamples is not None:
+            self.ctx.load_pgen_genovecs(genovecs, nsamples)
+        else:
+            raise ValueError("give a PLINK2 prefix or hard calls with nsamples")
+        self.nsamples = self.ctx.nsamples
+        self.nsnps = self.ctx.nsnps
+        self._counts = None
+
+
 @dataclass
 class Param:
     """The Param fields the RSVD path reads (src/Cmd.hpp:16-98) with the CLI's

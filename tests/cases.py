@@ -71,7 +71,7 @@ def parse_options(opts) -> RunOptions:
             o.emu = True
         elif a in ("-C", "--scale"):
             o.scale = int(next(it))
-        elif a in ("-b", "-B"):
+        elif a in ("-b", "-B", "-p", "--pgen"):
             next(it)
         elif a in ("-m", "--memory"):
             o.memory = float(next(it))
@@ -132,6 +132,29 @@ def binary_cases():
         meta = ref["meta"]
         out.append(BinaryCase(os.path.basename(path)[:-4], z["dense"], int(meta[0]), int(meta[1]), opts, ref))
     return out
+
+
+def pgen_cases():
+    """PLINK2 fixtures: fixed-width .pgen hard calls (genovec rows), read by the
+    reference through its pgenlib (-p)."""
+    out = []
+    for path in sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz"))):
+        z = np.load(path)
+        if "genovec" not in z.files:
+            continue
+        opts = parse_options(json.loads(str(z["options"])))
+        ref = {k: z[k] for k in z.files if k not in ("genovec", "options")}
+        meta = ref["meta"]
+        out.append(GoldenCase(os.path.basename(path)[:-4], z["genovec"], int(meta[0]), int(meta[1]), opts, ref))
+    return out
+
+
+def pgen_image(genovec: np.ndarray, nsamples: int) -> bytes:
+    """A fixed-width (storage mode 0x02) .pgen of the genovec rows: magic, mode,
+    variant count, sample count, control byte, then the records."""
+    m = genovec.shape[0]
+    head = bytes([0x6C, 0x1B, 0x02]) + int(m).to_bytes(4, "little") + int(nsamples).to_bytes(4, "little") + bytes([0])
+    return head + np.ascontiguousarray(genovec[:, : (nsamples + 3) // 4]).tobytes()
 
 
 def golden_case(name: str) -> GoldenCase:

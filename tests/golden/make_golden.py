@@ -7,6 +7,7 @@ tests never run this):
     python tests/golden/make_golden.py         # all fixtures
     python tests/golden/make_golden.py --eigs-only   # only tests/golden/eigs/
     python tests/golden/make_golden.py --ooc-only    # only the out-of-core (-m) cases
+    python tests/golden/make_golden.py --pgen-only   # only the PLINK2 .pgen cases
 
 Each case draws a seeded synthetic PLINK fileset (pcaone_gb300.synthetic),
 runs the reference's RSVD operators through oracle/_ref/ref_driver with the
@@ -31,6 +32,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
 from pcaone_gb300 import synthetic  # noqa: E402
+from tests.cases import pgen_image  # noqa: E402
 
 DRIVER = os.path.join(REPO, "oracle", "_ref", "ref_driver")
 
@@ -91,6 +93,57 @@ def run_ooc_case(name: str, model_kw: dict, opts: list) -> dict:
         if os.path.exists(os.path.join(out, "perm.npy")):
             res["perm"] = np.load(os.path.join(out, "perm.npy"))
     res["packed"] = packed
+    res["options"] = np.array(json.dumps(opts))
+    return res
+
+
+# PLINK2 input (-p prefix), read by the reference's pgenlib: fixed-width
+# .pgen files (storage mode 0x02: a 12-byte header -- magic, mode, variant
+# count, sample count, control byte -- then one record of ceil(N/4) bytes per
+# variant, 2-bit ALT allele counts, 3 = missing), with a .psam listing the samples
+PGEN_CASES = {
+    "pgen_wsvd_n301": (dict(nsamples=301, nsnps=2400, npop=3, fst=0.1, seed=31, mcar=0.01),
+                       ["-d", "2", "-k", "4", "--maxp", "6", "-w", "16"]),
+    "pgen_em_ssvd_n203": (dict(nsamples=203, nsnps=1500, npop=3, fst=0.1, seed=32, mcar=0.05),
+                          ["-d", "1", "--emu", "--maxiter", "5", "--maxp", "4", "-k", "3"]),
+}
+
+
+def bed_to_genovec(packed: np.ndarray, nsamples: int) -> np.ndarray:
+    """PLINK 1 codes -> PLINK 2 hard calls (ALT allele counts, A1 = ALT):
+    00 -> 2, 10 -> 1, 11 -> 0, 01 (missing) -> 3; padding lanes zero."""
+    p = np.asarray(packed, dtype=np.uint8)
+    out = np.zeros_like(p)
+    lut = np.array([2, 3, 1, 0], dtype=np.uint8)
+    for s in range(4):
+        out |= lut[(p >> (2 * s)) & 3] << (2 * s)
+    nb = (nsamples + 3) // 4
+    if nsamples % 4:
+        out[:, nb - 1] &= np.uint8((1 << (2 * (nsamples % 4))) - 1)
+    return out
+
+
+def run_pgen_case(name: str, model_kw: dict, opts: list) -> dict:
+    model = synthetic.draw_population_model(**model_kw)
+    packed = synthetic.sample_packed_bed(model)
+    genovec = bed_to_genovec(packed, model.nsamples)
+    with tempfile.TemporaryDirectory() as td:
+        prefix = os.path.join(td, name)
+        with open(prefix + ".pgen", "wb") as f:
+            f.write(pgen_image(genovec, model.nsamples))
+        with open(prefix + ".psam", "w") as f:
+            f.write("#IID\n" + "".join(f"s{i}\n" for i in range(model.nsamples)))
+        out = os.path.join(td, "out")
+        os.makedirs(out)
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        subprocess.check_call([DRIVER, out, "--dump-g0", "-p", prefix] + opts, env=env)
+        res = {k: np.load(os.path.join(out, k + ".npy")) for k in ("F", "U", "S", "V", "Omg0", "meta")}
+        g0 = np.load(os.path.join(out, "G0.npy"))
+        res["G0_sha256"] = np.frombuffer(hashlib.sha256(np.asfortranarray(g0).tobytes(order="F")).digest(),
+                                         dtype=np.uint8)
+        if os.path.exists(os.path.join(out, "perm.npy")):
+            res["perm"] = np.load(os.path.join(out, "perm.npy"))
+    res["genovec"] = genovec
     res["options"] = np.array(json.dumps(opts))
     return res
 
@@ -220,6 +273,12 @@ def main() -> None:
         for name in EIGS_CASES:
             run_eigs_case(name)
         return
+    if "--pgen-only" in sys.argv:
+        for name, (mkw, opts) in PGEN_CASES.items():
+            res = run_pgen_case(name, mkw, opts)
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+            print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"])
+        return
     if "--ooc-only" in sys.argv:
         for name, (mkw, opts) in OOC_CASES.items():
             res = run_ooc_case(name, mkw, opts)
@@ -238,6 +297,10 @@ def main() -> None:
         res = run_projection_case(name, mkw, nb, opts)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
         print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"], "P2[0]=", res["P2"][0])
+    for name, (mkw, opts) in PGEN_CASES.items():
+        res = run_pgen_case(name, mkw, opts)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+        print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"])
     for name, (mkw, opts) in OOC_CASES.items():
         res = run_ooc_case(name, mkw, opts)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)

@@ -2,6 +2,7 @@
 import os
 import re
 
+import numpy as np
 import pytest
 
 from pcaone_gb300 import build as B
@@ -106,3 +107,37 @@ def test_stream_plan(lib):
         with pytest.raises(capi.PcaoneError) as e:
             capi.stream_plan(*bad)
         assert e.value.code == -1
+
+
+def test_pgen_layout(lib):
+    """The .pgen storage modes the library reads itself (no GPU needed)."""
+    from tests.cases import pgen_cases, pgen_image
+    case = pgen_cases()[0]
+    N, M = case.nsamples, case.nsnps
+    bps = (N + 3) // 4
+    img = pgen_image(case.packed, N)
+    assert capi.pgen_layout(img) == {"mode": 2, "nsnps": M, "nsamples": N, "offset": 12, "record_bytes": bps}
+    assert capi.pgen_layout(img, N)["mode"] == 2
+    # the sample count of the .psam must agree
+    with pytest.raises(capi.PcaoneError) as e:
+        capi.pgen_layout(img, N + 1)
+    assert e.value.code == -1
+    # non-reference flags stored after the header shift the records
+    flags = bytes((M + 7) // 8)
+    img3 = img[:11] + bytes([0xC0]) + flags + img[12:]
+    assert capi.pgen_layout(img3)["offset"] == 12 + (M + 7) // 8
+    # mode 0x03: hard calls and 2 N bytes of dosages per record
+    rec = np.concatenate([case.packed[:, :bps], np.zeros((M, 2 * N), np.uint8)], axis=1)
+    img_d = img[:2] + bytes([3]) + img[3:12] + rec.tobytes()
+    assert capi.pgen_layout(img_d)["record_bytes"] == bps + 2 * N
+    # PLINK 1 rows under a .pgen name: counts from the size and the .psam
+    img1 = bytes([0x6C, 0x1B, 0x01]) + case.packed[:, :bps].tobytes()
+    assert capi.pgen_layout(img1, N) == {"mode": 1, "nsnps": M, "nsamples": N, "offset": 3, "record_bytes": bps}
+    for bad, code in [(img1, -1),                                    # mode 1 without a sample count
+                      (img[:-1], -4),                                # truncated
+                      (img[:2] + bytes([0x10]) + img[3:], -4),       # variable-width
+                      (img[:11] + bytes([1]) + img[12:], -4),        # control byte of a variable-width file
+                      (b"\x00\x00\x02" + img[3:], -4)]:           # magic
+        with pytest.raises(capi.PcaoneError) as e:
+            capi.pgen_layout(bad)
+        assert e.value.code == code

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from oracle import halko as H
-from tests.cases import align_signs, golden_cases
+from tests.cases import align_signs, golden_cases, pgen_cases
 
 CASES = golden_cases()
 IDS = [c.name for c in CASES]
@@ -173,6 +173,32 @@ def test_out_of_core_rsvd_matches_reference(case):
     o = case.opts
     packed = case.packed[case.ref["perm"]] if "perm" in case.ref else case.packed
     d = H.OracleData(packed, case.nsamples, emu=o.emu, perm=False, seed=o.seed, bands=o.bands, rand=o.rand,
+                     svd_t=o.svd, omega0=case.ref["Omg0"])
+    op = H.run_pca_with_halko(d, o.k, o.oversamples, maxp=o.maxp, tol=o.tol, maxiter=o.maxiter, tolem=o.tolem)
+    if o.emu:
+        assert op.em_iters == int(case.ref["meta"][2])
+    S = case.ref["S"]
+    assert np.max(np.abs(op.S ** 2 - S ** 2) / S ** 2) < 1e-9
+    assert np.max(np.abs(align_signs(op.U, case.ref["U"]) - case.ref["U"])) < 1e-8
+    assert np.max(np.abs(align_signs(op.V, case.ref["V"]) - case.ref["V"])) < 1e-8
+
+
+# ---- PLINK2 .pgen input (the reference's FilePgen through its pgenlib) -----
+PGEN = pgen_cases()
+
+
+@pytest.mark.parametrize("case", PGEN, ids=[c.name for c in PGEN])
+def test_pgen_hard_calls_as_plink1_codes(case):
+    """The hard calls translated to PLINK 1 codes give the reference's PGEN
+    allele frequencies and decoded, centred matrix bit for bit, and its PCs to
+    rounding."""
+    packed = H.genovec_to_bed(case.packed, case.nsamples)
+    F = H.allele_freq(H.bed_counts(packed, case.nsamples))
+    assert np.array_equal(F, case.ref["F"])
+    G0, _ = H.decode_centered(packed, case.nsamples, F)
+    assert hashlib.sha256(np.asfortranarray(G0).tobytes(order="F")).digest() == bytes(case.ref["G0_sha256"])
+    o = case.opts
+    d = H.OracleData(packed, case.nsamples, emu=o.emu, perm=o.perm, seed=o.seed, bands=o.bands, rand=o.rand,
                      svd_t=o.svd, omega0=case.ref["Omg0"])
     op = H.run_pca_with_halko(d, o.k, o.oversamples, maxp=o.maxp, tol=o.tol, maxiter=o.maxiter, tolem=o.tolem)
     if o.emu:
