@@ -40,7 +40,8 @@ def test_adapter_compiles_against_the_reference_headers(tmp_path):
                     'void use2(pcaone_gpu_ctx* c, const double* x, double* y) { perform_op_gpu(c, x, y, true); }\n')
     obj = tmp_path / "use.o"
     cmd = ["g++", "-std=c++17", "-DWITH_GB300", "-w", "-c", str(unit), "-o", str(obj), f"-I{tmp_path}",
-           f"-I{os.path.join(REPO, 'include')}", f"-I{tree}/src", f"-I{tree}/external", f"-I{tree}/external/zstd/lib"]
+           f"-I{os.path.join(REPO, 'include')}", f"-I{tree}/src", f"-I{tree}/external", f"-I{tree}/external/zstd/lib",
+           f"-I{tree}/external/pgenlib"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     # every pcaone_gpu_* symbol the adapter needs is exported by the library
