@@ -1,20 +1,21 @@
 // Arnoldi matvec y = X X^T x that allocates no device memory.
 //
-// Some callers cannot call cudaMalloc: code that is being recorded into a CUDA
-// graph (stream capture forbids allocation calls), hosts whose memory manager
-// owns every byte of the device and hands out fixed arenas, and latency-bound
+// Some callers cannot allocate device memory themselves: hosts whose own
+// allocator or memory arena owns every byte of the device, and latency-bound
 // loops that cannot afford the device-wide synchronisation cudaMalloc and
 // cudaFree may imply.  For them this file provides a variant of the matvec of
-// dense64.cu that runs on the caller's own device buffers and keeps its one
-// intermediate, t = X^T x (one double per SNP), in the file-scope array
-// below.  That array is part of the module: every GPU that loads the library
-// holds its 16 MiB from module load until process exit.
+// dense64.cu that runs on the caller's own device buffers and keeps its
+// intermediates, t = X^T x (one double per SNP) and the per-split partial sums
+// of y, in the file-scope array below.  That array is part of the module:
+// every GPU that loads the library holds its 16 MiB from module load until
+// process exit.
 //
 // The array is shared by every call on a device and keeps the last call's
 // contents; the first kernel overwrites every entry it uses, so nothing has to
 // be cleared between calls.  Calls whose work overlaps on the GPU (for example
 // from two streams at once) race on the array and must be serialised by the
 // caller.
+#include <algorithm>
 #include <mutex>
 
 #include "../../include/pcaone_gpu.h"
@@ -89,19 +90,37 @@ __global__ void k_static_t(const uint8_t* __restrict__ bed, uint64_t pitch, int6
   }
 }
 
-// y_i = sum_j (g_ij - f_j) t[j] over the SNPs where sample i is observed (one
-// thread per sample; neighbouring threads read neighbouring bytes of a row).
+// y_i = sum_j (g_ij - f_j) t[j] over the SNPs where sample i is observed: one
+// thread per sample and SNP range (blockIdx.y of nsplit ranges;
+// neighbouring threads read neighbouring bytes of a row), written to y
+// directly with one range, else to part[split][i] for k_static_reduce.
 __global__ void k_static_y(const uint8_t* __restrict__ bed, uint64_t pitch, int64_t nsnps, int nsamples,
-                           const double* __restrict__ F, const double* __restrict__ t, double* __restrict__ y) {
+                           const double* __restrict__ F, const double* __restrict__ t, int nsplit,
+                           double* __restrict__ part, double* __restrict__ y) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nsamples) return;
+  const int64_t per = (nsnps + nsplit - 1) / nsplit;
+  const int64_t j0 = (int64_t)blockIdx.y * per;
+  const int64_t j1 = j0 + per < nsnps ? j0 + per : nsnps;
   const int64_t byte = i >> 2;
   const int sh = 2 * (i & 3);
   double acc = 0.0;
-  for (int64_t j = 0; j < nsnps; ++j) {
+  for (int64_t j = j0; j < j1; ++j) {
     const uint32_t c = (bed[j * pitch + byte] >> sh) & 3u;
     if (c != 1u) acc = fma(geno_half(c) - F[j], t[j], acc);
   }
+  if (nsplit == 1)
+    y[i] = acc;
+  else
+    part[(size_t)blockIdx.y * nsamples + i] = acc;
+}
+
+// y_i = sum over the ranges of part[s][i], in range order (deterministic)
+__global__ void k_static_reduce(const double* __restrict__ part, int nsplit, int nsamples, double* __restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsamples) return;
+  double acc = 0.0;
+  for (int s = 0; s < nsplit; ++s) acc += part[(size_t)s * nsamples + i];
   y[i] = acc;
 }
 
@@ -125,7 +144,20 @@ extern "C" int pcaone_gpu_matvec_static(const uint8_t* d_packed, uint64_t row_pi
   const int N = (int)nsamples;
   k_static_t<<<(unsigned)((M * 32 + 255) / 256), 256, 0, s>>>(d_packed, row_pitch, M, N, d_F, standardize, d_x, t);
   if (cudaGetLastError() != cudaSuccess) return PCAONE_E_CUDA;
-  k_static_y<<<(unsigned)((N + 127) / 128), 128, 0, s>>>(d_packed, row_pitch, M, N, d_F, t, d_y);
+  // SNP ranges for the y pass: enough thread blocks to fill the GPU (about
+  // 1216), ranges of at least 32 SNPs, partial sums in the scratch behind t
+  const int xblocks = (N + 127) / 128;
+  const int64_t room = (kMaxSnps - M) / N;  // partial rows that fit behind t
+  int64_t nsplit = std::max<int64_t>(1, (1216 + xblocks - 1) / xblocks);
+  nsplit = std::min<int64_t>(nsplit, std::max<int64_t>(1, (M + 31) / 32));
+  nsplit = std::min<int64_t>(nsplit, std::max<int64_t>(1, std::min<int64_t>(room, 65535)));
+  double* part = t + M;
+  k_static_y<<<dim3((unsigned)xblocks, (unsigned)nsplit), 128, 0, s>>>(d_packed, row_pitch, M, N, d_F, t, (int)nsplit,
+                                                                       part, d_y);
   if (cudaGetLastError() != cudaSuccess) return PCAONE_E_CUDA;
+  if (nsplit > 1) {
+    k_static_reduce<<<(unsigned)xblocks, 128, 0, s>>>(part, (int)nsplit, N, d_y);
+    if (cudaGetLastError() != cudaSuccess) return PCAONE_E_CUDA;
+  }
   return PCAONE_OK;
 }

@@ -1,9 +1,9 @@
 """The matvec entry point that allocates no device memory.
 
-Callers that cannot call cudaMalloc (code recorded into a CUDA graph, hosts
-whose memory manager owns all device memory, loops that cannot afford an
+Callers that cannot allocate device memory themselves (hosts whose own
+allocator or arena owns all device memory, loops that cannot afford an
 allocation's synchronisation) use pcaone_gpu_matvec_static on their own device
-buffers; its one intermediate lives in a static device array shared by every
+buffers; its intermediates live in a static device array shared by every
 call.  This file is collected last so that a failure here comes after every
 other test has run.
 """
@@ -54,6 +54,15 @@ def test_static_matvec_matches_context_matvec_twice():
     d.standardize_E()
     yr = H.arnoldi_matvec(d, xs[1])
     assert np.linalg.norm(y - yr) / np.linalg.norm(yr) < REL_TOL
+    # rows at a wider pitch than the .bed body (padding bytes hold garbage)
+    wide = np.full((m, case.packed.shape[1] + 13), 0xA5, dtype=np.uint8)
+    wide[:, : case.packed.shape[1]] = case.packed
+    d_wide = torch.from_numpy(wide).to(dev)
+    rc = lib.pcaone_gpu_matvec_static(d_wide.data_ptr(), wide.shape[1], m, n, d_F.data_ptr(), 1, d_x.data_ptr(),
+                                      d_y.data_ptr(), stream.cuda_stream)
+    assert rc == 0
+    stream.synchronize()
+    assert np.linalg.norm(d_y.cpu().numpy() - refs[1]) / np.linalg.norm(refs[1]) < REL_TOL
     # sizes beyond the static array are rejected before any GPU work
     rc = lib.pcaone_gpu_matvec_static(d_bed.data_ptr(), case.packed.shape[1], (1 << 21) + 1, n, d_F.data_ptr(), 1,
                                       d_x.data_ptr(), d_y.data_ptr(), stream.cuda_stream)
