@@ -163,6 +163,15 @@ unsigned long long pcaone_gpu_launch_count(void);
  * tensor memory and flags the error, and the call returns PCAONE_E_CUDA; the
  * context stays usable. */
 int pcaone_gpu_set_wait_limit(pcaone_gpu_ctx* ctx, long long cycles);
+/* No counterpart in the reference: how the G-shaped tensor-core products
+ * (X_w * Omega, and X_w^T * G on the sample-major copy of the rows) are
+ * launched.  0: one CTA per (row tile, K chunk) item; 1: only as many CTAs as
+ * stay resident (two per SM where the plan pairs), each taking items in turn;
+ * 2 (the default): 1 for the exact forms' products, 0 in the FP8 form's E4M3
+ * epochs (the faster of the two for each on 200,000-sample windows).  Each
+ * item accumulates the same MMAs in the same order in every form, so results
+ * are identical bit for bit. */
+int pcaone_gpu_set_product_form(pcaone_gpu_ctx* ctx, int form);
 
 /* ---- data: replaces FileBed::read_all (src/FilePlink.cpp:26-120) --------- */
 /* packed: the .bed body after the 3 magic bytes, nsnps rows of (nsamples+3)/4

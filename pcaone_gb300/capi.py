@@ -34,6 +34,7 @@ EXPORTS = [
     "pcaone_gpu_mlp_stats", "pcaone_gpu_mlp_forward_backward", "pcaone_gpu_load_dense",
     "pcaone_gpu_load_binary_file_image", "pcaone_gpu_load_synthetic_dense", "pcaone_gpu_project",
     "pcaone_gpu_random_omega", "pcaone_gpu_shuffle_order", "pcaone_gpu_set_wait_limit",
+    "pcaone_gpu_set_product_form",
     "pcaone_gpu_load_bed_stream", "pcaone_gpu_load_bed_file_image_stream", "pcaone_gpu_stream_plan",
     "pcaone_gpu_stream_info", "pcaone_gpu_ooc_order", "pcaone_gpu_load_pgen_genovecs",
     "pcaone_gpu_load_pgen_file_image", "pcaone_gpu_pgen_layout",
@@ -117,6 +118,7 @@ def load(path: str = LIBPATH) -> ctypes.CDLL:
     lib.pcaone_gpu_random_omega.argtypes = [c_int, c_int, c_uint64, c_uint32, c_void_p]
     lib.pcaone_gpu_shuffle_order.argtypes = [c_uint64, c_void_p]
     lib.pcaone_gpu_set_wait_limit.argtypes = [c_void_p, ctypes.c_longlong]
+    lib.pcaone_gpu_set_product_form.argtypes = [c_void_p, c_int]
     lib.pcaone_gpu_load_bed_stream.argtypes = [c_void_p, c_void_p, c_uint64, c_uint32, c_uint64, c_uint32]
     lib.pcaone_gpu_load_bed_file_image_stream.argtypes = [c_void_p, c_void_p, c_uint64, c_uint64, c_uint32,
                                                           c_uint64, c_uint32]
@@ -443,6 +445,11 @@ class Context:
 
     def set_wait_limit(self, cycles: int):
         self._check(self.lib.pcaone_gpu_set_wait_limit(self.h, int(cycles)))
+
+    def set_product_form(self, form: int):
+        """G-shaped product launches: 0 one CTA per (tile, chunk) item, 1 resident CTAs
+        taking items in turn, 2 (default) resident CTAs except in the E4M3 epochs."""
+        self._check(self.lib.pcaone_gpu_set_product_form(self.h, int(form)))
 
     def set_profiling(self, on: bool):
         self._check(self.lib.pcaone_gpu_set_profiling(self.h, int(on)))

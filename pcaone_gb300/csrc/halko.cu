@@ -171,6 +171,10 @@ struct Context {
   bool fp8_now = false;   // the current epoch runs the E4M3 products
   int w_mode = -1;        // slices and format of the W slices now held (S * 4 + format)
   long long wait_cycles = 0;  // limit of the tensor-core pipeline waits (0: the kernels' default)
+  // launch form of the G-shaped products (pcaone_gpu_set_product_form):
+  // 0 one CTA per (tile, chunk) item, 1 resident CTAs taking items in turn,
+  // 2 resident CTAs except in the E4M3 epochs
+  int product_form = 2;
   bool fp64 = false;   // FP64-grade form: the QR and small-SVD kernels in plain FP64 too
 
   // optional per-kernel CUDA-event timing of the window products
@@ -1222,6 +1226,9 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
   ga.dense = c.dense ? 1 : 0;
   ga.wait_cycles = c.wait_cycles;
   ga.fp8 = fp8 ? 1 : 0;
+  // resident CTAs: 3-8% faster on the 27-bit BF16 products of the
+  // 200,000-sample windows, 3-4% slower on their E4M3 products
+  ga.persist = c.product_form == 1 || (c.product_form == 2 && !fp8) ? 1 : 0;
   mark(fp8 ? 2 : 0);
   tc::launch_g(fp8 ? c.map_bed_g8 : c.map_bed_g, fp8 ? c.map_w8 : c.map_w, ga, c.stream);
   close_mark();
@@ -1328,6 +1335,7 @@ static void window_product_tc(Context& c, int64_t pos0, int64_t n, double* Hx) {
     ta.dense = 0;
     ta.wait_cycles = c.wait_cycles;
     ta.fp8 = fp8 ? 1 : 0;
+    ta.persist = ga.persist;
     mark(fp8 ? 3 : 1);
     tc::launch_g(fp8 ? c.map_bt8 : c.map_bt, fp8 ? c.map_gt8 : c.map_gt, ta, c.stream);
     close_mark();
@@ -2000,6 +2008,13 @@ int pcaone_gpu_set_wait_limit(pcaone_gpu_ctx* ctx, long long cycles) {
   return guarded(ctx, [&](Context& c) {
     if (cycles < 0) throw Error(PCAONE_E_ARG, "negative wait limit");
     c.wait_cycles = cycles;
+  });
+}
+
+int pcaone_gpu_set_product_form(pcaone_gpu_ctx* ctx, int form) {
+  return guarded(ctx, [&](Context& c) {
+    if (form < 0 || form > 2) throw Error(PCAONE_E_ARG, "product form must be 0, 1 or 2");
+    c.product_form = form;
   });
 }
 

@@ -517,6 +517,18 @@ __device__ __forceinline__ void store_i64x8(long long* dst, const long long* v) 
 // ---------------------------------------------------------------------------
 // G product
 // ---------------------------------------------------------------------------
+// Work items: (row tile of 128 positions, K chunk) pairs q = tile + chunk *
+// ntile; CTA b takes items b, b + gridDim.x, ...  With one CTA per item the
+// grid is the item count; a persistent launch (GArgs.persist) keeps the
+// resident CTAs (two per SM where the plan pairs) and lets each take items in
+// turn, paying TMEM allocation, barrier and table set-up once.  The producer
+// runs ahead into a CTA's next item while its decoder warps read the last
+// item's accumulators; those warps then decode the next item, and their arrival
+// on its first stage's dec barrier orders their TMEM reads before the MMA that
+// overwrites the accumulators.  Every item accumulates the same MMAs, in the
+// same order, from a zeroed accumulator, so its partial sums do not depend on
+// the launch form.  acc_bar completes once per item (the commit after its last
+// MMA); done_bar once, after the MMA thread's last MMA, before TMEM is freed.
 template <int kMode>
 __global__ void __launch_bounds__(kThreads, 2)
     k_tc_g(const __grid_constant__ CUtensorMap map_bed, const __grid_constant__ CUtensorMap map_w, GArgs a) {
@@ -528,7 +540,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   constexpr bool kASmem = kDense;  // A operand in shared memory (else TMEM)
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  __shared__ uint64_t full_bar[kMaxStages], dec_bar[kMaxStages], empty_bar[kMaxStages], acc_bar;
+  __shared__ uint64_t full_bar[kMaxStages], dec_bar[kMaxStages], empty_bar[kMaxStages], acc_bar, done_bar;
   __shared__ uint32_t tmem_sh;
   __shared__ volatile int abort_sh;
   __shared__ float unit[3 * 112];
@@ -536,11 +548,11 @@ __global__ void __launch_bounds__(kThreads, 2)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int LP = a.LP, S = a.nslice;
   const SmemLayout lay = layout_for(LP, S, kTileBytes, kASmem);
-  const int row0 = blockIdx.x * 128;
   if (!kDense && !kFp8) lut_init(lut, tid, kThreads);
-  const int kbeg = blockIdx.y * a.chunk;
-  const int kend = min(kbeg + a.chunk, a.npad);
-  const int nk = (kend - kbeg + kK - 1) / kK;
+  const int ntile = (a.nsnp + 127) / 128;
+  const int nitems = ntile * a.nchunks;
+  // K steps of the item whose chunk starts at kbeg
+  auto steps_of = [&](int kbeg) { return (min(kbeg + a.chunk, a.npad) - kbeg + kK - 1) / kK; };
   const int nst = a.nstages;
   const int ncat = S * LP;  // slices concatenated along N
   const long long wlim = a.wait_cycles > 0 ? a.wait_cycles : kTimeoutCycles;
@@ -553,6 +565,7 @@ __global__ void __launch_bounds__(kThreads, 2)
       mbar_init(&empty_bar[s], 1);
     }
     mbar_init(&acc_bar, 1);
+    mbar_init(&done_bar, 1);
     fence_mbar_init();
   }
   if (kDense)
@@ -571,24 +584,27 @@ __global__ void __launch_bounds__(kThreads, 2)
     if (lane == 0) {
       const uint32_t tx_bytes = kTileBytes + (uint32_t)(ncat * 128);
       const int kdiv = kDense ? 0 : 2;  // inner TMA coordinate: samples, or packed bytes
-      int issued = 0;
-      const int prow = (int)(a.pos0 + row0);
       const int kofs = (int)a.kofs;
-      for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
-        tma_prefetch_2d(&map_bed, (kofs + kbeg + kb * kK) >> kdiv, prow);
-      int st = 0, round = 0;
-      for (int kb = 0; kb < nk; ++kb) {
-        const int k0 = kbeg + kb * kK;
-        if (kb + kPrefetchSteps < nk) tma_prefetch_2d(&map_bed, (kofs + k0 + kPrefetchSteps * kK) >> kdiv, prow);
-        if (round > 0 && !role_wait(&empty_bar[st], (uint32_t)(round - 1) & 1u, &abort_sh, wlim)) break;
-        uint8_t* base = smem + st * lay.stage_bytes;
-        mbar_expect_tx(&full_bar[st], tx_bytes);
-        tma_load_2d(base + lay.p, &map_bed, (kofs + k0) >> kdiv, prow, &full_bar[st]);
-        for (int s = 0; s < S; ++s) tma_load_2d(base + lay.b + s * LP * 128, &map_w, k0, s * LP, &full_bar[st]);
-        issued = kb + 1;
-        if (++st == nst) {
-          st = 0;
-          ++round;
+      int issued = 0, st = 0, round = 0;
+      for (int q = blockIdx.x; q < nitems && !abort_sh; q += gridDim.x) {
+        const int row0 = (q % ntile) * 128, kbeg = (q / ntile) * a.chunk;
+        const int nk = steps_of(kbeg);
+        const int prow = (int)(a.pos0 + row0);
+        for (int kb = 0; kb < nk && kb < kPrefetchSteps; ++kb)
+          tma_prefetch_2d(&map_bed, (kofs + kbeg + kb * kK) >> kdiv, prow);
+        for (int kb = 0; kb < nk; ++kb) {
+          const int k0 = kbeg + kb * kK;
+          if (kb + kPrefetchSteps < nk) tma_prefetch_2d(&map_bed, (kofs + k0 + kPrefetchSteps * kK) >> kdiv, prow);
+          if (round > 0 && !role_wait(&empty_bar[st], (uint32_t)(round - 1) & 1u, &abort_sh, wlim)) break;
+          uint8_t* base = smem + st * lay.stage_bytes;
+          mbar_expect_tx(&full_bar[st], tx_bytes);
+          tma_load_2d(base + lay.p, &map_bed, (kofs + k0) >> kdiv, prow, &full_bar[st]);
+          for (int s = 0; s < S; ++s) tma_load_2d(base + lay.b + s * LP * 128, &map_w, k0, s * LP, &full_bar[st]);
+          ++issued;
+          if (++st == nst) {
+            st = 0;
+            ++round;
+          }
         }
       }
       if (abort_sh) drain_copies(full_bar, issued, nst);
@@ -602,19 +618,27 @@ __global__ void __launch_bounds__(kThreads, 2)
       const uint64_t a_desc0 = desc_sw128(smem_u32(smem + lay.a));
       const uint64_t stage_units = lay.stage_bytes >> 4;
       int st = 0, round = 0;
-      for (int kb = 0; kb < nk; ++kb) {
-        if (!role_wait(&dec_bar[st], (uint32_t)round & 1u, &abort_sh, wlim)) break;
-        tc_fence_after();
-        const uint64_t so = (uint64_t)st * stage_units;
-        mma_stage<kMode, kASmem>(tmem, tmem + a_col0 + (uint32_t)st * 32u, a_desc0 + so, b_desc0 + so, ncat, id0, id1,
-                                 kb == 0);
-        mma_commit(&empty_bar[st]);
-        if (++st == nst) {
-          st = 0;
-          ++round;
+      bool ok = true;
+      for (int q = blockIdx.x; q < nitems && ok; q += gridDim.x) {
+        const int nk = steps_of((q / ntile) * a.chunk);
+        for (int kb = 0; kb < nk; ++kb) {
+          if (!role_wait(&dec_bar[st], (uint32_t)round & 1u, &abort_sh, wlim)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint64_t so = (uint64_t)st * stage_units;
+          mma_stage<kMode, kASmem>(tmem, tmem + a_col0 + (uint32_t)st * 32u, a_desc0 + so, b_desc0 + so, ncat, id0,
+                                   id1, kb == 0);
+          mma_commit(&empty_bar[st]);
+          if (++st == nst) {
+            st = 0;
+            ++round;
+          }
         }
+        if (ok) mma_commit(&acc_bar);  // the item's accumulators are complete
       }
-      mma_commit(&acc_bar);  // arrives once every MMA above has completed
+      mma_commit(&done_bar);  // arrives once every MMA above has completed
     }
   } else if (warp >= kDecodeWarp0) {
     // ---- decoders: TMEM lane quarter q4 = warp % 4 (row r = SNP 32*q4 + lane of
@@ -624,79 +648,83 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int q4 = warp & 3, ch = (warp - kDecodeWarp0) >> 2;
     const int r = q4 * 32 + lane;
     const uint32_t lane_off = (uint32_t)(q4 * 32) << 16;
-    int st = 0, round = 0;
-    for (int kb = 0; kb < nk; ++kb) {
-      if (!role_wait(&full_bar[st], (uint32_t)round & 1u, &abort_sh, wlim)) break;
-      uint8_t* base = smem + st * lay.stage_bytes;
-      uint32_t wd[16];
-      if (kDense) {
-        // row r holds 8 chunks of 16 B (8 FP16 values each), chunk c stored at
-        // position c ^ (r & 7) by the 128-byte swizzle; this thread takes
-        // chunks 4ch .. 4ch+3 (samples 32ch .. 32ch+31)
+    int st = 0, round = 0, li = 0;
+    for (int q = blockIdx.x; q < nitems && !abort_sh; q += gridDim.x, ++li) {
+      const int row0 = (q % ntile) * 128, chunk = q / ntile;
+      const int nk = steps_of(chunk * a.chunk);
+      for (int kb = 0; kb < nk; ++kb) {
+        // the warp leaves together: the TMEM stores and loads below are warp-wide
+        if (!__all_sync(0xffffffffu, role_wait(&full_bar[st], (uint32_t)round & 1u, &abort_sh, wlim))) break;
+        uint8_t* base = smem + st * lay.stage_bytes;
+        uint32_t wd[16];
+        if (kDense) {
+          // row r holds 8 chunks of 16 B (8 FP16 values each), chunk c stored at
+          // position c ^ (r & 7) by the 128-byte swizzle; this thread takes
+          // chunks 4ch .. 4ch+3 (samples 32ch .. 32ch+31)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int cpos = (ch * 4 + q) ^ (r & 7);
-          const uint4 v = *reinterpret_cast<const uint4*>(base + lay.p + r * 128 + cpos * 16);
-          wd[4 * q] = v.x;
-          wd[4 * q + 1] = v.y;
-          wd[4 * q + 2] = v.z;
-          wd[4 * q + 3] = v.w;
-        }
-      } else if (kFp8) {
-        // samples 64ch .. 64ch+63 of the step: 16 packed bytes, one per word
-        const uint4 pk = *reinterpret_cast<const uint4*>(base + lay.p + r * 32 + ch * 16);
-        e4m3_x16(pk.x, wd);
-        e4m3_x16(pk.y, wd + 4);
-        e4m3_x16(pk.z, wd + 8);
-        e4m3_x16(pk.w, wd + 12);
-      } else {
-        const uint2 pk = *reinterpret_cast<const uint2*>(base + lay.p + r * 16 + ch * 8);
-        const uint32_t* lut_l = lut + lane;
+          for (int qq = 0; qq < 4; ++qq) {
+            const int cpos = (ch * 4 + qq) ^ (r & 7);
+            const uint4 v = *reinterpret_cast<const uint4*>(base + lay.p + r * 128 + cpos * 16);
+            wd[4 * qq] = v.x;
+            wd[4 * qq + 1] = v.y;
+            wd[4 * qq + 2] = v.z;
+            wd[4 * qq + 3] = v.w;
+          }
+        } else if (kFp8) {
+          // samples 64ch .. 64ch+63 of the step: 16 packed bytes, one per word
+          const uint4 pk = *reinterpret_cast<const uint4*>(base + lay.p + r * 32 + ch * 16);
+          e4m3_x16(pk.x, wd);
+          e4m3_x16(pk.y, wd + 4);
+          e4m3_x16(pk.z, wd + 8);
+          e4m3_x16(pk.w, wd + 12);
+        } else {
+          const uint2 pk = *reinterpret_cast<const uint2*>(base + lay.p + r * 16 + ch * 8);
+          const uint32_t* lut_l = lut + lane;
 #pragma unroll
-        for (int e = 0; e < 16; ++e) {
-          const uint32_t w32 = e < 8 ? pk.x : pk.y;
-          const int sh = 4 * (e & 7);
-          wd[e] = lut_l[((w32 >> sh) & 15u) << 5];
+          for (int e = 0; e < 16; ++e) {
+            const uint32_t w32 = e < 8 ? pk.x : pk.y;
+            const int sh = 4 * (e & 7);
+            wd[e] = lut_l[((w32 >> sh) & 15u) << 5];
+          }
+        }
+        if constexpr (kASmem) {
+          st_a_row(base + lay.a, r, ch, wd);
+          fence_proxy_async_smem();
+        } else {
+          tmem_st16(tmem + lane_off + a_col0 + st * 32 + ch * 16, wd);
+          tmem_wait_st();
+          tc_fence_before();
+        }
+        mbar_arrive(&dec_bar[st]);
+        if (++st == nst) {
+          st = 0;
+          ++round;
         }
       }
-      if constexpr (kASmem) {
-        st_a_row(base + lay.a, r, ch, wd);
-        fence_proxy_async_smem();
-      } else {
-        tmem_st16(tmem + lane_off + a_col0 + st * 32 + ch * 16, wd);
-        tmem_wait_st();
-        tc_fence_before();
-      }
-      mbar_arrive(&dec_bar[st]);
-      if (++st == nst) {
-        st = 0;
-        ++round;
-      }
-    }
-    // ---- epilogue ----
-    const bool ok = nk > 0 && role_wait(&acc_bar, 0u, &abort_sh, wlim);
-    tc_fence_after();
-    const int quarter = warp & 3, chalf = (warp - kDecodeWarp0) >> 2;
-    const int j = row0 + quarter * 32 + lane;
-    const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
-    if (!abort_sh) {
+      // ---- epilogue of the item ----
+      if (!__all_sync(0xffffffffu, !abort_sh && role_wait(&acc_bar, (uint32_t)li & 1u, &abort_sh, wlim))) break;
+      tc_fence_after();
+      const int quarter = warp & 3, chalf = (warp - kDecodeWarp0) >> 2;
+      const int j = row0 + quarter * 32 + lane;
+      const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+      const bool any = nk > 0;  // an item without K steps holds zeros
       for (int c0 = chalf * (LP / 2); c0 < (chalf + 1) * (LP / 2); c0 += 8) {
         if constexpr (kDense) {
           // FP16 values: slice sums times their power-of-two units (FP32 FMAs)
           float sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-          if (ok) store_slice_sum(lane_base, c0, LP, S, unit, sum);
-          if (j < a.nsnp) store_f32x8(reinterpret_cast<float*>(a.part) + ((size_t)blockIdx.y * a.nsnp + j) * LP + c0, sum);
+          if (any) store_slice_sum(lane_base, c0, LP, S, unit, sum);
+          if (j < a.nsnp) store_f32x8(reinterpret_cast<float*>(a.part) + ((size_t)chunk * a.nsnp + j) * LP + c0, sum);
         } else {
           // genotypes: every slice sum is an integer below 2^23, combined
           // exactly in int64 in units of the last slice
-          const size_t off = ((size_t)blockIdx.y * a.nsnp + j) * LP + c0;
+          const size_t off = ((size_t)chunk * a.nsnp + j) * LP + c0;
           if (S <= kIntSlices) {
             long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            if (ok) combine_slices_exact(lane_base, c0, LP, S, acc, kFp8 ? kDigitBits8 : kDigitBits);
+            if (any) combine_slices_exact(lane_base, c0, LP, S, acc, kFp8 ? kDigitBits8 : kDigitBits);
             if (j < a.nsnp) store_i64x8(reinterpret_cast<long long*>(a.part) + off, acc);
           } else {
             double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            if (ok) combine_slices_fp64(lane_base, c0, LP, S, acc);
+            if (any) combine_slices_fp64(lane_base, c0, LP, S, acc);
             if (j < a.nsnp) store_f64x8(reinterpret_cast<double*>(a.part) + off, acc);
           }
         }
@@ -706,7 +734,14 @@ __global__ void __launch_bounds__(kThreads, 2)
   tc_fence_before();
   __syncthreads();
   if (tid == 0 && abort_sh) *a.err = 1;
-  cta_release(acc_bar, abort_sh, warp, lane, tmem, (uint32_t)a.tmem_cols);
+  // the MMA thread's last commit may still be on its way after the last
+  // epilogue (or an abort): wait for it (bounded) before freeing TMEM
+  if (warp == 0) {
+    if (lane == 0) mbar_wait(&done_bar, 0u);
+    __syncwarp();
+    tc_fence_after();
+    tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1366,8 +1401,9 @@ void launch_g_t(const CUtensorMap& map_bed, const CUtensorMap& map_w, const GArg
     PCAONE_CUDA(cudaFuncSetAttribute(k_tc_g<kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize, 214 * 1024));
     attr = true;
   }
-  dim3 grid((a.nsnp + 127) / 128, a.nchunks);
-  k_tc_g<kMode><<<grid, kThreads, smem, s>>>(map_bed, map_w, a);
+  const int nitems = (a.nsnp + 127) / 128 * a.nchunks;
+  const int grid = a.persist ? std::min(nitems, cta_slots(a.LP, a.nslice, a.dense != 0)) : nitems;
+  k_tc_g<kMode><<<std::max(grid, 1), kThreads, smem, s>>>(map_bed, map_w, a);
 }
 
 template <int kMode>

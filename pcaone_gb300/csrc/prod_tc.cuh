@@ -30,6 +30,8 @@ struct GArgs {
   int dense;              // 1: FP16 values (FileBinary input) instead of packed codes
   long long wait_cycles;  // limit of the pipeline waits in SM cycles (0: about 2 s)
   int fp8;                // 1: E4M3 operands (128 samples per pipeline stage)
+  int persist;            // 1: as many CTAs as stay resident, each taking (tile, chunk) items in
+                          // turn; 0: one CTA per item.  The partial sums are the same.
 };
 
 // Sample-major copy of the packed rows for the H products (k_tc_g then runs
