@@ -219,6 +219,20 @@ int pcaone_gpu_load_synthetic(pcaone_gpu_ctx* ctx, uint64_t nsnps, uint32_t nsam
 /* Copies the resident packed genotypes back (nsnps rows of (nsamples+3)/4
  * bytes, the .bed body). */
 int pcaone_gpu_get_bed(pcaone_gpu_ctx* ctx, uint8_t* packed);
+/* --maf: Data::filter_snps_resize_F (src/Data.cpp:88-105), called by
+ * FileBed / FilePgen::read_all (src/FilePlink.cpp:61, src/FilePgen.cpp:53).
+ * Keeps the SNPs whose minor allele frequency min(F, 1 - F) exceeds maf, in
+ * file order; the context then holds only those rows (counts, F, the shuffle
+ * and the products see the filtered matrix; pcaone_gpu_op_init again before
+ * a run).  0 < maf < 0.5 (src/Cmd.cpp:222); genotype input held in HBM only
+ * (the reference has no filter out of core, src/Cmd.cpp:223, nor for
+ * FileBinary input).  No SNP left: PCAONE_E_ARG.  nkept (may be NULL): the
+ * new SNP count. */
+int pcaone_gpu_filter_maf(pcaone_gpu_ctx* ctx, double maf, uint64_t* nkept);
+/* Data::keepSNPs (src/Data.hpp:56): for each resident SNP its row in the
+ * loaded file, composed over repeated filters (idx: nsnps entries); the
+ * identity when no filter was applied since the load. */
+int pcaone_gpu_kept_snps(pcaone_gpu_ctx* ctx, int64_t* idx);
 
 /* ---- PLINK2 input: replaces FilePgen (src/FilePgen.hpp, FilePgen.cpp:27-86) -
  * Hard calls only: ALT allele counts 0/1/2 (3 = missing), the values FilePgen

@@ -155,6 +155,13 @@ def allele_freq(counts: np.ndarray) -> np.ndarray:
     return np.where(c == 0, 0.0, f)
 
 
+def maf_keep(F: np.ndarray, maf: float) -> np.ndarray:
+    """Data::filter_snps_resize_F (src/Data.cpp:88-105): the SNPs whose minor
+    allele frequency (MAF macro, src/Common.hpp:26) exceeds maf, in file order."""
+    F = np.asarray(F, dtype=np.float64)
+    return np.flatnonzero(np.where(F > 0.5, 1.0 - F, F) > maf).astype(np.int64)
+
+
 def decode_centered(packed: np.ndarray, nsamples: int, F: np.ndarray):
     """X (N x M) = BED2GENO[code] - F_j with missing entries set to 0 (mean
     imputation), and the missing mask C (M x N, bool); src/FilePlink.cpp:71-110."""

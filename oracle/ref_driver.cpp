@@ -150,6 +150,11 @@ int main(int argc, char** argv) {
   const auto t1 = clk::now();
   if (timing) dump_g0 = false;
   if ((params.file_t == FileType::PLINK || params.file_t == FileType::PGEN) && !timing) dump1(outdir, "F", data->F);
+  if (!data->keepSNPs.empty() && !timing) {
+    // --maf: the file rows of the SNPs kept by Data::filter_snps_resize_F
+    std::vector<long long> keep(data->keepSNPs.begin(), data->keepSNPs.end());
+    write_npy(outdir + "/keep.npy", "<i8", keep.data(), 8, {(long long)keep.size()}, false);
+  }
   if (dump_g0) dump(outdir, "G0", data->G);
 
   // operator selection and call sequence of run_pca_with_halko (src/Halko.cpp:271-320)

@@ -37,7 +37,8 @@ EXPORTS = [
     "pcaone_gpu_set_product_form",
     "pcaone_gpu_load_bed_stream", "pcaone_gpu_load_bed_file_image_stream", "pcaone_gpu_stream_plan",
     "pcaone_gpu_stream_info", "pcaone_gpu_ooc_order", "pcaone_gpu_load_pgen_genovecs",
-    "pcaone_gpu_load_pgen_file_image", "pcaone_gpu_pgen_layout",
+    "pcaone_gpu_load_pgen_file_image", "pcaone_gpu_pgen_layout", "pcaone_gpu_filter_maf",
+    "pcaone_gpu_kept_snps",
 ]
 MLP_PARAMS, MLP_INPUTS = 82689, 64
 
@@ -99,6 +100,8 @@ def load(path: str = LIBPATH) -> ctypes.CDLL:
     lib.pcaone_gpu_load_synthetic.argtypes = [c_void_p, c_uint64, c_uint32, c_int, c_void_p, c_void_p, c_void_p,
                                               c_void_p, c_uint64]
     lib.pcaone_gpu_get_bed.argtypes = [c_void_p, c_void_p]
+    lib.pcaone_gpu_filter_maf.argtypes = [c_void_p, ctypes.c_double, c_void_p]
+    lib.pcaone_gpu_kept_snps.argtypes = [c_void_p, c_void_p]
     lib.pcaone_gpu_set_profiling.argtypes = [c_void_p, c_int]
     lib.pcaone_gpu_kernel_stats.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p]
     lib.pcaone_gpu_launch_count.argtypes = []
@@ -344,6 +347,20 @@ class Context:
         """pcaone_gpu_load_bed from a raw host pointer (e.g. pinned memory)."""
         self._check(self.lib.pcaone_gpu_load_bed(self.h, c_void_p(host_ptr), nsnps, nsamples))
         self.nsamples, self.nsnps = int(nsamples), int(nsnps)
+
+    def filter_maf(self, maf: float) -> int:
+        """--maf: keep the SNPs with min(F, 1-F) > maf (Data::filter_snps_resize_F);
+        returns the new SNP count."""
+        n = ctypes.c_uint64(0)
+        self._check(self.lib.pcaone_gpu_filter_maf(self.h, float(maf), ctypes.byref(n)))
+        self.nsnps = int(n.value)
+        return self.nsnps
+
+    def kept_snps(self) -> np.ndarray:
+        """File row of each resident SNP (Data::keepSNPs)."""
+        out = np.empty(self.nsnps, dtype=np.int64)
+        self._check(self.lib.pcaone_gpu_kept_snps(self.h, _ptr(out)))
+        return out
 
     def counts(self):
         cnt = np.empty((self.nsnps, 4), dtype=np.int32)

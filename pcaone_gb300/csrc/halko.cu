@@ -124,6 +124,9 @@ struct Context {
   DBuf<int32_t> perm;
   bool permuted = false;
   std::vector<int32_t> perm_host;
+  // file row of each resident SNP after a MAF filter (Data::keepSNPs,
+  // src/Data.hpp:56); empty: no filter applied since the load
+  std::vector<int64_t> kept;
   int bandsize = 1;
   int64_t blocksize = 0;
   // window scratch
@@ -342,6 +345,8 @@ static void load_common(Context& c, uint64_t nsnps, uint32_t nsamples, bool dens
   c.bk_valid = false;
   c.nnz = -1;
   c.counts_host.clear();
+  c.kept.clear();
+  c.permuted = false;  // the rows are in file order until the next op_init shuffles them
 }
 
 static void finish_load(Context& c) {
@@ -458,6 +463,44 @@ static void load_bed_device(Context& c, const void* src, uint64_t pitch, uint64_
   const size_t bps = ((size_t)nsamples + 3) / 4;
   PCAONE_CUDA(cudaMemcpy2DAsync(c.bed.p, c.stride, src, pitch, bps, nsnps, cudaMemcpyDeviceToDevice, c.stream));
   finish_load(c);
+}
+
+// Data::filter_snps_resize_F (src/Data.cpp:88-105, MAF of src/Common.hpp:26):
+// keep the SNPs whose minor allele frequency exceeds maf, in file order.  The
+// kept rows are gathered into a new buffer and loaded from there, so that
+// counts, F (the same bits, from the same rows), the missing-entry index and
+// every later step see the filtered matrix, as in the reference, whose
+// FileBed::read_all decodes only the kept SNPs (src/FilePlink.cpp:61-72).
+static int64_t filter_maf(Context& c, double maf) {
+  if (!(maf > 0 && maf < 0.5)) throw Error(PCAONE_E_ARG, "--maf has to be between (0, 0.5)");
+  if (c.dense) throw Error(PCAONE_E_ARG, "no MAF filter for dense (FileBinary) input");
+  if (c.streamed) throw Error(PCAONE_E_ARG, "does not support --maf filters for out-of-core mode");
+  std::vector<double> F((size_t)c.M);
+  PCAONE_CUDA(cudaMemcpyAsync(F.data(), c.F.p, F.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  std::vector<int32_t> keep;
+  keep.reserve(F.size());
+  for (int64_t j = 0; j < c.M; ++j) {
+    const double f = F[(size_t)j];
+    if ((f > 0.5 ? 1 - f : f) > maf) keep.push_back((int32_t)j);
+  }
+  const int64_t nk = (int64_t)keep.size();
+  if (nk < 1) throw Error(PCAONE_E_ARG, "no SNPs left after filtering");
+  std::vector<int64_t> prev = c.kept;
+  std::vector<int64_t> kept((size_t)nk);
+  for (int64_t i = 0; i < nk; ++i) kept[(size_t)i] = prev.empty() ? keep[(size_t)i] : prev[(size_t)keep[(size_t)i]];
+  if (nk < c.M) {
+    DBuf<uint8_t> rows;
+    DBuf<int32_t> idx;
+    rows.ensure((size_t)nk * c.stride, c.stream, false);
+    idx.ensure((size_t)nk, c.stream, false);
+    PCAONE_CUDA(cudaMemcpyAsync(idx.p, keep.data(), (size_t)nk * sizeof(int32_t), cudaMemcpyHostToDevice, c.stream));
+    tc::launch_gather_rows(c.bed.p, rows.p, c.stride, idx.p, nk, c.stream);
+    load_bed_device(c, rows.p, (uint64_t)c.stride, (uint64_t)nk, (uint32_t)c.N);
+    PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  }
+  c.kept = std::move(kept);
+  return nk;
 }
 
 static void load_synthetic(Context& c, uint64_t nsnps, uint32_t nsamples, int npop, const double* freq,
@@ -2193,6 +2236,22 @@ int pcaone_gpu_load_bed_device(pcaone_gpu_ctx* ctx, const void* dev_packed, uint
     if (src_pitch < ((uint64_t)nsamples + 3) / 4) throw Error(PCAONE_E_ARG, "row pitch below (N+3)/4");
     pcaone::load_bed_device(c, dev_packed, src_pitch, nsnps, nsamples);
     PCAONE_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int pcaone_gpu_filter_maf(pcaone_gpu_ctx* ctx, double maf, uint64_t* nkept) {
+  return guarded(ctx, [&](Context& c) {
+    pcaone::need_data(c);
+    const int64_t nk = pcaone::filter_maf(c, maf);
+    if (nkept) *nkept = (uint64_t)nk;
+  });
+}
+
+int pcaone_gpu_kept_snps(pcaone_gpu_ctx* ctx, int64_t* idx) {
+  return guarded(ctx, [&](Context& c) {
+    pcaone::need_data(c);
+    if (!idx) throw Error(PCAONE_E_ARG, "null index buffer");
+    for (int64_t i = 0; i < c.M; ++i) idx[i] = c.kept.empty() ? i : c.kept[(size_t)i];
   });
 }
 

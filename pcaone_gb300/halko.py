@@ -30,11 +30,15 @@ class FileBed:
     the rows stay in pinned host memory and SNP blocks are streamed to the GPU;
     the window method's shuffle then follows permute_plink with ``buffer`` GB
     (the --buffer option) as the reference's out-of-core mode does.
+
+    ``maf`` (the --maf option) keeps the SNPs whose minor allele frequency
+    exceeds it (Data::filter_snps_resize_F, called by read_all at
+    FilePlink.cpp:61); ``keepSNPs`` then lists their rows in the file.
     """
 
     def __init__(self, prefix: Optional[str] = None, *, packed: Optional[np.ndarray] = None,
                  nsamples: Optional[int] = None, device: int = 0, verbose: int = 0,
-                 memory: Optional[float] = None, buffer: int = 2):
+                 memory: Optional[float] = None, buffer: int = 2, maf: float = 0.0):
         self.ctx = capi.Context(device, verbose)
         self.out_of_core = memory is not None
         budget = int(memory * (1 << 30)) if memory is not None else 0
@@ -58,8 +62,14 @@ class FileBed:
                 self.ctx.load_bed(packed, nsamples)
         else:
             raise ValueError("give a PLINK prefix or packed genotypes with nsamples")
+        self._finish_read(maf)
+
+    def _finish_read(self, maf: float):
+        if maf > 0:
+            self.ctx.filter_maf(maf)
         self.nsamples = self.ctx.nsamples
         self.nsnps = self.ctx.nsnps
+        self.keepSNPs = self.ctx.kept_snps() if maf > 0 else np.empty(0, dtype=np.int64)
         self._counts = None
 
     @property
@@ -83,10 +93,11 @@ class FilePgen(FileBed):
     """PLINK2 fileset on the GPU (src/FilePgen.hpp:13-40): the sample count from
     the .psam (lines not starting with '#'), hard calls from the .pgen (storage
     modes 0x01-0x04; variable-width files are decoded by pgenlib on the host and
-    given as ``genovecs``, rows of 2-bit ALT counts with 3 = missing)."""
+    given as ``genovecs``, rows of 2-bit ALT counts with 3 = missing); ``maf``
+    as for FileBed (FilePgen.cpp:53)."""
 
     def __init__(self, prefix: Optional[str] = None, *, genovecs: Optional[np.ndarray] = None,
-                 nsamples: Optional[int] = None, device: int = 0, verbose: int = 0):
+                 nsamples: Optional[int] = None, device: int = 0, verbose: int = 0, maf: float = 0.0):
         self.ctx = capi.Context(device, verbose)
         self.out_of_core = False
         if prefix is not None:
@@ -99,9 +110,7 @@ class FilePgen(FileBed):
             self.ctx.load_pgen_genovecs(genovecs, nsamples)
         else:
             raise ValueError("give a PLINK2 prefix or hard calls with nsamples")
-        self.nsamples = self.ctx.nsamples
-        self.nsnps = self.ctx.nsnps
-        self._counts = None
+        self._finish_read(maf)
 
 
 @dataclass

@@ -30,6 +30,7 @@ class RunOptions:
     noshuffle: bool = False
     scale: int = -9
     memory: float = 0.0  # -m GB: out-of-core (src/Cmd.cpp:218)
+    maf: float = 0.0     # --maf: SNP filter before the run (src/Cmd.cpp:220)
     extra: dict = field(default_factory=dict)
 
     @property
@@ -75,6 +76,8 @@ def parse_options(opts) -> RunOptions:
             next(it)
         elif a in ("-m", "--memory"):
             o.memory = float(next(it))
+        elif a == "--maf":
+            o.maf = float(next(it))
         else:
             raise ValueError(f"option {a} not handled")
     o.oversamples = max(o.oversamples, o.k)
@@ -93,20 +96,23 @@ class GoldenCase:
     ref: dict
 
 
-def golden_cases(out_of_core: bool = False):
-    """PLINK fixtures (packed genotypes): the in-core runs, or with
-    out_of_core the reference's -m runs."""
+def golden_cases(out_of_core: bool = False, maf: bool = False):
+    """PLINK fixtures (packed genotypes): the in-core runs, with out_of_core
+    the reference's -m runs, with maf the --maf runs (every row of the file in
+    ``packed`` and nsnps; ref["keep"] the kept rows, ref["meta"][1] their
+    number)."""
     out = []
     for path in sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz"))):
         z = np.load(path)
         if "packed" not in z.files:
             continue
         opts = parse_options(json.loads(str(z["options"])))
-        if (opts.memory > 0) != out_of_core:
+        if (opts.memory > 0) != out_of_core or (opts.maf > 0) != maf:
             continue
         ref = {k: z[k] for k in z.files if k not in ("packed", "options")}
         meta = ref["meta"]
-        out.append(GoldenCase(os.path.basename(path)[:-4], z["packed"], int(meta[0]), int(meta[1]), opts, ref))
+        packed = z["packed"]
+        out.append(GoldenCase(os.path.basename(path)[:-4], packed, int(meta[0]), int(packed.shape[0]), opts, ref))
     return out
 
 
@@ -158,7 +164,7 @@ def pgen_image(genovec: np.ndarray, nsamples: int) -> bytes:
 
 
 def golden_case(name: str) -> GoldenCase:
-    for c in golden_cases() + golden_cases(out_of_core=True):
+    for c in golden_cases() + golden_cases(out_of_core=True) + golden_cases(maf=True):
         if c.name == name:
             return c
     raise KeyError(name)

@@ -8,6 +8,7 @@ tests never run this):
     python tests/golden/make_golden.py --eigs-only   # only tests/golden/eigs/
     python tests/golden/make_golden.py --ooc-only    # only the out-of-core (-m) cases
     python tests/golden/make_golden.py --pgen-only   # only the PLINK2 .pgen cases
+    python tests/golden/make_golden.py --maf-only    # only the --maf cases
 
 Each case draws a seeded synthetic PLINK fileset (pcaone_gb300.synthetic),
 runs the reference's RSVD operators through oracle/_ref/ref_driver with the
@@ -57,6 +58,18 @@ CASES = {
     # EMU on the single-pass method
     "em_ssvd": (dict(nsamples=160, nsnps=1200, npop=3, fst=0.1, seed=7, mcar=0.08),
                 ["-d", "1", "--emu", "--maxiter", "5", "--maxp", "3", "-k", "2"]),
+}
+
+# --maf: Data::filter_snps_resize_F drops the SNPs with minor allele frequency
+# at or below the bound before anything else (src/FilePlink.cpp:61); the
+# fixture keeps every row of the file, and keep.npy lists the kept ones
+MAF_CASES = {
+    # ancestral frequencies from 0.02, so that about a fifth of the SNPs go
+    "maf_wsvd_n301": (dict(nsamples=301, nsnps=2400, npop=3, fst=0.1, seed=51, mcar=0.01, anc_range=(0.02, 0.5),
+                           pad_garbage=True),
+                      ["-d", "2", "-k", "4", "--maxp", "6", "-w", "16", "--maf", "0.1"]),
+    "maf_em_ssvd_n203": (dict(nsamples=203, nsnps=1500, npop=3, fst=0.1, seed=52, mcar=0.05, anc_range=(0.02, 0.5)),
+                         ["-d", "1", "--emu", "--maxiter", "5", "--maxp", "4", "-k", "3", "--maf", "0.08"]),
 }
 
 # Out-of-core runs (-m GB): the reference streams blocks from the .bed file;
@@ -176,6 +189,8 @@ def run_case(name: str, model_kw: dict, opts: list) -> dict:
                                          dtype=np.uint8)
         if os.path.exists(os.path.join(out, "perm.npy")):
             res["perm"] = np.load(os.path.join(out, "perm.npy"))
+        if os.path.exists(os.path.join(out, "keep.npy")):
+            res["keep"] = np.load(os.path.join(out, "keep.npy"))
     res["packed"] = packed
     res["options"] = np.array(json.dumps(opts))
     return res
@@ -279,6 +294,12 @@ def main() -> None:
             np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
             print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"])
         return
+    if "--maf-only" in sys.argv:
+        for name, (mkw, opts) in MAF_CASES.items():
+            res = run_case(name, mkw, opts)
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+            print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "kept", len(res["keep"]), "S=", res["S"])
+        return
     if "--ooc-only" in sys.argv:
         for name, (mkw, opts) in OOC_CASES.items():
             res = run_ooc_case(name, mkw, opts)
@@ -305,6 +326,10 @@ def main() -> None:
         res = run_ooc_case(name, mkw, opts)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
         print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "S=", res["S"])
+    for name, (mkw, opts) in MAF_CASES.items():
+        res = run_case(name, mkw, opts)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+        print(name, "N=%d M=%d" % (res["meta"][0], res["meta"][1]), "kept", len(res["keep"]), "S=", res["S"])
     for name in EIGS_CASES:
         run_eigs_case(name)
 

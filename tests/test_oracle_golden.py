@@ -207,3 +207,39 @@ def test_pgen_hard_calls_as_plink1_codes(case):
     assert np.max(np.abs(op.S ** 2 - S ** 2) / S ** 2) < 1e-9
     assert np.max(np.abs(align_signs(op.U, case.ref["U"]) - case.ref["U"])) < 1e-8
     assert np.max(np.abs(align_signs(op.V, case.ref["V"]) - case.ref["V"])) < 1e-8
+
+
+# ---- --maf: Data::filter_snps_resize_F before the run ----
+MAF = golden_cases(maf=True)
+
+
+@pytest.mark.parametrize("case", MAF, ids=[c.name for c in MAF])
+def test_maf_filter_matches_reference(case):
+    """The kept rows (keepSNPs), their allele frequencies, decoded matrix,
+    shuffle and PCs equal the reference's --maf run."""
+    F_all = H.allele_freq(H.bed_counts(case.packed, case.nsamples))
+    keep = H.maf_keep(F_all, case.opts.maf)
+    assert np.array_equal(keep, case.ref["keep"])
+    assert 0 < keep.size < case.nsnps and keep.size == int(case.ref["meta"][1])
+    assert np.array_equal(F_all[keep], case.ref["F"])
+    packed = case.packed[keep]
+    G0, _ = H.decode_centered(packed, case.nsamples, case.ref["F"])
+    assert hashlib.sha256(np.asfortranarray(G0).tobytes(order="F")).digest() == bytes(case.ref["G0_sha256"])
+    o = case.opts
+    if o.perm:
+        assert np.array_equal(H.shuffle_columns(keep.size), case.ref["perm"])
+    d = H.OracleData(packed, case.nsamples, emu=o.emu, perm=o.perm, seed=o.seed, bands=o.bands, rand=o.rand,
+                     svd_t=o.svd, omega0=case.ref["Omg0"])
+    op = H.run_pca_with_halko(d, o.k, o.oversamples, maxp=o.maxp, tol=o.tol, maxiter=o.maxiter, tolem=o.tolem)
+    if o.emu:
+        assert op.em_iters == int(case.ref["meta"][2])
+    S = case.ref["S"]
+    assert np.max(np.abs(op.S ** 2 - S ** 2) / S ** 2) < 1e-9
+    assert np.max(np.abs(align_signs(op.U, case.ref["U"]) - case.ref["U"])) < 1e-8
+    assert np.max(np.abs(align_signs(op.V, case.ref["V"]) - case.ref["V"])) < 1e-8
+
+
+def test_maf_keep_boundaries():
+    """MAF(F) = min(F, 1 - F) must exceed the bound strictly (Data.cpp:95)."""
+    F = np.array([0.0, 0.1, 0.9, 0.10000000000000002, 0.5, 0.95, 1.0, 0.3])
+    assert H.maf_keep(F, 0.1).tolist() == [3, 4, 7]
